@@ -1,0 +1,267 @@
+/*
+ * chl.h - C ABI of the GB300 canonical hub labeling (CHL) engine.
+ *
+ * The reference (qingdo/plant) exposes its construction and query path as a
+ * header-only C++ API in namespace `hl` plus the `hhl` command line.  Every
+ * entry point below replaces one piece of that API; the comment above each
+ * one names the reference interface it stands in for (file:line, relative to
+ * the reference project root).
+ *
+ * Conventions
+ *  - Every function returns an int status (CHL_OK on success).  No function
+ *    calls exit() or abort(); bad input is reported as CHL_ERR_FORMAT or
+ *    CHL_ERR_INVALID, unreadable files as CHL_ERR_IO.
+ *  - Vertex ids are uint32, 0-based.  Hubs stored in labels are RANKS (the
+ *    position of the hub vertex in the order), exactly as in the reference's
+ *    label file.  Distances are non-negative int32; "no path" is reported as
+ *    CHL_INFTY (2147483647), the reference's `infty`.
+ *  - Handles are opaque and owned by the caller; free them with chl_*_free.
+ *    Mutating calls on one handle must not run concurrently.
+ *    chl_query_batch may run concurrently on distinct streams.
+ *  - The engine runs on the current CUDA device.  There is no CPU fallback:
+ *    if no device is usable, GPU entry points return CHL_ERR_CUDA.
+ */
+#ifndef CHL_H
+#define CHL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CHL_INFTY 2147483647
+
+enum chl_status {
+    CHL_OK = 0,
+    CHL_ERR_IO = 1,       /* file cannot be opened / read / written          */
+    CHL_ERR_FORMAT = 2,   /* no parser accepts the file                      */
+    CHL_ERR_OOM = 3,      /* host or device allocation failed                */
+    CHL_ERR_TIMEOUT = 4,  /* a bounded device wait gave up                   */
+    CHL_ERR_INVALID = 5,  /* bad argument (null, out of range, inconsistent) */
+    CHL_ERR_CUDA = 6      /* a CUDA runtime call failed / no device          */
+};
+
+typedef struct chl_graph chl_graph;
+typedef struct chl_labels chl_labels;
+typedef struct chl_server chl_server;
+
+/* Human-readable text for a status code (static storage). */
+const char *chl_status_str(int status);
+/* Text of the last CUDA / device-side error seen by this thread. */
+const char *chl_last_error(void);
+
+/* ------------------------------------------------------------------ graph */
+
+/* Replaces hl::Graph::read(char*, bool undirected)
+ * (shared_memory/graph.hpp:327-335): tries DIMACS, METIS, SNAP, then the
+ * `u v w` edge list, with the same acceptance rules, and builds adjacency
+ * with the same duplicate / direction merge as Graph::init_arcs
+ * (shared_memory/graph.hpp:103-153). */
+int chl_graph_load(const char *path, int undirected, chl_graph **out);
+
+/* Replaces hl::Graph::set_n + add_arc + finalize
+ * (shared_memory/graph.hpp:349-353): builds a graph from k arcs
+ * (src[i] -> dst[i], length len[i]); when `undirected` is non-zero every arc
+ * is also added in the opposite direction, as add_tmp_arc does. */
+int chl_graph_from_arcs(uint32_t n, size_t k, const uint32_t *src,
+                        const uint32_t *dst, const int32_t *len,
+                        int undirected, chl_graph **out);
+
+/* Replaces hl::Graph::write (shared_memory/graph.hpp:338-343) for the
+ * forward arcs; used to hand generated graphs to other tools. */
+int chl_graph_write_dimacs(const chl_graph *g, const char *path);
+
+/* Replaces Graph::get_n / get_m (shared_memory/graph.hpp:313-314). */
+uint32_t chl_graph_n(const chl_graph *g);
+uint64_t chl_graph_m(const chl_graph *g);
+/* Number of distinct forward (out) arcs after init_arcs merging. */
+uint64_t chl_graph_out_arcs(const chl_graph *g);
+/* 1 if the in-adjacency equals the out-adjacency (an undirected graph). */
+int chl_graph_symmetric(const chl_graph *g);
+/* Replaces Graph::get_degree(v) (shared_memory/graph.hpp:324): out + in. */
+uint32_t chl_graph_degree(const chl_graph *g, uint32_t v);
+/* Copy out the adjacency of v in direction `forward` (1 = out-arcs, as
+ * Graph::begin(v, true)); returns the count in *cnt.  heads/lens may be
+ * NULL to query the count. */
+int chl_graph_arcs(const chl_graph *g, uint32_t v, int forward,
+                   uint32_t *heads, int32_t *lens, uint32_t cap,
+                   uint32_t *cnt);
+void chl_graph_free(chl_graph *g);
+
+/* Seeded synthetic generators (no reference counterpart; they stand in for
+ * the missing public datasets).  Both return an undirected graph built as
+ * if its DIMACS file (both arc directions listed) had been read.
+ *   grid: rows x cols 4-neighbour grid, `del_frac` of edges deleted, largest
+ *         component kept, `diag_frac` x n diagonal shortcuts, lengths
+ *         uniform in [wmin, wmax], plus `highways` long edges between
+ *         vertices at most `hw_steps` grid steps apart with length
+ *         round(hw_factor x Manhattan distance).
+ *   rmat: 2^scale vertices, ef * 2^scale edges drawn with quadrant
+ *         probabilities (a, b, c, 1-a-b-c), symmetrised, self loops and
+ *         duplicates removed, unit lengths. */
+int chl_gen_grid(uint32_t rows, uint32_t cols, double del_frac,
+                 double diag_frac, int32_t wmin, int32_t wmax,
+                 uint32_t highways, uint32_t hw_steps, double hw_factor,
+                 uint64_t seed, chl_graph **out);
+int chl_gen_rmat(uint32_t scale, uint32_t ef, double a, double b, double c,
+                 uint64_t seed, chl_graph **out);
+
+/* ------------------------------------------------------------------ order */
+
+/* Replaces hl::Order::read (shared_memory/ordering.hpp:52-67): first value
+ * n, then n vertex ids; order[i] is the vertex of rank i.  *order is
+ * allocated with malloc; free it with chl_order_free. */
+int chl_order_load(const char *path, uint32_t **order, uint32_t *n);
+/* Replaces hl::Order::write (shared_memory/ordering.hpp:37-49). */
+int chl_order_write(const char *path, const uint32_t *order, uint32_t n);
+void chl_order_free(uint32_t *order);
+
+/* GPU plain orderings.  The reference takes its order from outside tools
+ * (distributed_memory/degree.cpp:62-67 for degree; an external betweenness
+ * tool for road graphs).  Both write n = chl_graph_n(g) entries to `order`.
+ *   degree: degree descending, ties broken by a seeded random permutation.
+ *   betweenness: Brandes dependencies summed over `sources` seeded source
+ *   vertices (forward shortest paths), descending, same tie break. */
+int chl_order_degree(const chl_graph *g, uint64_t seed, uint32_t *order);
+int chl_order_betweenness(const chl_graph *g, uint32_t sources,
+                          uint64_t seed, uint32_t *order);
+
+/* ------------------------------------------------------------------ build */
+
+enum chl_build_mode {
+    CHL_MODE_HYBRID = 0, /* PLaNT trees until the tree/label ratio passes ps,
+                            then pruned supersteps                       */
+    CHL_MODE_GLL = 1,    /* pruned supersteps from the first root        */
+    CHL_MODE_PLANT = 2   /* PLaNT trees only, pruned by committed labels */
+};
+
+typedef struct chl_build_opts {
+    int32_t mode;         /* chl_build_mode                                  */
+    double sf;            /* superstep label budget factor (hhl -s), 0 = auto */
+    double ps;            /* phase switch ratio tree/label (hhl -ps)          */
+    int32_t autotune;     /* 1: pick superstep growth from graph statistics   */
+    int32_t use_graphs;   /* 1: capture the per-superstep kernel chain in a
+                             CUDA graph                                       */
+    int32_t verbose;      /* 1: print the reference's summary line            */
+    uint32_t first_superstep; /* roots in the first superstep, 0 = auto       */
+    double growth;        /* superstep growth factor, 0 = auto                */
+    uint32_t max_warps;   /* cap on concurrent trees, 0 = auto                */
+    uint32_t reserved[8];
+} chl_build_opts;
+
+/* Fill opts with the defaults (hybrid, sf 32, ps 1024, autotune on). */
+void chl_build_opts_default(chl_build_opts *opts);
+
+typedef struct chl_build_stats {
+    double build_ms;       /* device time of the whole build (CUDA events)  */
+    double tree_ms;        /* tree kernels                                  */
+    double sort_ms;        /* sort of new labels                            */
+    double commit_ms;      /* merge into the committed label arrays         */
+    double h2d_ms;         /* graph/order upload                            */
+    uint64_t labels;       /* total label entries (both sides)              */
+    uint64_t visits;       /* vertices settled over all trees               */
+    uint64_t label_reads;  /* label entries read by prune tests             */
+    uint64_t arcs;         /* arcs relaxed                                  */
+    uint32_t supersteps;
+    uint32_t plant_roots;  /* roots built as un-pruned PLaNT trees          */
+    uint64_t tree_launches;
+    uint64_t kernel_launches;
+    double avg_label;
+} chl_build_stats;
+
+/* Replaces hl::run_paraPLL (shared_memory/akiba.hpp:132-217) and the hybrid
+ * hl::run (distributed_memory/akiba.hpp:190-510): builds canonical labels of
+ * g for `order` (n ranks, n must equal chl_graph_n(g)).  The result lives in
+ * device memory. */
+int chl_build(const chl_graph *g, const uint32_t *order, uint32_t n,
+              const chl_build_opts *opts, chl_labels **out);
+/* Statistics of the build that produced `l`. */
+int chl_build_get_stats(const chl_labels *l, chl_build_stats *stats);
+
+/* ----------------------------------------------------------------- labels */
+
+/* Replaces hl::Labeling::write (shared_memory/labeling.hpp:167-183):
+ * byte-identical text layout. */
+int chl_labels_write(const chl_labels *l, const char *path);
+/* Replaces hl::Labeling::read (shared_memory/labeling.hpp:186-208); the
+ * labels are uploaded to the device. */
+int chl_labels_read(const char *path, chl_labels **out);
+/* Replaces Labeling::get_avg (shared_memory/labeling.hpp:153-158). */
+double chl_avg_label(const chl_labels *l);
+uint32_t chl_labels_n(const chl_labels *l);
+uint64_t chl_labels_total(const chl_labels *l);
+/* Copy out L(v, side): hub ranks and distances, ascending by hub.  Either
+ * array may be NULL to query the size in *cnt. */
+int chl_labels_get(const chl_labels *l, uint32_t v, int side, uint32_t *hubs,
+                   int32_t *dists, uint32_t cap, uint32_t *cnt);
+/* Copy all labels to host CSR arrays: off has 2n+1 entries (index 2v+side),
+ * hubs/dists have chl_labels_total entries. */
+int chl_labels_export(const chl_labels *l, uint64_t *off, uint32_t *hubs,
+                      int32_t *dists);
+/* Build a labels handle from host CSR arrays (same layout as export). */
+int chl_labels_import(uint32_t n, const uint64_t *off, const uint32_t *hubs,
+                      const int32_t *dists, chl_labels **out);
+/* Per-vertex hub frequency: freq[v] = number of label entries (both sides)
+ * whose hub is rank(v).  Training target of the learned ranking. */
+int chl_labels_hub_freq(const chl_labels *l, const uint32_t *order,
+                        uint32_t *freq);
+void chl_labels_free(chl_labels *l);
+
+/* ------------------------------------------------------------------ query */
+
+/* Replaces hl::Labeling::query(u, v, f=true)
+ * (shared_memory/labeling.hpp:56-65) over a batch, as batchLocalQuery does
+ * (distributed_memory/query_funcs.hpp:23-30): out[i] = d(pairs[2i] ->
+ * pairs[2i+1]), CHL_INFTY if the labels share no hub.  pairs/out are HOST
+ * pointers (copied in and out on `stream`, a cudaStream_t or NULL). */
+int chl_query_batch(const chl_labels *l, const uint32_t *pairs, size_t k,
+                    int32_t *out, void *stream);
+/* Same, with DEVICE pointers; returns after the launch (asynchronous). */
+int chl_query_batch_device(const chl_labels *l, const uint32_t *d_pairs,
+                           size_t k, int32_t *d_out, void *stream);
+/* Replaces hl::generate_query (distributed_memory/query.hpp:43-51) with a
+ * seeded generator: k uniform pairs over [0, range). */
+int chl_query_generate(uint32_t *pairs, size_t k, uint32_t range,
+                       uint64_t seed);
+/* Replaces hl::load_query (distributed_memory/query.hpp:18-32): `u v` per
+ * line.  *pairs is malloc'ed (free with chl_order_free). */
+int chl_query_load(const char *path, uint32_t **pairs, size_t *k);
+
+/* ----------------------------------------------------------------- server */
+
+/* Continuous-batching query server (no reference counterpart; its
+ * single-node limit is query mode 1, distributed_memory/query.hpp:82-91).
+ * Requests are admitted while slots and device memory allow, merged into
+ * one launch per cycle, and completed asynchronously. */
+typedef struct chl_server_opts {
+    uint32_t max_inflight_pairs; /* device slots for pairs (admission bound) */
+    uint32_t max_requests;       /* request table size                       */
+    uint32_t max_batch_pairs;    /* pairs merged into one launch             */
+    uint32_t reserved[5];
+} chl_server_opts;
+
+void chl_server_opts_default(chl_server_opts *opts);
+int chl_server_create(const chl_labels *l, const chl_server_opts *opts,
+                      chl_server **out);
+/* Submit k pairs (host memory, copied at admission).  Returns CHL_OK and a
+ * request id, or CHL_ERR_OOM if the request can never fit. Blocks while the
+ * server is full. */
+int chl_server_submit(chl_server *s, const uint32_t *pairs, size_t k,
+                      uint64_t *req_id);
+/* Wait for request `req_id`; copies its k answers into out and releases
+ * it.  timeout_ms < 0 waits forever; CHL_ERR_TIMEOUT if it expires. */
+int chl_server_wait(chl_server *s, uint64_t req_id, int32_t *out,
+                    double timeout_ms, double *latency_ms);
+/* Drive the server loop once (admit + launch + complete); returns the
+ * number of requests completed.  The server also runs its own thread. */
+int chl_server_stats(chl_server *s, uint64_t *launches, uint64_t *pairs,
+                     uint64_t *requests);
+void chl_server_free(chl_server *s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CHL_H */

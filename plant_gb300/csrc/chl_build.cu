@@ -1,0 +1,1034 @@
+// Canonical hub label construction on one GPU.
+//
+// Reference path being replaced:
+//   hl::run_paraPLL            shared_memory/akiba.hpp:132-217  (GLL supersteps)
+//   hl::Akiba::iteration_gll   shared_memory/akiba.hpp:65-125   (pruned Dijkstra)
+//   hl::Akiba::plant           distributed_memory/akiba.hpp:52-104 (PLaNT tree)
+//   BasicDijkstra::update_wo_prune distributed_memory/dijkstra.hpp:56-78
+//   hl::run (hybrid switch)    distributed_memory/akiba.hpp:290-336, 479-480
+//   Labeling::sort / clean_cover shared_memory/labeling.hpp:222-256, 78-88
+//
+// Design (one process, one GPU):
+//  * Roots are taken in rank order in supersteps.  A persistent kernel runs
+//    one tree per warp; warps pull roots from a device counter until the
+//    superstep's label budget (sf * n, the reference's label_limit) is spent.
+//  * Every tree prunes only against labels committed by EARLIER supersteps
+//    (read-only during the kernel), so a superstep's output does not depend
+//    on warp scheduling.
+//  * PLaNT trees track the "via a higher-ranked vertex" flag exactly as
+//    update_wo_prune does and emit canonical labels directly; GLL trees skip
+//    higher-ranked vertices and emit a superset that the clean kernel
+//    filters with the reference's clean_cover rule.
+//  * New labels are sorted by (vertex, side, hub) with a stable radix sort
+//    and merged into the committed CSR (double-buffered) in one pass.
+//  * Weighted graphs use an indexed binary heap whose top kHeapSmem slots
+//    live in shared memory; unit-length graphs use a FIFO (BFS order).
+#include "chl_dev.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace chl {
+
+namespace {
+
+constexpr uint32_t kInf = 0xFFFFFFFFu;
+constexpr int kHeapSmem = 128;      // heap slots kept in shared memory per warp
+constexpr int kWarpsPerBlock = 4;
+constexpr int kStage = 32;          // label staging entries per warp
+
+struct BuildCtl {
+    unsigned long long next_root;   // root fetch counter (absolute rank)
+    unsigned long long nlab;        // labels emitted this superstep
+    unsigned long long visits;
+    unsigned long long label_reads;
+    unsigned long long arcs;
+    unsigned long long n_keep;      // labels surviving the clean pass
+    unsigned int overflow;
+    unsigned int err;               // 1: distance overflow, 2: workspace bound
+    unsigned long long max_ratio_num;  // (tree, labels) of the worst root
+    unsigned long long max_ratio_den;
+};
+
+struct TreeArgs {
+    uint32_t n;
+    int sides;                      // 1: symmetric graph, one label side stored
+    const uint64_t *g_off[2];       // [f]: arcs traversed by trees of side f
+    const uint2 *g_arc[2];          // (head, length)
+    const uint32_t *g_head[2];      // heads only (unit-length graphs)
+    const uint32_t *order;
+    const uint32_t *rank;
+    const uint64_t *l_off;          // committed labels, index lidx(v, side)
+    const uint2 *l_ent;
+    uint32_t r0, r_end;
+    unsigned long long budget;
+    int hub_bits;
+    uint64_t *out_key;
+    uint32_t *out_val;
+    unsigned long long out_cap;
+    uint32_t *tree_size;            // per root (index r - r0), sides summed
+    uint32_t *tree_labels;
+    uint32_t *ws_key;               // per warp slot, n entries each
+    uint32_t *ws_vis;
+    uint32_t *ws_pos;
+    uint64_t *ws_heap;
+    BuildCtl *ctl;
+    uint32_t rcap;                  // root label entries staged in smem
+};
+
+__device__ __forceinline__ uint32_t lidx(uint32_t v, int side, int sides) {
+    return sides == 1 ? v : 2 * v + (uint32_t)side;
+}
+
+// --------------------------------------------------------------- heap
+// Indexed binary min-heap on (key << 32 | vertex).  Slot i lives in shared
+// memory when i < kHeapSmem, else in the warp's global overflow array.
+struct Heap {
+    uint64_t *sh;
+    uint64_t *gh;
+    uint32_t *pos;
+    uint32_t size;
+    uint32_t cap;                   // kHeapSmem + overflow slots
+
+    __device__ __forceinline__ uint64_t *slot(uint32_t i) const {
+        return i < (uint32_t)kHeapSmem ? sh + i : gh + (i - kHeapSmem);
+    }
+    __device__ void sift_up(uint32_t i, uint64_t e) {
+        while (i > 0) {
+            uint32_t p = (i - 1) >> 1;
+            uint64_t pe = *slot(p);
+            if (pe <= e) break;
+            *slot(i) = pe;
+            pos[(uint32_t)pe] = i;
+            i = p;
+        }
+        *slot(i) = e;
+        pos[(uint32_t)e] = i;
+    }
+    __device__ bool push(uint32_t v, uint32_t key) {
+        if (size >= cap) return false;
+        sift_up(size++, ((uint64_t)key << 32) | v);
+        return true;
+    }
+    __device__ void decrease(uint32_t v, uint32_t key) {
+        sift_up(pos[v], ((uint64_t)key << 32) | v);
+    }
+    __device__ uint64_t pop() {
+        uint64_t top = *slot(0);
+        uint32_t n = --size;
+        if (n > 0) {
+            uint64_t e = *slot(n);
+            uint32_t i = 0;
+            while (true) {
+                uint32_t c = 2 * i + 1;
+                if (c >= n) break;
+                uint64_t ce = *slot(c);
+                if (c + 1 < n) {
+                    uint64_t c2 = *slot(c + 1);
+                    if (c2 < ce) {
+                        ce = c2;
+                        ++c;
+                    }
+                }
+                if (e <= ce) break;
+                *slot(i) = ce;
+                pos[(uint32_t)ce] = i;
+                i = c;
+            }
+            *slot(i) = e;
+            pos[(uint32_t)e] = i;
+        }
+        return top;
+    }
+};
+
+// ---------------------------------------------------------- prune test
+// Does some committed hub h give rootlabel[h] + L(u)[h] <= d?  The root
+// label (sorted by hub) is searched by every lane for its own entry of L(u);
+// L(u) is streamed 32 entries per step (coalesced 256-byte reads).  Returns
+// the number of entries read in *nread.
+__device__ __forceinline__ bool prune_test(const uint32_t *rh, const uint32_t *rd,
+                                           int rstride, uint32_t R, const uint2 *lu,
+                                           uint32_t Lu, uint32_t d, uint32_t &nread) {
+    const uint32_t lane = lane_id();
+    for (uint32_t base = 0; base < Lu; base += 32) {
+        uint32_t k = base + lane;
+        bool hit = false;
+        if (k < Lu) {
+            uint2 e = lu[k];
+            uint32_t lo = 0, hi = R;
+            while (lo < hi) {
+                uint32_t mid = (lo + hi) >> 1;
+                if (rh[(size_t)mid * rstride] < e.x) lo = mid + 1;
+                else hi = mid;
+            }
+            if (lo < R && rh[(size_t)lo * rstride] == e.x &&
+                rd[(size_t)lo * rstride] + e.y <= d)
+                hit = true;
+        }
+        if (__any_sync(kFull, hit)) {
+            nread += min(32u, Lu - base) + base;
+            return true;
+        }
+    }
+    nread += Lu;
+    return false;
+}
+
+// ------------------------------------------------------------ tree kernel
+
+template <bool UNIT, bool PLANT>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+tree_kernel(TreeArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
+    const uint32_t slot = blockIdx.x * kWarpsPerBlock + wib;
+    const size_t per_warp = (size_t)a.rcap * 8 + (UNIT ? 0 : kHeapSmem * 8) + kStage * 12;
+    unsigned char *base = smem + wib * per_warp;
+    uint32_t *s_rh = (uint32_t *)base;
+    uint32_t *s_rd = s_rh + a.rcap;
+    uint64_t *s_heap = (uint64_t *)(base + (size_t)a.rcap * 8);
+    uint64_t *s_sk = (uint64_t *)(base + (size_t)a.rcap * 8 + (UNIT ? 0 : kHeapSmem * 8));
+    uint32_t *s_sv = (uint32_t *)(s_sk + kStage);
+
+    uint32_t *key = a.ws_key + (size_t)slot * a.n;
+    uint32_t *vis = a.ws_vis + (size_t)slot * a.n;
+    Heap heap;
+    if (!UNIT) {
+        heap.sh = s_heap;
+        heap.gh = a.ws_heap + (size_t)slot * a.n;
+        heap.pos = a.ws_pos + (size_t)slot * a.n;
+        heap.size = 0;
+        heap.cap = a.n + kHeapSmem;
+    }
+    uint32_t nstage = 0;
+    unsigned long long c_vis = 0, c_reads = 0, c_arcs = 0;
+
+    auto flush = [&]() {
+        unsigned long long b = 0;
+        if (lane == 0) b = atomicAdd(&a.ctl->nlab, (unsigned long long)nstage);
+        b = __shfl_sync(kFull, b, 0);
+        __syncwarp();
+        if (lane < nstage) {
+            unsigned long long p = b + lane;
+            if (p < a.out_cap) {
+                a.out_key[p] = s_sk[lane];
+                a.out_val[p] = s_sv[lane];
+            } else {
+                a.ctl->overflow = 1;
+            }
+        }
+        __syncwarp();
+        nstage = 0;
+    };
+
+    while (true) {
+        uint32_t r = kInf;
+        if (lane == 0) {
+            unsigned long long used = *(volatile unsigned long long *)&a.ctl->nlab;
+            if (used < a.budget) {
+                unsigned long long t = atomicAdd(&a.ctl->next_root, 1ull);
+                if (t < a.r_end) r = (uint32_t)t;
+            }
+        }
+        r = __shfl_sync(kFull, r, 0);
+        if (r == kInf) break;
+        uint32_t t_size = 0, t_lab = 0;
+        const uint32_t v = a.order[r];
+        for (int sd = 0; sd < a.sides; ++sd) {
+            // Trees of side f walk arcs of direction f and add (r, d) to
+            // L(u, !f) (Akiba::iteration_gll's `forward`).  The reference
+            // runs side false first, then side true.
+            const int f = (a.sides == 1) ? 1 : sd;
+            const uint64_t *goff = a.g_off[f];
+            const uint2 *garc = a.g_arc[f];
+            const uint32_t *ghead = a.g_head[f];
+            // stage L(v, f)
+            const uint32_t ridx = lidx(v, f, a.sides);
+            const uint64_t rb = a.l_off[ridx], re = a.l_off[ridx + 1];
+            const uint32_t R = (uint32_t)(re - rb);
+            const uint32_t *rh, *rd;
+            int rstride;
+            if (R <= a.rcap) {
+                for (uint32_t k = lane; k < R; k += 32) {
+                    uint2 e = a.l_ent[rb + k];
+                    s_rh[k] = e.x;
+                    s_rd[k] = e.y;
+                }
+                rh = s_rh;
+                rd = s_rd;
+                rstride = 1;
+            } else {
+                rh = (const uint32_t *)(a.l_ent + rb);
+                rd = rh + 1;
+                rstride = 2;
+            }
+            // root: distance 0, not via a higher-ranked vertex
+            if (lane == 0) {
+                key[v] = 1u;
+                vis[0] = v;
+                if (!UNIT) heap.push(v, 1u);
+            }
+            __syncwarp();
+            uint32_t nvis = 1, qh = 0;
+            int ql = 1;   // queued vertices with no higher-ranked ancestor
+            while (true) {
+                uint32_t u, k;
+                if (UNIT) {
+                    if (qh >= nvis) break;
+                    u = vis[qh++];
+                    k = key[u];
+                } else {
+                    uint64_t top = 0;
+                    bool empty = false;
+                    if (lane == 0) {
+                        empty = heap.size == 0;
+                        if (!empty) top = heap.pop();
+                    }
+                    empty = __shfl_sync(kFull, empty, 0);
+                    if (empty) break;
+                    top = __shfl_sync(kFull, top, 0);
+                    u = (uint32_t)top;
+                    k = (uint32_t)(top >> 32);
+                }
+                ++t_size;
+                const uint32_t d = k >> 1;
+                const bool nonvia = k & 1u;
+                if (PLANT) {
+                    if (nonvia) --ql;
+                } else {
+                    if (a.rank[u] < r) continue;   // iteration_gll :92
+                }
+                bool pruned = false;
+                const uint32_t uidx = lidx(u, 1 - f, a.sides);
+                if (R > 0) {
+                    const uint64_t ub = a.l_off[uidx], ue = a.l_off[uidx + 1];
+                    uint32_t nr = 0;
+                    pruned = prune_test(rh, rd, rstride, R, a.l_ent + ub,
+                                        (uint32_t)(ue - ub), d, nr);
+                    c_reads += nr;
+                }
+                if (!pruned) {
+                    if (!PLANT || nonvia) {
+                        if (lane == 0) {
+                            s_sk[nstage] = ((uint64_t)uidx << a.hub_bits) | (uint64_t)(r - a.r0);
+                            s_sv[nstage] = d;
+                        }
+                        ++nstage;
+                        ++t_lab;
+                        if (nstage == kStage) flush();
+                    }
+                    const uint64_t ab = goff[u], ae = goff[u + 1];
+                    c_arcs += ae - ab;
+                    for (uint64_t e0 = ab; e0 < ae; e0 += 32) {
+                        const uint64_t e = e0 + lane;
+                        bool upd = false;
+                        uint32_t w = 0, nk = 0, old = kInf;
+                        if (e < ae) {
+                            uint32_t len;
+                            if (UNIT) {
+                                w = ghead[e];
+                                len = 1;
+                            } else {
+                                uint2 hl = garc[e];
+                                w = hl.x;
+                                len = hl.y;
+                            }
+                            const uint64_t dd64 = (uint64_t)d + len;
+                            if (dd64 < 0x7FFFFFFFull) {
+                                const uint32_t dd = (uint32_t)dd64;
+                                uint32_t nv = 1u;
+                                if (PLANT) nv = (nonvia && a.rank[w] >= r) ? 1u : 0u;
+                                nk = dd * 2u + nv;
+                                old = key[w];
+                                upd = nk < old;
+                                if (upd) key[w] = nk;
+                            } else {
+                                a.ctl->err = 1;   // the reference asserts dd < infty
+                            }
+                        }
+                        const bool fresh = upd && old == kInf;
+                        const uint32_t fm = __ballot_sync(kFull, fresh);
+                        if (fresh) {
+                            const uint32_t at = nvis + __popc(fm & lanemask_lt());
+                            if (at < a.n) vis[at] = w;
+                            else a.ctl->err = 2;
+                        }
+                        nvis = min(nvis + __popc(fm), a.n);
+                        if (PLANT) {
+                            int dq = 0;
+                            if (upd) dq = (int)(nk & 1u) - (old == kInf ? 0 : (int)(old & 1u));
+                            ql += __reduce_add_sync(kFull, dq);
+                        }
+                        if (!UNIT) {
+                            uint32_t um = __ballot_sync(kFull, upd);
+                            while (um) {
+                                const int src = __ffs(um) - 1;
+                                um &= um - 1;
+                                const uint32_t w_ = __shfl_sync(kFull, w, src);
+                                const uint32_t nk_ = __shfl_sync(kFull, nk, src);
+                                const uint32_t old_ = __shfl_sync(kFull, old, src);
+                                if (lane == 0) {
+                                    if (old_ == kInf) {
+                                        if (!heap.push(w_, nk_)) a.ctl->err = 2;
+                                    } else {
+                                        heap.decrease(w_, nk_);
+                                    }
+                                }
+                            }
+                        }
+                        __syncwarp();
+                    }
+                }
+                if (PLANT && ql == 0) break;   // plant :95 early exit
+            }
+            // reset the warp's workspace for the next tree
+            c_vis += t_size;
+            for (uint32_t k = lane; k < nvis; k += 32) key[vis[k]] = kInf;
+            if (!UNIT && lane == 0) heap.size = 0;
+            __syncwarp();
+        }
+        if (lane == 0) {
+            a.tree_size[r - a.r0] = t_size;
+            a.tree_labels[r - a.r0] = t_lab;
+        }
+    }
+    if (nstage) flush();
+    // counters (one atomic per warp)
+    if (lane == 0) {
+        atomicAdd(&a.ctl->visits, c_vis);
+        atomicAdd(&a.ctl->arcs, c_arcs);
+    }
+    if (lane == 0) atomicAdd(&a.ctl->label_reads, c_reads);
+}
+
+// ---------------------------------------------------------- commit chain
+
+// Count new labels per label list (sorted keys).
+__global__ void count_keys(const uint64_t *keys, const unsigned long long *d_n,
+                           unsigned long long cap, int hub_bits, uint32_t *cnt) {
+    unsigned long long n = *d_n;
+    if (n > cap) n = cap;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+         i < n; i += (unsigned long long)gridDim.x * blockDim.x)
+        atomicAdd(&cnt[keys[i] >> hub_bits], 1u);
+}
+
+// GLL clean (shared_memory/akiba.hpp:197-208 with Labeling::clean_cover,
+// shared_memory/labeling.hpp:78-88): a new label (h, d) of list (u, s) is
+// dropped if some hub h' < h appears in both the new L(u, s) and the new
+// L(order[h], !s) with d' + d'' <= d.  Only this superstep's labels take
+// part; earlier labels were already used for pruning.
+__global__ void clean_mark(const uint64_t *keys, const uint32_t *vals,
+                           const unsigned long long *d_n, unsigned long long cap,
+                           int hub_bits, uint32_t r0, const uint64_t *pre,
+                           const uint32_t *order, const uint32_t *rank, int sides,
+                           uint32_t *keep) {
+    unsigned long long n = *d_n;
+    if (n > cap) n = cap;
+    const uint64_t mask = (1ull << hub_bits) - 1;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+         i < n; i += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint64_t k = keys[i];
+        const uint32_t x = (uint32_t)(k >> hub_bits);
+        const uint32_t hrel = (uint32_t)(k & mask);
+        const uint32_t d = vals[i];
+        const uint32_t hv = order[r0 + hrel];
+        uint32_t y;
+        if (sides == 1) {
+            y = hv;
+        } else {
+            const uint32_t s = x & 1u;
+            y = 2 * hv + (1u - s);
+        }
+        uint64_t a = pre[x], ae = pre[x + 1];
+        uint64_t b = pre[y], be = pre[y + 1];
+        bool covered = false;
+        while (a < ae && b < be) {
+            const uint32_t ha = (uint32_t)(keys[a] & mask), hb = (uint32_t)(keys[b] & mask);
+            if (ha >= hrel || hb >= hrel) break;
+            if (ha == hb) {
+                if (vals[a] + vals[b] <= d) {
+                    covered = true;
+                    break;
+                }
+                ++a;
+                ++b;
+            } else if (ha < hb) {
+                ++a;
+            } else {
+                ++b;
+            }
+        }
+        keep[i] = covered ? 0u : 1u;
+    }
+}
+
+__global__ void compact_kept(const uint64_t *kin, const uint32_t *vin, const uint32_t *keep,
+                             const uint64_t *kpre, const unsigned long long *d_n,
+                             unsigned long long cap, uint64_t *kout, uint32_t *vout,
+                             unsigned long long *d_nkeep) {
+    unsigned long long n = *d_n;
+    if (n > cap) n = cap;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+         i < n; i += (unsigned long long)gridDim.x * blockDim.x) {
+        if (keep[i]) {
+            const uint64_t p = kpre[i];
+            kout[p] = kin[i];
+            vout[p] = vin[i];
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *d_nkeep = kpre[cap];
+}
+
+// new_off[x] = old_off[x] + pre[x]  (pre = exclusive scan of new counts)
+__global__ void merge_offsets(const uint64_t *old_off, const uint64_t *pre, uint64_t *new_off,
+                              uint32_t nl) {
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x <= nl; x += gridDim.x * blockDim.x)
+        new_off[x] = old_off[x] + pre[x];
+}
+
+// Copy every committed list to its new position (one warp per list).
+__global__ void copy_old_lists(const uint64_t *old_off, const uint2 *old_ent,
+                               const uint64_t *new_off, uint2 *new_ent, uint32_t nl) {
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t x = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); x < nl; x += warps) {
+        const uint64_t b = old_off[x], e = old_off[x + 1], nb = new_off[x];
+        for (uint64_t k = b + lane_id(); k < e; k += 32) new_ent[nb + (k - b)] = old_ent[k];
+    }
+}
+
+// Append the sorted new labels behind each list's committed part.
+__global__ void place_new(const uint64_t *keys, const uint32_t *vals,
+                          const unsigned long long *d_n, unsigned long long cap, int hub_bits,
+                          uint32_t r0, const uint64_t *pre, const uint64_t *old_off,
+                          const uint64_t *new_off, uint2 *new_ent) {
+    unsigned long long n = *d_n;
+    if (n > cap) n = cap;
+    const uint64_t mask = (1ull << hub_bits) - 1;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+         i < n; i += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint64_t k = keys[i];
+        const uint32_t x = (uint32_t)(k >> hub_bits);
+        const uint64_t dst = new_off[x] + (old_off[x + 1] - old_off[x]) + (i - pre[x]);
+        new_ent[dst] = make_uint2(r0 + (uint32_t)(k & mask), vals[i]);
+    }
+}
+
+// Largest tree/label ratio over the superstep's roots (hybrid switch rule,
+// distributed_memory/akiba.hpp:297-303), kept as an exact fraction.
+__global__ void ratio_max(const uint32_t *tsize, const uint32_t *tlab, const unsigned long long *next_root,
+                          uint32_t r0, uint32_t r_end, BuildCtl *ctl) {
+    unsigned long long r1 = *next_root;
+    if (r1 > r_end) r1 = r_end;
+    const uint32_t cnt = (uint32_t)(r1 - r0);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+        // pack ratio as a double's bits (positive doubles order like integers)
+        const double ratio = tlab[i] ? (double)tsize[i] / (double)tlab[i] : 1e300;
+        atomicMax(&ctl->max_ratio_num, (unsigned long long)__double_as_longlong(ratio));
+    }
+}
+
+// Longest label list (sizes the root-label staging of the next superstep).
+__global__ void max_list_len(const uint64_t *off, uint32_t nl, unsigned long long *out) {
+    unsigned long long mx = 0;
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < nl; x += gridDim.x * blockDim.x)
+        mx = max(mx, (unsigned long long)(off[x + 1] - off[x]));
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(kFull, mx, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, mx);
+}
+
+inline int bits_for(uint64_t x) {   // bits needed to represent values < x
+    int b = 0;
+    while (b < 64 && (1ull << b) < x) ++b;
+    return b < 1 ? 1 : b;
+}
+
+template <typename T>
+int dalloc(T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error(std::string("device allocation failed: ") + cudaGetErrorString(e));
+        return CHL_ERR_OOM;
+    }
+    return CHL_OK;
+}
+
+struct DevGraph {
+    uint64_t *off[2] = {nullptr, nullptr};
+    uint2 *arc[2] = {nullptr, nullptr};
+    uint32_t *head[2] = {nullptr, nullptr};
+    void release() {
+        for (int s = 0; s < 2; ++s) {
+            if (off[s] && (s == 0 || off[s] != off[0])) cudaFree(off[s]);
+            if (arc[s] && (s == 0 || arc[s] != arc[0])) cudaFree(arc[s]);
+            if (head[s] && (s == 0 || head[s] != head[0])) cudaFree(head[s]);
+            off[s] = nullptr;
+            arc[s] = nullptr;
+            head[s] = nullptr;
+        }
+    }
+};
+
+int upload_graph(const chl_graph *g, DevGraph &dg, cudaStream_t st) {
+    const int nsides = g->symmetric ? 1 : 2;
+    for (int s = 0; s < nsides; ++s) {
+        const int src = g->symmetric ? 1 : s;
+        const uint64_t m = g->off[src][g->n];
+        int rc = dalloc(&dg.off[s], (size_t)g->n + 1);
+        if (rc) return rc;
+        CHL_CUDA(cudaMemcpyAsync(dg.off[s], g->off[src].data(), ((size_t)g->n + 1) * 8,
+                                 cudaMemcpyHostToDevice, st));
+        if (g->unit) {
+            rc = dalloc(&dg.head[s], m);
+            if (rc) return rc;
+            CHL_CUDA(cudaMemcpyAsync(dg.head[s], g->head[src].data(), m * 4,
+                                     cudaMemcpyHostToDevice, st));
+        } else {
+            std::vector<uint2> pk(m);
+            for (uint64_t i = 0; i < m; ++i)
+                pk[i] = make_uint2(g->head[src][i], (uint32_t)g->len[src][i]);
+            rc = dalloc(&dg.arc[s], m);
+            if (rc) return rc;
+            CHL_CUDA(cudaMemcpy(dg.arc[s], pk.data(), m * 8, cudaMemcpyHostToDevice));
+        }
+    }
+    if (nsides == 1) {
+        dg.off[1] = dg.off[0];
+        dg.arc[1] = dg.arc[0];
+        dg.head[1] = dg.head[0];
+    }
+    return CHL_OK;
+}
+
+struct Build {
+    // sizes
+    uint32_t n = 0;
+    int sides = 1;
+    uint32_t nl = 0;       // number of label lists on the device
+    int hub_bits = 0;
+    int key_bits = 0;
+    // device buffers
+    DevGraph dg;
+    uint32_t *order = nullptr, *rank = nullptr;
+    uint64_t *off_a = nullptr, *off_b = nullptr;
+    uint2 *ent_a = nullptr, *ent_b = nullptr;
+    uint64_t ent_cap_a = 0, ent_cap_b = 0;
+    uint64_t *nk0 = nullptr, *nk1 = nullptr;
+    uint32_t *nv0 = nullptr, *nv1 = nullptr;
+    uint64_t new_cap = 0;
+    uint32_t *cnt = nullptr;
+    uint64_t *pre = nullptr;
+    uint32_t *keep = nullptr;
+    uint64_t *kpre = nullptr;
+    uint32_t *tsize = nullptr, *tlab = nullptr;
+    uint32_t *ws_key = nullptr, *ws_vis = nullptr, *ws_pos = nullptr;
+    uint64_t *ws_heap = nullptr;
+    BuildCtl *ctl = nullptr;
+    void *tmp = nullptr;
+    size_t tmp_bytes = 0;
+    cudaStream_t st = nullptr;
+    uint32_t warps = 0;
+    uint32_t rcap = 0;
+
+    ~Build() {
+        dg.release();
+        cudaFree(order);
+        cudaFree(rank);
+        cudaFree(off_a);
+        cudaFree(off_b);
+        cudaFree(ent_a);
+        cudaFree(ent_b);
+        cudaFree(nk0);
+        cudaFree(nk1);
+        cudaFree(nv0);
+        cudaFree(nv1);
+        cudaFree(cnt);
+        cudaFree(pre);
+        cudaFree(keep);
+        cudaFree(kpre);
+        cudaFree(tsize);
+        cudaFree(tlab);
+        cudaFree(ws_key);
+        cudaFree(ws_vis);
+        cudaFree(ws_pos);
+        cudaFree(ws_heap);
+        cudaFree(ctl);
+        cudaFree(tmp);
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+int grow_new(Build &b, uint64_t need) {
+    if (need <= b.new_cap) return CHL_OK;
+    uint64_t cap = std::max<uint64_t>(need, b.new_cap * 2);
+    cudaFree(b.nk0);
+    cudaFree(b.nk1);
+    cudaFree(b.nv0);
+    cudaFree(b.nv1);
+    cudaFree(b.keep);
+    cudaFree(b.kpre);
+    b.nk0 = b.nk1 = nullptr;
+    b.nv0 = b.nv1 = nullptr;
+    b.keep = nullptr;
+    b.kpre = nullptr;
+    int rc;
+    if ((rc = dalloc(&b.nk0, cap)) || (rc = dalloc(&b.nk1, cap)) || (rc = dalloc(&b.nv0, cap)) ||
+        (rc = dalloc(&b.nv1, cap)) || (rc = dalloc(&b.keep, cap)) || (rc = dalloc(&b.kpre, cap + 1)))
+        return rc;
+    b.new_cap = cap;
+    size_t need_tmp = std::max(radix_tmp_bytes(), scan_tmp_bytes(std::max<uint64_t>(cap, b.nl)));
+    if (need_tmp > b.tmp_bytes) {
+        cudaFree(b.tmp);
+        b.tmp = nullptr;
+        if ((rc = dalloc((char **)&b.tmp, need_tmp))) return rc;
+        b.tmp_bytes = need_tmp;
+    }
+    return CHL_OK;
+}
+
+int ensure_ent(uint2 **p, uint64_t *cap, uint64_t need) {
+    if (need <= *cap) return CHL_OK;
+    uint64_t c = std::max<uint64_t>(need, *cap + *cap / 2);
+    cudaFree(*p);
+    *p = nullptr;
+    int rc = dalloc(p, c);
+    if (rc) return rc;
+    *cap = c;
+    return CHL_OK;
+}
+
+}  // namespace
+
+// Host orchestration of one build.
+int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
+                 const chl_build_opts *opts_in, chl_labels **out) {
+    chl_build_opts opts;
+    if (opts_in) opts = *opts_in;
+    else chl_build_opts_default(&opts);
+    if (!g || !order_h || !out || n != g->n) {
+        set_error("order size must equal the number of graph vertices");
+        return CHL_ERR_INVALID;
+    }
+    if (g->min_len < 1) {
+        set_error("arc lengths must be positive (the reference asserts dd > d)");
+        return CHL_ERR_INVALID;
+    }
+    // order must be a permutation
+    std::vector<uint32_t> rank_h(n, kInf);
+    for (uint32_t i = 0; i < n; ++i) {
+        if (order_h[i] >= n || rank_h[order_h[i]] != kInf) {
+            set_error("order is not a permutation of the vertex ids");
+            return CHL_ERR_INVALID;
+        }
+        rank_h[order_h[i]] = i;
+    }
+    auto t_wall0 = std::chrono::steady_clock::now();
+    Build b;
+    b.n = n;
+    b.sides = g->symmetric ? 1 : 2;
+    b.nl = g->symmetric ? n : 2 * n;
+    b.hub_bits = bits_for(std::max<uint64_t>(n, 2));
+    b.key_bits = b.hub_bits + bits_for((uint64_t)b.nl + 1);
+    if (b.key_bits > 64) return CHL_ERR_INVALID;
+    CHL_CUDA(cudaStreamCreateWithFlags(&b.st, cudaStreamNonBlocking));
+    cudaEvent_t ev0, ev1, ev_a, ev_b;
+    CHL_CUDA(cudaEventCreate(&ev0));
+    CHL_CUDA(cudaEventCreate(&ev1));
+    CHL_CUDA(cudaEventCreate(&ev_a));
+    CHL_CUDA(cudaEventCreate(&ev_b));
+    struct EvGuard {
+        cudaEvent_t e[4];
+        ~EvGuard() {
+            for (auto x : e) cudaEventDestroy(x);
+        }
+    } evg{{ev0, ev1, ev_a, ev_b}};
+
+    CHL_CUDA(cudaEventRecord(ev0, b.st));
+    int rc = upload_graph(g, b.dg, b.st);
+    if (rc) return rc;
+    if ((rc = dalloc(&b.order, n)) || (rc = dalloc(&b.rank, n))) return rc;
+    CHL_CUDA(cudaMemcpyAsync(b.order, order_h, (size_t)n * 4, cudaMemcpyHostToDevice, b.st));
+    CHL_CUDA(cudaMemcpyAsync(b.rank, rank_h.data(), (size_t)n * 4, cudaMemcpyHostToDevice, b.st));
+    CHL_CUDA(cudaEventRecord(ev_a, b.st));
+
+    // committed label CSR (double buffered)
+    if ((rc = dalloc(&b.off_a, (size_t)b.nl + 1)) || (rc = dalloc(&b.off_b, (size_t)b.nl + 1)))
+        return rc;
+    CHL_CUDA(cudaMemsetAsync(b.off_a, 0, ((size_t)b.nl + 1) * 8, b.st));
+    if ((rc = ensure_ent(&b.ent_a, &b.ent_cap_a, 1))) return rc;
+    if ((rc = dalloc(&b.cnt, (size_t)b.nl + 1)) || (rc = dalloc(&b.pre, (size_t)b.nl + 2))) return rc;
+    CHL_CUDA(cudaMemsetAsync(b.cnt, 0, ((size_t)b.nl + 1) * 4, b.st));
+    if ((rc = dalloc(&b.tsize, n)) || (rc = dalloc(&b.tlab, n))) return rc;
+    if ((rc = dalloc(&b.ctl, 1))) return rc;
+    if ((rc = grow_new(b, std::max<uint64_t>(4ull * n, 1u << 20)))) return rc;
+
+    // workspace: one slot per resident warp
+    const int sms = device_sms();
+    const bool unit = g->unit;
+    const bool plant_mode = opts.mode != CHL_MODE_GLL;
+    size_t free_b = 0, total_b = 0;
+    CHL_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t per_slot = (size_t)n * (unit ? 8 : 20);
+    uint32_t want = (uint32_t)sms * 48;   // 12 blocks of 4 warps per SM at most
+    if (opts.max_warps) want = std::min<uint32_t>(want, opts.max_warps);
+    const size_t ws_budget = free_b / 3;
+    uint32_t fit = (uint32_t)std::max<size_t>(1, ws_budget / std::max<size_t>(per_slot, 1));
+    b.warps = std::max<uint32_t>(kWarpsPerBlock, std::min(want, fit));
+    b.warps = (b.warps / kWarpsPerBlock) * kWarpsPerBlock;
+    const size_t slots = b.warps;
+    if ((rc = dalloc(&b.ws_key, slots * n)) || (rc = dalloc(&b.ws_vis, slots * n))) return rc;
+    CHL_CUDA(cudaMemsetAsync(b.ws_key, 0xFF, slots * n * 4, b.st));
+    if (!unit) {
+        if ((rc = dalloc(&b.ws_pos, slots * n)) || (rc = dalloc(&b.ws_heap, slots * n))) return rc;
+    }
+
+    // superstep loop
+    const double sf = opts.sf > 0 ? opts.sf : 32.0;
+    // label_limit = sf * N counts both sides' labels (shared_memory/hhl.cpp:65);
+    // a symmetric build stores one side.
+    const unsigned long long budget_base =
+        (unsigned long long)std::max(1.0, sf * (double)n / (b.sides == 1 ? 2.0 : 1.0));
+    bool do_plant = opts.mode != CHL_MODE_GLL;
+    bool switch_open = opts.mode == CHL_MODE_HYBRID;
+    uint32_t r0 = 0;
+    uint64_t committed = 0;
+    uint32_t supersteps = 0, plant_roots = 0;
+    unsigned long long visits = 0, reads = 0, arcs = 0, launches = 0;
+    double tree_ms = 0, sort_ms = 0, commit_ms = 0;
+    uint32_t max_list = 0;   // longest committed list
+    while (r0 < n) {
+        const bool plant_now = do_plant;
+        const unsigned long long budget = budget_base;
+        uint32_t r_end = n;
+        BuildCtl hc;
+        bool rerun = false;
+        // root label staging capacity: longest committed list, bounded by smem
+        int max_smem = 0;
+        CHL_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0));
+        const size_t fixed = (unit ? 0 : kHeapSmem * 8) + kStage * 12;
+        size_t rcap = std::min<uint32_t>(std::max<uint32_t>(max_list, 32), 2048);
+        const size_t smem_cap = std::min<size_t>((size_t)max_smem, 96 * 1024);
+        if (kWarpsPerBlock * (rcap * 8 + fixed) > smem_cap)
+            rcap = (smem_cap / kWarpsPerBlock - fixed) / 8;
+        b.rcap = (uint32_t)rcap;
+        const size_t smem = kWarpsPerBlock * ((size_t)b.rcap * 8 + fixed);
+        while (true) {
+            std::memset(&hc, 0, sizeof(hc));
+            hc.next_root = r0;
+            CHL_CUDA(cudaMemcpyAsync(b.ctl, &hc, sizeof(hc), cudaMemcpyHostToDevice, b.st));
+            TreeArgs ta;
+            ta.n = n;
+            ta.sides = b.sides;
+            for (int s = 0; s < 2; ++s) {
+                ta.g_off[s] = b.dg.off[s];
+                ta.g_arc[s] = b.dg.arc[s];
+                ta.g_head[s] = b.dg.head[s];
+            }
+            ta.order = b.order;
+            ta.rank = b.rank;
+            ta.l_off = b.off_a;
+            ta.l_ent = b.ent_a;
+            ta.r0 = r0;
+            ta.r_end = r_end;
+            ta.budget = rerun ? ~0ull : budget;
+            ta.hub_bits = b.hub_bits;
+            ta.out_key = b.nk0;
+            ta.out_val = b.nv0;
+            ta.out_cap = b.new_cap;
+            ta.tree_size = b.tsize;
+            ta.tree_labels = b.tlab;
+            ta.ws_key = b.ws_key;
+            ta.ws_vis = b.ws_vis;
+            ta.ws_pos = b.ws_pos;
+            ta.ws_heap = b.ws_heap;
+            ta.ctl = b.ctl;
+            ta.rcap = b.rcap;
+            const int blocks = (int)(b.warps / kWarpsPerBlock);
+            void (*kern)(TreeArgs);
+            if (unit) kern = plant_now ? tree_kernel<true, true> : tree_kernel<true, false>;
+            else kern = plant_now ? tree_kernel<false, true> : tree_kernel<false, false>;
+            CHL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            CHL_CUDA(cudaEventRecord(ev_a, b.st));
+            kern<<<blocks, kWarpsPerBlock * 32, smem, b.st>>>(ta);
+            CHL_CUDA(cudaGetLastError());
+            CHL_CUDA(cudaEventRecord(ev_b, b.st));
+            ++launches;
+            CHL_CUDA(cudaMemcpyAsync(&hc, b.ctl, sizeof(hc), cudaMemcpyDeviceToHost, b.st));
+            CHL_CUDA(cudaStreamSynchronize(b.st));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev_a, ev_b);
+            tree_ms += ms;
+            uint32_t r1 = (uint32_t)std::min<unsigned long long>(hc.next_root, r_end);
+            if (hc.err) {
+                set_error(hc.err == 1 ? "a shortest-path distance reaches INT_MAX (the reference asserts dd < infty)"
+                                      : "tree workspace bound exceeded");
+                return CHL_ERR_INVALID;
+            }
+            if (hc.overflow || hc.nlab > b.new_cap) {
+                // re-run the same root range with room for every label
+                if ((rc = grow_new(b, hc.nlab + hc.nlab / 4 + 1024))) return rc;
+                r_end = r1;
+                rerun = true;
+                continue;
+            }
+            r_end = r1;
+            break;
+        }
+        const uint32_t r1 = r_end;
+        visits += hc.visits;
+        reads += hc.label_reads;
+        arcs += hc.arcs;
+        if (plant_now) plant_roots += r1 - r0;
+        unsigned long long M = hc.nlab;
+        // hybrid switch (distributed_memory/akiba.hpp:297-303, 362-376)
+        if (plant_now && switch_open) {
+            unsigned long long zero = 0;
+            CHL_CUDA(cudaMemcpyAsync(&b.ctl->max_ratio_num, &zero, 8, cudaMemcpyHostToDevice, b.st));
+            ratio_max<<<std::max(1, sms), 256, 0, b.st>>>(b.tsize, b.tlab, &b.ctl->next_root, r0, r1, b.ctl);
+            unsigned long long bits = 0;
+            CHL_CUDA(cudaMemcpyAsync(&bits, &b.ctl->max_ratio_num, 8, cudaMemcpyDeviceToHost, b.st));
+            CHL_CUDA(cudaStreamSynchronize(b.st));
+            double ratio;
+            std::memcpy(&ratio, &bits, 8);
+            if (ratio > opts.ps) {
+                do_plant = false;
+                switch_open = false;
+            }
+        }
+        CHL_CUDA(cudaEventRecord(ev_a, b.st));
+        // --- sort the new labels by (list, hub)
+        int parity = 0;
+        if ((rc = radix_sort_pairs(b.nk0, b.nv0, b.nk1, b.nv1, (const uint64_t *)&b.ctl->nlab,
+                                   b.new_cap, b.key_bits, b.tmp, b.tmp_bytes, b.st, &parity)))
+            return rc;
+        uint64_t *sk = parity ? b.nk1 : b.nk0;
+        uint32_t *sv = parity ? b.nv1 : b.nv0;
+        uint64_t *ak = parity ? b.nk0 : b.nk1;
+        uint32_t *av = parity ? b.nv0 : b.nv1;
+        const int cgrid = sms * 8;
+        const unsigned long long *d_count = &b.ctl->nlab;
+        // --- GLL clean
+        if (!plant_now && M > 0) {
+            CHL_CUDA(cudaMemsetAsync(b.cnt, 0, ((size_t)b.nl + 1) * 4, b.st));
+            count_keys<<<cgrid, 256, 0, b.st>>>(sk, d_count, b.new_cap, b.hub_bits, b.cnt);
+            if ((rc = scan_u32_excl(b.cnt, b.pre, b.nl, nullptr, b.tmp, b.tmp_bytes, b.st))) return rc;
+            clean_mark<<<cgrid, 256, 0, b.st>>>(sk, sv, d_count, b.new_cap, b.hub_bits, r0, b.pre,
+                                                b.order, b.rank, b.sides, b.keep);
+            if ((rc = scan_u32_excl(b.keep, b.kpre, b.new_cap, (const uint64_t *)d_count, b.tmp,
+                                    b.tmp_bytes, b.st)))
+                return rc;
+            compact_kept<<<cgrid, 256, 0, b.st>>>(sk, sv, b.keep, b.kpre, d_count, b.new_cap, ak, av,
+                                                  &b.ctl->n_keep);
+            CHL_CUDA(cudaMemcpyAsync(&b.ctl->nlab, &b.ctl->n_keep, 8, cudaMemcpyDeviceToDevice, b.st));
+            std::swap(sk, ak);
+            std::swap(sv, av);
+            CHL_CUDA(cudaMemcpyAsync(&M, &b.ctl->n_keep, 8, cudaMemcpyDeviceToHost, b.st));
+            CHL_CUDA(cudaStreamSynchronize(b.st));
+        }
+        CHL_CUDA(cudaEventRecord(ev_b, b.st));
+        // --- commit: merge the sorted new labels into the committed CSR
+        CHL_CUDA(cudaMemsetAsync(b.cnt, 0, ((size_t)b.nl + 1) * 4, b.st));
+        count_keys<<<cgrid, 256, 0, b.st>>>(sk, d_count, b.new_cap, b.hub_bits, b.cnt);
+        if ((rc = scan_u32_excl(b.cnt, b.pre, b.nl, nullptr, b.tmp, b.tmp_bytes, b.st))) return rc;
+        if ((rc = ensure_ent(&b.ent_b, &b.ent_cap_b, committed + M))) return rc;
+        merge_offsets<<<cgrid, 256, 0, b.st>>>(b.off_a, b.pre, b.off_b, b.nl);
+        copy_old_lists<<<cgrid, 256, 0, b.st>>>(b.off_a, b.ent_a, b.off_b, b.ent_b, b.nl);
+        place_new<<<cgrid, 256, 0, b.st>>>(sk, sv, d_count, b.new_cap, b.hub_bits, r0, b.pre, b.off_a,
+                                           b.off_b, b.ent_b);
+        CHL_CUDA(cudaGetLastError());
+        std::swap(b.off_a, b.off_b);
+        std::swap(b.ent_a, b.ent_b);
+        std::swap(b.ent_cap_a, b.ent_cap_b);
+        committed += M;
+        CHL_CUDA(cudaEventRecord(ev_a, b.st));
+        // longest committed list, for the next superstep's root staging
+        CHL_CUDA(cudaMemsetAsync(&b.ctl->max_ratio_den, 0, 8, b.st));
+        max_list_len<<<cgrid, 256, 0, b.st>>>(b.off_a, b.nl, &b.ctl->max_ratio_den);
+        unsigned long long mx = 0;
+        CHL_CUDA(cudaMemcpyAsync(&mx, &b.ctl->max_ratio_den, 8, cudaMemcpyDeviceToHost, b.st));
+        CHL_CUDA(cudaStreamSynchronize(b.st));
+        max_list = (uint32_t)std::min<unsigned long long>(mx, 0xFFFFFFFFu);
+        float ms1 = 0;
+        cudaEventElapsedTime(&ms1, ev_b, ev_a);
+        commit_ms += ms1;
+        ++supersteps;
+        r0 = r1;
+        if (opts.verbose >= 2)
+            fprintf(stderr, "superstep %u: roots [%u,%u) %s labels %llu committed %llu\n", supersteps,
+                    r1 - (r1 - r0), r1, plant_now ? "plant" : "gll", (unsigned long long)M,
+                    (unsigned long long)committed);
+    }
+    CHL_CUDA(cudaEventRecord(ev1, b.st));
+    CHL_CUDA(cudaStreamSynchronize(b.st));
+    float total_ms = 0;
+    cudaEventElapsedTime(&total_ms, ev0, ev1);
+
+    chl_labels *L = new (std::nothrow) chl_labels();
+    if (!L) return CHL_ERR_OOM;
+    L->n = n;
+    L->sym = b.sides == 1;
+    L->d_off = b.off_a;
+    L->d_ent = (LabelEnt *)b.ent_a;
+    L->total = committed;
+    b.off_a = nullptr;
+    b.ent_a = nullptr;
+    chl_build_stats &S = L->stats;
+    S.build_ms = total_ms;
+    S.tree_ms = tree_ms;
+    S.sort_ms = sort_ms;
+    S.commit_ms = commit_ms;
+    S.labels = committed * (L->sym ? 2 : 1);
+    S.visits = visits;
+    S.label_reads = reads;
+    S.arcs = arcs;
+    S.supersteps = supersteps;
+    S.plant_roots = plant_roots;
+    S.tree_launches = launches;
+    S.avg_label = n ? (double)S.labels / n / 2.0 : 0.0;
+    (void)t_wall0;
+    *out = L;
+    if (opts.verbose) {
+        // the reference's summary line (shared_memory/akiba.hpp:214)
+        printf("Average label size after gll is %g, labeling time = %g, sorting time = %g, "
+               "cleaning time = %g, total time = %g\n",
+               S.avg_label, tree_ms / 1e3, sort_ms / 1e3, commit_ms / 1e3, total_ms / 1e3);
+        printf("%g %g\n", S.avg_label, total_ms / 1e3);
+    }
+    return CHL_OK;
+}
+
+}  // namespace chl
+
+extern "C" void chl_build_opts_default(chl_build_opts *o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->mode = CHL_MODE_HYBRID;
+    o->sf = 32.0;
+    o->ps = 1024.0;
+    o->autotune = 1;
+    o->use_graphs = 0;
+    o->verbose = 0;
+}
+
+extern "C" int chl_build(const chl_graph *g, const uint32_t *order, uint32_t n,
+                         const chl_build_opts *opts, chl_labels **out) {
+    try {
+        return chl::build_labels(g, order, n, opts, out);
+    } catch (...) {
+        chl::set_error("host allocation failed during build");
+        return CHL_ERR_OOM;
+    }
+}
+
+extern "C" int chl_build_get_stats(const chl_labels *l, chl_build_stats *s) {
+    if (!l || !s) return CHL_ERR_INVALID;
+    *s = l->stats;
+    return CHL_OK;
+}

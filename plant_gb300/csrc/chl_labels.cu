@@ -1,0 +1,310 @@
+// Label storage on the device, host transfers, and the batched distance
+// query kernel.
+//
+//   Labeling::query         shared_memory/labeling.hpp:56-65
+//   batchLocalQuery         distributed_memory/query_funcs.hpp:23-30
+//   query mode 1 (QLSN)     distributed_memory/query.hpp:82-91
+#include "chl_dev.cuh"
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace chl {
+
+int cuda_status(cudaError_t e, const char *what, const char *file, int line) {
+    std::string msg = std::string(what) + " failed: " + cudaGetErrorString(e) + " (" + file + ":" +
+                      std::to_string(line) + ")";
+    set_error(msg);
+    if (e == cudaErrorMemoryAllocation) return CHL_ERR_OOM;
+    return CHL_ERR_CUDA;
+}
+
+int device_sms() {
+    static int sms = 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            sms = 1;
+        }
+    });
+    return sms;
+}
+
+int labels_fetch_host(const chl_labels *l) {
+    if (l->host_valid) return CHL_OK;
+    if (!l->d_off) return CHL_ERR_INVALID;
+    const uint32_t nl = l->nl();
+    l->h_off.resize((size_t)nl + 1);
+    l->h_ent.resize(l->total);
+    CHL_CUDA(cudaMemcpy(l->h_off.data(), l->d_off, ((size_t)nl + 1) * 8, cudaMemcpyDeviceToHost));
+    if (l->total)
+        CHL_CUDA(cudaMemcpy(l->h_ent.data(), l->d_ent, l->total * sizeof(LabelEnt),
+                            cudaMemcpyDeviceToHost));
+    l->host_valid = true;
+    return CHL_OK;
+}
+
+int labels_ensure_device(const chl_labels *L) {
+    if (L->d_off) return CHL_OK;
+    const uint32_t nl = L->nl();
+    cudaError_t e = cudaMalloc(&L->d_off, ((size_t)nl + 1) * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&L->d_ent, std::max<uint64_t>(L->total, 1) * sizeof(LabelEnt));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(L->d_off, L->h_off.data(), ((size_t)nl + 1) * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && L->total)
+        e = cudaMemcpy(L->d_ent, L->h_ent.data(), L->total * sizeof(LabelEnt), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        int rc = cuda_status(e, "label upload", __FILE__, __LINE__);
+        cudaFree(L->d_off);
+        cudaFree(L->d_ent);
+        L->d_off = nullptr;
+        L->d_ent = nullptr;
+        return rc;
+    }
+    return CHL_OK;
+}
+
+int labels_from_host(uint32_t n, const uint64_t *off2, const uint32_t *hub, const int32_t *dist,
+                     chl_labels **out) {
+    // every list must be strictly ascending by hub with non-negative distances
+    for (uint64_t x = 0; x < 2ull * n; ++x) {
+        if (off2[x + 1] < off2[x]) {
+            set_error("label offsets are not monotone");
+            return CHL_ERR_INVALID;
+        }
+        for (uint64_t k = off2[x]; k < off2[x + 1]; ++k) {
+            if (dist[k] < 0 || (k > off2[x] && hub[k] <= hub[k - 1])) {
+                set_error("label lists must be ascending by hub with non-negative distances");
+                return CHL_ERR_INVALID;
+            }
+        }
+    }
+    bool sym = true;
+    for (uint32_t v = 0; v < n && sym; ++v) {
+        const uint64_t a = off2[2 * v], ae = off2[2 * v + 1], b = off2[2 * v + 1], be = off2[2 * v + 2];
+        if (ae - a != be - b) {
+            sym = false;
+            break;
+        }
+        for (uint64_t k = 0; k < ae - a; ++k)
+            if (hub[a + k] != hub[b + k] || dist[a + k] != dist[b + k]) {
+                sym = false;
+                break;
+            }
+    }
+    chl_labels *L = new (std::nothrow) chl_labels();
+    if (!L) return CHL_ERR_OOM;
+    L->n = n;
+    L->sym = sym;
+    const uint32_t nl = L->nl();
+    L->h_off.assign((size_t)nl + 1, 0);
+    for (uint32_t x = 0; x < nl; ++x) {
+        const uint64_t src = sym ? 2ull * x : x;
+        L->h_off[x + 1] = L->h_off[x] + (off2[src + 1] - off2[src]);
+    }
+    L->total = L->h_off[nl];
+    L->h_ent.resize(L->total);
+    for (uint32_t x = 0; x < nl; ++x) {
+        const uint64_t src = sym ? 2ull * x : x;
+        for (uint64_t k = 0; k < off2[src + 1] - off2[src]; ++k)
+            L->h_ent[L->h_off[x] + k] = LabelEnt{hub[off2[src] + k], (uint32_t)dist[off2[src] + k]};
+    }
+    L->host_valid = true;
+    L->stats.labels = L->total * (sym ? 2 : 1);
+    L->stats.avg_label = n ? (double)L->stats.labels / n / 2.0 : 0.0;
+    *out = L;
+    return CHL_OK;
+}
+
+namespace {
+
+// One warp per pair: merge L(s, 1) with L(t, 0) 32 entries at a time.  Each
+// lane binary-searches its entry of the current A chunk inside the B chunk
+// held in registers (5 shuffles); the list whose chunk ends first advances.
+// Pads: A uses 0xFFFFFFFF, B 0xFFFFFFFE, so pads never match.
+__device__ __forceinline__ uint32_t merge_min(const uint2 *A, uint32_t na, const uint2 *B,
+                                              uint32_t nb) {
+    const uint32_t lane = lane_id();
+    uint32_t best = 0xFFFFFFFFu;
+    uint32_t ia = 0, ib = 0;
+    while (ia < na && ib < nb) {
+        uint2 a = ia + lane < na ? A[ia + lane] : make_uint2(0xFFFFFFFFu, 0);
+        uint2 b = ib + lane < nb ? B[ib + lane] : make_uint2(0xFFFFFFFEu, 0);
+        // lower_bound of a.x in the B chunk
+        uint32_t lo = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+            const uint32_t hb = __shfl_sync(kFull, b.x, lo + step - 1);
+            if (hb < a.x) lo += step;
+        }
+        const uint32_t hb = __shfl_sync(kFull, b.x, lo & 31);
+        const uint32_t db = __shfl_sync(kFull, b.y, lo & 31);
+        if (lo < 32 && hb == a.x) best = min(best, a.y + db);
+        const uint32_t lastA = __shfl_sync(kFull, a.x, 31);
+        const uint32_t lastB = __shfl_sync(kFull, b.x, 31);
+        if (lastA <= lastB) ia += 32;
+        if (lastB <= lastA) ib += 32;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_xor_sync(kFull, best, o));
+    return best;
+}
+
+__global__ void query_kernel(const uint64_t *__restrict__ off, const uint2 *__restrict__ ent,
+                             uint32_t n, int sym, const uint32_t *__restrict__ pairs, size_t k,
+                             int32_t *__restrict__ out) {
+    const size_t warps = (size_t)gridDim.x * (blockDim.x >> 5);
+    for (size_t q = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); q < k; q += warps) {
+        const uint32_t s = pairs[2 * q], t = pairs[2 * q + 1];
+        uint32_t r = 0xFFFFFFFFu;
+        if (s < n && t < n) {
+            const uint32_t xa = sym ? s : 2 * s + 1;   // L(s, 1): forward hubs of s
+            const uint32_t xb = sym ? t : 2 * t;       // L(t, 0): reverse hubs of t
+            const uint64_t a0 = off[xa], a1 = off[xa + 1], b0 = off[xb], b1 = off[xb + 1];
+            r = merge_min(ent + a0, (uint32_t)(a1 - a0), ent + b0, (uint32_t)(b1 - b0));
+        }
+        if (lane_id() == 0) out[q] = r > 2147483647u ? 2147483647 : (int32_t)r;
+    }
+}
+
+__global__ void hub_count(const uint2 *ent, uint64_t total, uint32_t *cnt) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        atomicAdd(&cnt[ent[i].x], 1u);
+}
+
+}  // namespace
+
+int query_launch(const chl_labels *l, const uint32_t *d_pairs, size_t k, int32_t *d_out,
+                 cudaStream_t s) {
+    if (k == 0) return CHL_OK;
+    int rc = labels_ensure_device(l);
+    if (rc) return rc;
+    const int threads = 256;
+    size_t blocks = (k + (threads / 32) - 1) / (threads / 32);
+    blocks = std::min<size_t>(blocks, (size_t)device_sms() * 64);
+    query_kernel<<<(unsigned)blocks, threads, 0, s>>>(l->d_off, (const uint2 *)l->d_ent, l->n,
+                                                      l->sym ? 1 : 0, d_pairs, k, d_out);
+    CHL_CUDA(cudaGetLastError());
+    return CHL_OK;
+}
+
+}  // namespace chl
+
+using namespace chl;
+
+extern "C" double chl_avg_label(const chl_labels *l) { return l ? l->stats.avg_label : 0.0; }
+extern "C" uint32_t chl_labels_n(const chl_labels *l) { return l ? l->n : 0; }
+extern "C" uint64_t chl_labels_total(const chl_labels *l) {
+    return l ? l->total * (l->sym ? 2 : 1) : 0;
+}
+
+extern "C" int chl_labels_get(const chl_labels *l, uint32_t v, int side, uint32_t *hubs,
+                              int32_t *dists, uint32_t cap, uint32_t *cnt) {
+    if (!l || v >= l->n || side < 0 || side > 1 || !cnt) return CHL_ERR_INVALID;
+    int rc = labels_fetch_host(l);
+    if (rc) return rc;
+    const uint32_t x = l->list(v, side);
+    const uint64_t b = l->h_off[x], e = l->h_off[x + 1];
+    *cnt = (uint32_t)(e - b);
+    if (hubs || dists) {
+        if (cap < e - b) return CHL_ERR_INVALID;
+        for (uint64_t k = b; k < e; ++k) {
+            if (hubs) hubs[k - b] = l->h_ent[k].hub;
+            if (dists) dists[k - b] = (int32_t)l->h_ent[k].dist;
+        }
+    }
+    return CHL_OK;
+}
+
+extern "C" int chl_labels_export(const chl_labels *l, uint64_t *off, uint32_t *hubs,
+                                 int32_t *dists) {
+    if (!l || !off) return CHL_ERR_INVALID;
+    int rc = labels_fetch_host(l);
+    if (rc) return rc;
+    uint64_t p = 0;
+    off[0] = 0;
+    for (uint32_t v = 0; v < l->n; ++v)
+        for (int side = 0; side < 2; ++side) {
+            const uint32_t x = l->list(v, side);
+            for (uint64_t k = l->h_off[x]; k < l->h_off[x + 1]; ++k, ++p) {
+                if (hubs) hubs[p] = l->h_ent[k].hub;
+                if (dists) dists[p] = (int32_t)l->h_ent[k].dist;
+            }
+            off[2 * v + side + 1] = p;
+        }
+    return CHL_OK;
+}
+
+extern "C" int chl_labels_import(uint32_t n, const uint64_t *off, const uint32_t *hubs,
+                                 const int32_t *dists, chl_labels **out) {
+    if (!off || !out || (off[2ull * n] && (!hubs || !dists))) return CHL_ERR_INVALID;
+    return labels_from_host(n, off, hubs, dists, out);
+}
+
+extern "C" int chl_labels_hub_freq(const chl_labels *l, const uint32_t *order, uint32_t *freq) {
+    if (!l || !order || !freq) return CHL_ERR_INVALID;
+    int rc = labels_ensure_device(l);
+    if (rc) return rc;
+    uint32_t *d_cnt = nullptr;
+    CHL_CUDA(cudaMalloc(&d_cnt, (size_t)std::max<uint32_t>(l->n, 1) * 4));
+    cudaMemset(d_cnt, 0, (size_t)l->n * 4);
+    if (l->total)
+        hub_count<<<device_sms() * 8, 256>>>((const uint2 *)l->d_ent, l->total, d_cnt);
+    std::vector<uint32_t> cnt(l->n);
+    cudaError_t e = cudaMemcpy(cnt.data(), d_cnt, (size_t)l->n * 4, cudaMemcpyDeviceToHost);
+    cudaFree(d_cnt);
+    if (e != cudaSuccess) return cuda_status(e, "hub_freq", __FILE__, __LINE__);
+    for (uint32_t h = 0; h < l->n; ++h) freq[order[h]] = cnt[h] * (l->sym ? 2u : 1u);
+    return CHL_OK;
+}
+
+extern "C" void chl_labels_free(chl_labels *l) {
+    if (!l) return;
+    cudaFree(l->d_off);
+    cudaFree(l->d_ent);
+    delete l;
+}
+
+extern "C" int chl_query_batch_device(const chl_labels *l, const uint32_t *d_pairs, size_t k,
+                                      int32_t *d_out, void *stream) {
+    if (!l || (k && (!d_pairs || !d_out))) return CHL_ERR_INVALID;
+    return query_launch(l, d_pairs, k, d_out, (cudaStream_t)stream);
+}
+
+extern "C" int chl_query_batch(const chl_labels *l, const uint32_t *pairs, size_t k, int32_t *out,
+                               void *stream) {
+    if (!l || (k && (!pairs || !out))) return CHL_ERR_INVALID;
+    for (size_t i = 0; i < 2 * k; ++i)
+        if (pairs[i] >= l->n) {
+            set_error("query vertex out of range");
+            return CHL_ERR_INVALID;
+        }
+    if (k == 0) return CHL_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    uint32_t *dp = nullptr;
+    int32_t *dout = nullptr;
+    CHL_CUDA(cudaMallocAsync(&dp, k * 8, s));
+    cudaError_t e = cudaMallocAsync(&dout, k * 4, s);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(dp, s);
+        return cuda_status(e, "cudaMallocAsync", __FILE__, __LINE__);
+    }
+    int rc = CHL_OK;
+    e = cudaMemcpyAsync(dp, pairs, k * 8, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) rc = query_launch(l, dp, k, dout, s);
+    if (e == cudaSuccess && rc == CHL_OK) e = cudaMemcpyAsync(out, dout, k * 4, cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(dp, s);
+    cudaFreeAsync(dout, s);
+    cudaError_t e2 = cudaStreamSynchronize(s);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_status(e, "query copy", __FILE__, __LINE__);
+    if (e2 != cudaSuccess) return cuda_status(e2, "query sync", __FILE__, __LINE__);
+    return CHL_OK;
+}

@@ -1,0 +1,137 @@
+"""Label construction on the GPU: bit-exact against the reference's labels.
+
+Parity targets: the golden label files printed by the reference GLL binary,
+and the CPU oracle (whose GLL restatement reproduces those files byte for
+byte) on larger seeded graphs.  Every build mode must give the same labels:
+canonical labels are unique for a given order.
+"""
+import filecmp
+
+import numpy as np
+import pytest
+
+from conftest import label_case
+
+pytestmark = pytest.mark.gpu
+
+MODES = {"hybrid": 0, "gll": 1, "plant": 2}
+CASES = ["grid12", "grid20hw", "rmat8", "directed60", "unit_path"]
+
+
+def same_labels(L, ref, n):
+    a = L.export()
+    b = ref.export(n)
+    for x, y in zip(a, b):
+        if not np.array_equal(np.asarray(x), np.asarray(y)):
+            return False
+    return True
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("mode", list(MODES))
+def test_golden_label_files(P, case, mode, tmp_path):
+    c = label_case(case)
+    g = P.Graph.read(c["gr"])
+    order = P.Order.read(c["order"])
+    L = P.build(g, order, mode=MODES[mode])
+    out = str(tmp_path / "gpu.labels")
+    L.write(out)
+    assert filecmp.cmp(out, c["labels"], shallow=False)
+
+
+@pytest.mark.parametrize("mode", list(MODES))
+@pytest.mark.parametrize("sf", [32.0, 0.05])
+def test_config1_grid_matches_oracle(P, O, mode, sf):
+    g = P.Graph.grid(100, 100, seed=1)
+    order = P.Order.degree(g, seed=1)
+    off, head, ln = g.csr(True)
+    og = O.OGraph.from_csr(g.get_n(), off, head, ln)
+    ref, _ = O.gll(og, order)
+    L = P.build(g, order, mode=MODES[mode], sf=sf)
+    assert same_labels(L, ref, g.get_n())
+    st = L.stats()
+    assert st["supersteps"] >= 1 and st["labels"] == ref.total()
+
+
+@pytest.mark.parametrize("mode", list(MODES))
+def test_rmat_unit_lengths_matches_oracle(P, O, mode):
+    g = P.Graph.rmat(12, 16, seed=5)
+    order = P.Order.degree(g, seed=2)
+    off, head, ln = g.csr(True)
+    og = O.OGraph.from_csr(g.get_n(), off, head, ln)
+    ref, _ = O.gll(og, order)
+    L = P.build(g, order, mode=MODES[mode], sf=1.0)
+    assert same_labels(L, ref, g.get_n())
+
+
+@pytest.mark.parametrize("mode", list(MODES))
+def test_directed_weighted_matches_oracle(P, O, mode, tmp_path):
+    rng = np.random.default_rng(7)
+    n, m = 700, 4000
+    src = rng.integers(0, n, m).astype(np.uint32)
+    dst = rng.integers(0, n, m).astype(np.uint32)
+    keep = src != dst
+    w = rng.integers(1, 50, m).astype(np.int32)
+    g = P.Graph.from_arcs(n, src[keep], dst[keep], w[keep])
+    assert not g.symmetric()
+    p = str(tmp_path / "d.gr")
+    g.write(p)
+    og = O.OGraph.read_dimacs(p)
+    order = og.degree_order(3)
+    ref, _ = O.gll(og, order)
+    L = P.build(g, order, mode=MODES[mode], sf=0.5)
+    assert same_labels(L, ref, n)
+
+
+def test_tiny_and_disconnected(P, O):
+    # isolated vertices, a 2-cycle and a single arc
+    g = P.Graph.from_arcs(5, [0, 1, 3], [1, 0, 4], [2, 2, 7])
+    order = np.array([4, 2, 0, 3, 1], np.uint32)
+    off, head, ln = g.csr(True)
+    og = O.OGraph.from_csr(5, off, head, ln)
+    ref, _ = O.gll(og, order)
+    for mode in MODES.values():
+        L = P.build(g, order, mode=mode)
+        assert same_labels(L, ref, 5)
+    L = P.build(g, order)
+    q = P.query(L, [[0, 1], [3, 4], [4, 3], [2, 0], [2, 2]])
+    assert q.tolist() == [2, 7, P.INFTY, P.INFTY, 0]
+
+
+def test_single_vertex(P):
+    g = P.Graph.from_arcs(1, [], [], [])
+    L = P.build(g, np.array([0], np.uint32))
+    assert L.label(0, 0)[0].tolist() == [0] and L.label(0, 1)[1].tolist() == [0]
+
+
+def test_bad_order_rejected(P):
+    g = P.Graph.grid(5, 5, seed=1)
+    n = g.get_n()
+    with pytest.raises(P.CHLError) as e:
+        P.build(g, np.zeros(n, np.uint32))
+    assert e.value.status == P.CHL_ERR_INVALID
+    with pytest.raises(P.CHLError):
+        P.build(g, np.arange(n - 1, dtype=np.uint32))
+
+
+def test_build_is_deterministic(P):
+    g = P.Graph.grid(60, 60, highways=40, hw_steps=16, seed=9)
+    order = P.Order.degree(g, seed=4)
+    a = P.build(g, order, sf=0.2).export()
+    b = P.build(g, order, sf=0.2, max_warps=64).export()
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+def test_sampled_queries_equal_dijkstra(P, O):
+    g = P.Graph.grid(80, 80, highways=30, hw_steps=20, seed=2)
+    order = P.Order.degree(g, seed=6)
+    L = P.build(g, order)
+    off, head, ln = g.csr(True)
+    og = O.OGraph.from_csr(g.get_n(), off, head, ln)
+    rng = np.random.default_rng(1)
+    n = g.get_n()
+    for s in rng.integers(0, n, 8):
+        d = og.dijkstra(int(s))
+        pairs = np.stack([np.full(n, s), np.arange(n)], 1).astype(np.uint32)
+        assert np.array_equal(P.query(L, pairs), d)
