@@ -1,0 +1,314 @@
+#!/usr/bin/env python3
+"""Benchmark: canonical hub label build on a ~1M-vertex road-like grid.
+
+Workload (the metric's configuration): 1024 x 1024 perturbed 4-neighbour
+grid (5% edges deleted, largest component, 1% diagonal shortcuts, lengths
+uniform in [1, 1000]) plus 2,000 highway edges at most 64 grid steps long
+(length round(150 x Manhattan)); ranking = sampled betweenness from 256
+seeded sources computed on the GPU (untimed set-up).  One step = one full
+label build (all roots, canonical labels) with the graph resident in HBM.
+
+  value  : labels/s of the device-timed builds (CUDA events on the build
+           stream; the label CSR alone is several GB, far above L2, so no
+           flush is needed between steps)
+  e2e    : labels/s through the C ABI from host buffers: graph + order
+           upload, build, and the labels read back to host memory, timed on
+           the host around each step
+  roofline: tree kernel, algorithmic bytes (sequential-PLL work of the
+           labelled vertices: 8 B per relaxed arc + 8 B per label entry the
+           prune test reads + 8 B per label written) / tree-kernel time
+  cpu_baseline: the CPU restatement of the reference GLL (OpenMP, all host
+           cores) on a bounded sample: the first R roots of the same build
+
+--impl reference times that CPU restatement (the reference itself does not
+build on this host: shared_memory/akiba.hpp includes <immintrin.h>, x86 only,
+and its sources are not present on the GPU host) on the same bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "CHL label build throughput (canonical labels, 1024x1024 road-like grid, betweenness order)"
+UNIT = "labels/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--side", type=int, default=1024)
+    ap.add_argument("--highways", type=int, default=2000)
+    ap.add_argument("--sources", type=int, default=256)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+class Clocks:
+    """Samples nvidia-smi during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        sm = []
+        mx = None
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx = float(r[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[3:7]):
+                if v.strip().lower() in ("active", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """Per-launch DRAM traffic of the tree kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "tree_kernel_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+def make_workload(P, args):
+    g = P.Graph.grid(args.side, args.side, del_frac=0.05, diag_frac=0.01, wmin=1, wmax=1000,
+                     highways=args.highways, hw_steps=64, hw_factor=150.0, seed=1)
+    order = P.Order.betweenness(g, args.sources, seed=1)
+    return g, order
+
+
+def cpu_sample(g, order, seconds, threads=None):
+    """Oracle GLL restatement on the first R roots; R sized to ~`seconds`."""
+    from oracle import oracle as O
+    off, head, ln = g.csr(True)
+    og = O.OGraph.from_csr(g.get_n(), off, head, ln)
+    threads = threads or os.cpu_count() or 1
+    r = 32
+    labels, secs = O.gll_sample(og, order, r, threads)
+    while secs < seconds / 4 and r < len(order):
+        r = min(len(order), int(r * max(2.0, min(8.0, seconds / max(secs, 1e-3) / 2))))
+        labels, secs = O.gll_sample(og, order, r, threads)
+    return og, r, threads, labels, secs
+
+
+def build_work_bytes(L, g):
+    """Sequential-PLL bytes of the labelled vertices, from list sizes: a list
+    of length k at vertex u (side s, built by trees walking direction 1-s)
+    costs sum_{j<k} (8*outdeg(u) + 8*j + 8)."""
+    sizes = L.list_sizes().astype(np.float64).reshape(-1, 2)
+    deg_fwd = g.degrees(True).astype(np.float64)
+    deg_rev = g.degrees(False).astype(np.float64)
+    tot = 0.0
+    for side, deg in ((0, deg_fwd), (1, deg_rev)):
+        k = sizes[:, side]
+        tot += float(np.sum(8.0 * k * deg + 8.0 * k * (k - 1) / 2.0 + 8.0 * k))
+    return tot
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    import plant_gb300 as P
+    from oracle import oracle as O
+    P.lib()
+    g, order = make_workload(P, args)
+    off, head, ln = g.csr(True)
+    og, r, threads, labels, secs = cpu_sample(g, order, args.cpu_seconds)
+    vals = []
+    for _ in range(args.warmup):
+        O.gll_sample(og, order, r, threads)
+    for _ in range(args.steps):
+        lab, s = O.gll_sample(og, order, r, threads)
+        vals.append(lab / s)
+    v = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean([labels / x for x in vals])),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic",
+            "config": {"workload": f"grid{args.side}x{args.side}+hw{args.highways}, betweenness({args.sources})",
+                       "sample_roots": r},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"first {r} of {len(order)} roots (both sides), GLL restatement"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, ws, rank):
+    import plant_gb300 as P
+    P.lib()
+    dist = None
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    g, order = make_workload(P, args)
+    n = g.get_n()
+    g.to_device()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        L = P.build(g, order)
+        del L
+    barrier()
+    stats = []
+    t0 = time.time()
+    with Clocks() as ck:
+        for _ in range(args.steps):
+            L = P.build(g, order)
+            stats.append(L.stats())
+    wall = time.time() - t0
+    barrier()
+    build_ms = [s["build_ms"] for s in stats]
+    tree_ms = [s["tree_ms"] for s in stats]
+    labels = stats[-1]["labels"]
+    ms_step = float(np.mean(build_ms))
+    if dist is not None:
+        import torch
+        t = torch.tensor([ms_step], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = ws * labels / (ms_step / 1e3)
+    work = build_work_bytes(L, g)
+    avg_tree_ms = float(np.mean(tree_ms))
+    per_launch_tree = avg_tree_ms / max(1, stats[-1]["tree_launches"])
+    peak, peak_kind = peaks()
+    achieved = work / (avg_tree_ms / 1e3) / 1e9
+    traffic = profile_traffic()
+    # queries on the resident labels (uniform pairs, device resident)
+    qk = 1 << 22
+    q_ms, q_bytes = P.query_bench(L, qk, iters=20, seed=7)
+    qps = qk / (q_ms / 1e3)
+    # e2e through the C ABI from host buffers
+    g.release_device()
+    off, head, ln = g.csr(True)
+    h2d = off.nbytes + head.nbytes + ln.nbytes + order.nbytes
+    if not g.symmetric():
+        off0, head0, ln0 = g.csr(False)
+        h2d += off0.nbytes + head0.nbytes + ln0.nbytes
+    e2e_s = []
+    d2h = 0
+    for _ in range(max(1, args.steps)):
+        t = time.time()
+        L2 = P.build(g, order)
+        o2, h2, d2 = L2.export()
+        e2e_s.append(time.time() - t)
+        d2h = o2.nbytes + h2.nbytes + d2.nbytes
+        del L2, o2, h2, d2
+    e2e = ws * labels / float(np.mean(e2e_s))
+    launches = int(stats[-1]["kernel_launches"])
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
+        "config": {"workload": f"grid{args.side}x{args.side}+hw{args.highways}, betweenness({args.sources}), full build",
+                   "vertices": n, "arcs": int(g.out_arcs()), "l2": "inputs larger than L2 (label CSR of several GB)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "clocks": ck.summary(),
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": (traffic or {}).get("bytes_per_unit_scaled"),
+                     "kernel": "tree_kernel", "algorithmic_bytes_per_build": work,
+                     "tree_ms_per_build": avg_tree_ms, "tree_launches": stats[-1]["tree_launches"],
+                     "ms_per_launch": per_launch_tree},
+        "build": {"build_s": ms_step / 1e3, "avg_label": stats[-1]["avg_label"], "labels": labels,
+                  "supersteps": stats[-1]["supersteps"], "tree_ms": avg_tree_ms,
+                  "commit_ms": float(np.mean([s["commit_ms"] for s in stats])),
+                  "visits": stats[-1]["visits"], "label_reads": stats[-1]["label_reads"],
+                  "wall_s_per_step": wall / args.steps},
+        "query": {"pairs": qk, "qps": qps, "ms_per_batch": q_ms, "bytes_per_batch": q_bytes,
+                  "achieved_gbs": q_bytes / (q_ms / 1e3) / 1e9},
+    }
+    if rank == 0 and not args.no_cpu:
+        og, r, threads, lab, secs = cpu_sample(g, order, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": lab / secs, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"GLL restatement on the first {r} of {n} roots (both sides)",
+                                "seconds": secs}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    ws, rank = dist_info()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank)
+
+
+if __name__ == "__main__":
+    main()

@@ -88,6 +88,18 @@ uint32_t chl_graph_degree(const chl_graph *g, uint32_t v);
 int chl_graph_arcs(const chl_graph *g, uint32_t v, int forward,
                    uint32_t *heads, int32_t *lens, uint32_t cap,
                    uint32_t *cnt);
+/* Per-vertex arc counts of one direction (forward = 1: out-arcs). */
+int chl_graph_degrees(const chl_graph *g, int forward, uint32_t *deg);
+/* Copy one direction's adjacency as CSR: off has n+1 entries; head/len
+ * have chl_graph_out_arcs (forward) or the in-arc count entries; head/len
+ * may be NULL. */
+int chl_graph_export(const chl_graph *g, int forward, uint64_t *off, uint32_t *head,
+                     int32_t *len);
+/* Keep a device copy of the adjacency in the graph handle, so builds start
+ * with their input resident in HBM (no counterpart: the reference is CPU
+ * only).  chl_graph_free releases it. */
+int chl_graph_to_device(chl_graph *g);
+int chl_graph_release_device(chl_graph *g);
 void chl_graph_free(chl_graph *g);
 
 /* Seeded synthetic generators (no reference counterpart; they stand in for
@@ -196,6 +208,8 @@ uint64_t chl_labels_total(const chl_labels *l);
  * array may be NULL to query the size in *cnt. */
 int chl_labels_get(const chl_labels *l, uint32_t v, int side, uint32_t *hubs,
                    int32_t *dists, uint32_t cap, uint32_t *cnt);
+/* sizes[2v+side] = |L(v, side)| (2n entries). */
+int chl_labels_list_sizes(const chl_labels *l, uint32_t *sizes);
 /* Copy all labels to host CSR arrays: off has 2n+1 entries (index 2v+side),
  * hubs/dists have chl_labels_total entries. */
 int chl_labels_export(const chl_labels *l, uint64_t *off, uint32_t *hubs,
@@ -221,6 +235,13 @@ int chl_query_batch(const chl_labels *l, const uint32_t *pairs, size_t k,
 /* Same, with DEVICE pointers; returns after the launch (asynchronous). */
 int chl_query_batch_device(const chl_labels *l, const uint32_t *d_pairs,
                            size_t k, int32_t *d_out, void *stream);
+/* Device-resident query benchmark (no reference counterpart): k uniform
+ * pairs generated on the device, `iters` timed launches of the batch query
+ * kernel (CUDA events on its own stream); returns the mean ms per launch
+ * and the algorithmic bytes of one launch (8 B per label entry of both
+ * lists, plus the 8-byte pair and 4-byte answer). */
+int chl_query_bench(const chl_labels *l, size_t k, uint64_t seed, int iters,
+                    double *ms_per_iter, uint64_t *bytes_per_iter);
 /* Replaces hl::generate_query (distributed_memory/query.hpp:43-51) with a
  * seeded generator: k uniform pairs over [0, range). */
 int chl_query_generate(uint32_t *pairs, size_t k, uint32_t range,

@@ -89,6 +89,10 @@ SIGNATURES = {
     "chl_graph_symmetric": (C.c_int, [_P]),
     "chl_graph_degree": (C.c_uint32, [_P, C.c_uint32]),
     "chl_graph_arcs": (C.c_int, [_P, C.c_uint32, C.c_int, _U32P, _I32P, C.c_uint32, _U32P]),
+    "chl_graph_degrees": (C.c_int, [_P, C.c_int, _U32P]),
+    "chl_graph_export": (C.c_int, [_P, C.c_int, _U64P, _U32P, _I32P]),
+    "chl_graph_to_device": (C.c_int, [_P]),
+    "chl_graph_release_device": (C.c_int, [_P]),
     "chl_graph_free": (None, [_P]),
     "chl_gen_grid": (C.c_int, [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_int32, C.c_int32,
                                C.c_uint32, C.c_uint32, C.c_double, C.c_uint64, C.POINTER(_P)]),
@@ -108,12 +112,14 @@ SIGNATURES = {
     "chl_labels_n": (C.c_uint32, [_P]),
     "chl_labels_total": (C.c_uint64, [_P]),
     "chl_labels_get": (C.c_int, [_P, C.c_uint32, C.c_int, _U32P, _I32P, C.c_uint32, _U32P]),
+    "chl_labels_list_sizes": (C.c_int, [_P, _U32P]),
     "chl_labels_export": (C.c_int, [_P, _U64P, _U32P, _I32P]),
     "chl_labels_import": (C.c_int, [C.c_uint32, _U64P, _U32P, _I32P, C.POINTER(_P)]),
     "chl_labels_hub_freq": (C.c_int, [_P, _U32P, _U32P]),
     "chl_labels_free": (None, [_P]),
     "chl_query_batch": (C.c_int, [_P, _U32P, C.c_size_t, _I32P, _P]),
     "chl_query_batch_device": (C.c_int, [_P, _P, C.c_size_t, _P, _P]),
+    "chl_query_bench": (C.c_int, [_P, C.c_size_t, C.c_uint64, C.c_int, C.POINTER(C.c_double), _U64P]),
     "chl_query_generate": (C.c_int, [_U32P, C.c_size_t, C.c_uint32, C.c_uint64]),
     "chl_query_load": (C.c_int, [C.c_char_p, C.POINTER(_U32P), C.POINTER(C.c_size_t)]),
     "chl_server_opts_default": (None, [C.POINTER(ServerOpts)]),
@@ -227,14 +233,25 @@ class Graph:
     def csr(self, forward: bool = True):
         """(off, head, len) numpy arrays of one direction."""
         n = self.get_n()
-        heads, lens, off = [], [], [0]
-        for v in range(n):
-            h, w = self.arcs(v, forward)
-            heads.append(h)
-            lens.append(w)
-            off.append(off[-1] + len(h))
-        return (np.array(off, np.uint64), np.concatenate(heads) if heads else np.zeros(0, np.uint32),
-                np.concatenate(lens) if lens else np.zeros(0, np.int32))
+        off = np.zeros(n + 1, np.uint64)
+        _check(lib().chl_graph_export(self._h, int(forward), _ptr(off, _U64P), None, None), "export")
+        m = int(off[-1])
+        head = np.zeros(max(m, 1), np.uint32)
+        ln = np.zeros(max(m, 1), np.int32)
+        _check(lib().chl_graph_export(self._h, int(forward), _ptr(off, _U64P), _ptr(head, _U32P),
+                                      _ptr(ln, _I32P)), "export")
+        return off, head[:m], ln[:m]
+
+    def degrees(self, forward: bool = True) -> np.ndarray:
+        d = np.zeros(self.get_n(), np.uint32)
+        _check(lib().chl_graph_degrees(self._h, int(forward), _ptr(d, _U32P)), "degrees")
+        return d
+
+    def to_device(self) -> None:
+        _check(lib().chl_graph_to_device(self._h), "graph to device")
+
+    def release_device(self) -> None:
+        _check(lib().chl_graph_release_device(self._h), "graph release")
 
     def __del__(self):
         if getattr(self, "_h", None) and _lib is not None:
@@ -329,6 +346,12 @@ class Labeling:
                "export")
         return off, hub[:t], dist[:t]
 
+    def list_sizes(self) -> np.ndarray:
+        """sizes[2v+side] = |L(v, side)|."""
+        z = np.zeros(2 * self.n(), np.uint32)
+        _check(lib().chl_labels_list_sizes(self._h, _ptr(z, _U32P)), "list sizes")
+        return z
+
     def stats(self) -> dict:
         s = BuildStats()
         _check(lib().chl_build_get_stats(self._h, C.byref(s)), "stats")
@@ -382,6 +405,14 @@ def query(labels: Labeling, pairs) -> np.ndarray:
     out = np.zeros(len(p), np.int32)
     _check(lib().chl_query_batch(labels._h, _ptr(p, _U32P), len(p), _ptr(out, _I32P), None), "query")
     return out
+
+
+def query_bench(labels: Labeling, k: int, iters: int = 10, seed: int = 1):
+    """(ms per launch, algorithmic bytes per launch) of k device-resident pairs."""
+    ms = C.c_double()
+    b = C.c_uint64()
+    _check(lib().chl_query_bench(labels._h, k, seed, iters, C.byref(ms), C.byref(b)), "query bench")
+    return ms.value, b.value
 
 
 def generate_query(k: int, n: int, seed: int = 1) -> np.ndarray:

@@ -565,10 +565,14 @@ struct DevGraph {
     uint2 *arc[2] = {nullptr, nullptr};
     uint32_t *head[2] = {nullptr, nullptr};
     void release() {
+        // side 1 may alias side 0 (symmetric graphs): free each buffer once
+        if (off[1] != off[0]) cudaFree(off[1]);
+        if (arc[1] != arc[0]) cudaFree(arc[1]);
+        if (head[1] != head[0]) cudaFree(head[1]);
+        cudaFree(off[0]);
+        cudaFree(arc[0]);
+        cudaFree(head[0]);
         for (int s = 0; s < 2; ++s) {
-            if (off[s] && (s == 0 || off[s] != off[0])) cudaFree(off[s]);
-            if (arc[s] && (s == 0 || arc[s] != arc[0])) cudaFree(arc[s]);
-            if (head[s] && (s == 0 || head[s] != head[0])) cudaFree(head[s]);
             off[s] = nullptr;
             arc[s] = nullptr;
             head[s] = nullptr;
@@ -607,6 +611,19 @@ int upload_graph(const chl_graph *g, DevGraph &dg, cudaStream_t st) {
     return CHL_OK;
 }
 
+}  // namespace
+
+void graph_release_device(chl_graph *g) {
+    if (g && g->dev) {
+        DevGraph *d = (DevGraph *)g->dev;
+        d->release();
+        delete d;
+        g->dev = nullptr;
+    }
+}
+
+namespace {
+
 struct Build {
     // sizes
     uint32_t n = 0;
@@ -615,7 +632,8 @@ struct Build {
     int hub_bits = 0;
     int key_bits = 0;
     // device buffers
-    DevGraph dg;
+    DevGraph own;                   // graph uploaded for this build only
+    const DevGraph *dg = nullptr;
     uint32_t *order = nullptr, *rank = nullptr;
     uint64_t *off_a = nullptr, *off_b = nullptr;
     uint2 *ent_a = nullptr, *ent_b = nullptr;
@@ -638,7 +656,7 @@ struct Build {
     uint32_t rcap = 0;
 
     ~Build() {
-        dg.release();
+        own.release();
         cudaFree(order);
         cudaFree(rank);
         cudaFree(off_a);
@@ -738,25 +756,31 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     b.key_bits = b.hub_bits + bits_for((uint64_t)b.nl + 1);
     if (b.key_bits > 64) return CHL_ERR_INVALID;
     CHL_CUDA(cudaStreamCreateWithFlags(&b.st, cudaStreamNonBlocking));
-    cudaEvent_t ev0, ev1, ev_a, ev_b;
+    cudaEvent_t ev0, ev1, ev_a, ev_b, ev_up;
+    CHL_CUDA(cudaEventCreate(&ev_up));
     CHL_CUDA(cudaEventCreate(&ev0));
     CHL_CUDA(cudaEventCreate(&ev1));
     CHL_CUDA(cudaEventCreate(&ev_a));
     CHL_CUDA(cudaEventCreate(&ev_b));
     struct EvGuard {
-        cudaEvent_t e[4];
+        cudaEvent_t e[5];
         ~EvGuard() {
             for (auto x : e) cudaEventDestroy(x);
         }
-    } evg{{ev0, ev1, ev_a, ev_b}};
+    } evg{{ev0, ev1, ev_a, ev_b, ev_up}};
 
     CHL_CUDA(cudaEventRecord(ev0, b.st));
-    int rc = upload_graph(g, b.dg, b.st);
-    if (rc) return rc;
+    int rc;
+    if (g->dev) {
+        b.dg = (const DevGraph *)g->dev;
+    } else {
+        if ((rc = upload_graph(g, b.own, b.st))) return rc;
+        b.dg = &b.own;
+    }
     if ((rc = dalloc(&b.order, n)) || (rc = dalloc(&b.rank, n))) return rc;
     CHL_CUDA(cudaMemcpyAsync(b.order, order_h, (size_t)n * 4, cudaMemcpyHostToDevice, b.st));
     CHL_CUDA(cudaMemcpyAsync(b.rank, rank_h.data(), (size_t)n * 4, cudaMemcpyHostToDevice, b.st));
-    CHL_CUDA(cudaEventRecord(ev_a, b.st));
+    CHL_CUDA(cudaEventRecord(ev_up, b.st));
 
     // committed label CSR (double buffered)
     if ((rc = dalloc(&b.off_a, (size_t)b.nl + 1)) || (rc = dalloc(&b.off_b, (size_t)b.nl + 1)))
@@ -800,7 +824,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     uint32_t r0 = 0;
     uint64_t committed = 0;
     uint32_t supersteps = 0, plant_roots = 0;
-    unsigned long long visits = 0, reads = 0, arcs = 0, launches = 0;
+    unsigned long long visits = 0, reads = 0, arcs = 0, launches = 0, kernels = 0;
     double tree_ms = 0, sort_ms = 0, commit_ms = 0;
     uint32_t max_list = 0;   // longest committed list
     while (r0 < n) {
@@ -827,9 +851,9 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             ta.n = n;
             ta.sides = b.sides;
             for (int s = 0; s < 2; ++s) {
-                ta.g_off[s] = b.dg.off[s];
-                ta.g_arc[s] = b.dg.arc[s];
-                ta.g_head[s] = b.dg.head[s];
+                ta.g_off[s] = b.dg->off[s];
+                ta.g_arc[s] = b.dg->arc[s];
+                ta.g_head[s] = b.dg->head[s];
             }
             ta.order = b.order;
             ta.rank = b.rank;
@@ -860,10 +884,11 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             CHL_CUDA(cudaGetLastError());
             CHL_CUDA(cudaEventRecord(ev_b, b.st));
             ++launches;
+            ++kernels;
             CHL_CUDA(cudaMemcpyAsync(&hc, b.ctl, sizeof(hc), cudaMemcpyDeviceToHost, b.st));
             CHL_CUDA(cudaStreamSynchronize(b.st));
             float ms = 0;
-            cudaEventElapsedTime(&ms, ev_a, ev_b);
+            CHL_CUDA(cudaEventElapsedTime(&ms, ev_a, ev_b));
             tree_ms += ms;
             uint32_t r1 = (uint32_t)std::min<unsigned long long>(hc.next_root, r_end);
             if (hc.err) {
@@ -892,6 +917,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             unsigned long long zero = 0;
             CHL_CUDA(cudaMemcpyAsync(&b.ctl->max_ratio_num, &zero, 8, cudaMemcpyHostToDevice, b.st));
             ratio_max<<<std::max(1, sms), 256, 0, b.st>>>(b.tsize, b.tlab, &b.ctl->next_root, r0, r1, b.ctl);
+            ++kernels;
             unsigned long long bits = 0;
             CHL_CUDA(cudaMemcpyAsync(&bits, &b.ctl->max_ratio_num, 8, cudaMemcpyDeviceToHost, b.st));
             CHL_CUDA(cudaStreamSynchronize(b.st));
@@ -908,6 +934,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         if ((rc = radix_sort_pairs(b.nk0, b.nv0, b.nk1, b.nv1, (const uint64_t *)&b.ctl->nlab,
                                    b.new_cap, b.key_bits, b.tmp, b.tmp_bytes, b.st, &parity)))
             return rc;
+        kernels += 3 * ((b.key_bits + 7) / 8);
         uint64_t *sk = parity ? b.nk1 : b.nk0;
         uint32_t *sv = parity ? b.nv1 : b.nv0;
         uint64_t *ak = parity ? b.nk0 : b.nk1;
@@ -927,6 +954,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             compact_kept<<<cgrid, 256, 0, b.st>>>(sk, sv, b.keep, b.kpre, d_count, b.new_cap, ak, av,
                                                   &b.ctl->n_keep);
             CHL_CUDA(cudaMemcpyAsync(&b.ctl->nlab, &b.ctl->n_keep, 8, cudaMemcpyDeviceToDevice, b.st));
+            kernels += 9;   // count, scan x3, clean, scan x3, compact
             std::swap(sk, ak);
             std::swap(sv, av);
             CHL_CUDA(cudaMemcpyAsync(&M, &b.ctl->n_keep, 8, cudaMemcpyDeviceToHost, b.st));
@@ -943,6 +971,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         place_new<<<cgrid, 256, 0, b.st>>>(sk, sv, d_count, b.new_cap, b.hub_bits, r0, b.pre, b.off_a,
                                            b.off_b, b.ent_b);
         CHL_CUDA(cudaGetLastError());
+        kernels += 7;   // count, scan x3, offsets, copy, place
         std::swap(b.off_a, b.off_b);
         std::swap(b.ent_a, b.ent_b);
         std::swap(b.ent_cap_a, b.ent_cap_b);
@@ -951,12 +980,13 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         // longest committed list, for the next superstep's root staging
         CHL_CUDA(cudaMemsetAsync(&b.ctl->max_ratio_den, 0, 8, b.st));
         max_list_len<<<cgrid, 256, 0, b.st>>>(b.off_a, b.nl, &b.ctl->max_ratio_den);
+        ++kernels;
         unsigned long long mx = 0;
         CHL_CUDA(cudaMemcpyAsync(&mx, &b.ctl->max_ratio_den, 8, cudaMemcpyDeviceToHost, b.st));
         CHL_CUDA(cudaStreamSynchronize(b.st));
         max_list = (uint32_t)std::min<unsigned long long>(mx, 0xFFFFFFFFu);
         float ms1 = 0;
-        cudaEventElapsedTime(&ms1, ev_b, ev_a);
+        CHL_CUDA(cudaEventElapsedTime(&ms1, ev_b, ev_a));
         commit_ms += ms1;
         ++supersteps;
         r0 = r1;
@@ -967,8 +997,9 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     }
     CHL_CUDA(cudaEventRecord(ev1, b.st));
     CHL_CUDA(cudaStreamSynchronize(b.st));
-    float total_ms = 0;
-    cudaEventElapsedTime(&total_ms, ev0, ev1);
+    float total_ms = 0, up_ms = 0;
+    CHL_CUDA(cudaEventElapsedTime(&total_ms, ev_up, ev1));
+    CHL_CUDA(cudaEventElapsedTime(&up_ms, ev0, ev_up));
 
     chl_labels *L = new (std::nothrow) chl_labels();
     if (!L) return CHL_ERR_OOM;
@@ -981,6 +1012,8 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     b.ent_a = nullptr;
     chl_build_stats &S = L->stats;
     S.build_ms = total_ms;
+    S.h2d_ms = up_ms;
+    S.kernel_launches = kernels;
     S.tree_ms = tree_ms;
     S.sort_ms = sort_ms;
     S.commit_ms = commit_ms;
@@ -1025,6 +1058,31 @@ extern "C" int chl_build(const chl_graph *g, const uint32_t *order, uint32_t n,
         chl::set_error("host allocation failed during build");
         return CHL_ERR_OOM;
     }
+}
+
+extern "C" int chl_graph_to_device(chl_graph *g) {
+    if (!g) return CHL_ERR_INVALID;
+    if (g->dev) return CHL_OK;
+    chl::DevGraph *d = new (std::nothrow) chl::DevGraph();
+    if (!d) return CHL_ERR_OOM;
+    int rc = chl::upload_graph(g, *d, 0);
+    if (rc == CHL_OK) {
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) rc = chl::cuda_status(e, "graph upload", __FILE__, __LINE__);
+    }
+    if (rc != CHL_OK) {
+        d->release();
+        delete d;
+        return rc;
+    }
+    g->dev = d;
+    return CHL_OK;
+}
+
+extern "C" int chl_graph_release_device(chl_graph *g) {
+    if (!g) return CHL_ERR_INVALID;
+    chl::graph_release_device(g);
+    return CHL_OK;
 }
 
 extern "C" int chl_build_get_stats(const chl_labels *l, chl_build_stats *s) {

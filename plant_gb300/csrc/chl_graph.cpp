@@ -418,6 +418,23 @@ extern "C" uint32_t chl_graph_degree(const chl_graph *g, uint32_t v) {
     return (uint32_t)((g->off[1][v + 1] - g->off[1][v]) + (g->off[0][v + 1] - g->off[0][v]));
 }
 
+extern "C" int chl_graph_degrees(const chl_graph *g, int forward, uint32_t *deg) {
+    if (!g || !deg) return CHL_ERR_INVALID;
+    const int s = forward ? 1 : 0;
+    for (uint32_t v = 0; v < g->n; ++v) deg[v] = (uint32_t)(g->off[s][v + 1] - g->off[s][v]);
+    return CHL_OK;
+}
+
+extern "C" int chl_graph_export(const chl_graph *g, int forward, uint64_t *off, uint32_t *head,
+                                int32_t *len) {
+    if (!g || !off) return CHL_ERR_INVALID;
+    const int s = forward ? 1 : 0;
+    std::copy(g->off[s].begin(), g->off[s].end(), off);
+    if (head) std::copy(g->head[s].begin(), g->head[s].end(), head);
+    if (len) std::copy(g->len[s].begin(), g->len[s].end(), len);
+    return CHL_OK;
+}
+
 extern "C" int chl_graph_arcs(const chl_graph *g, uint32_t v, int forward,
                               uint32_t *heads, int32_t *lens, uint32_t cap,
                               uint32_t *cnt) {
@@ -435,7 +452,11 @@ extern "C" int chl_graph_arcs(const chl_graph *g, uint32_t v, int forward,
     return CHL_OK;
 }
 
-extern "C" void chl_graph_free(chl_graph *g) { delete g; }
+extern "C" void chl_graph_free(chl_graph *g) {
+    if (!g) return;
+    graph_release_device(g);
+    delete g;
+}
 
 // ------------------------------------------------------------ generators
 //

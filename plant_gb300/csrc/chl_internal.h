@@ -64,6 +64,7 @@ struct chl_graph {
     bool symmetric = false;
     bool unit = false;               // every arc length is 1
     int32_t min_len = 0, max_len = 0;
+    void *dev = nullptr;             // device CSR (chl_graph_to_device), owned
 };
 
 // One label entry: hub rank and distance (8 bytes, read as uint2 on device).
@@ -99,6 +100,8 @@ int labels_ensure_device(const chl_labels *l);
 // when both sides are identical.
 int labels_from_host(uint32_t n, const uint64_t *off2, const uint32_t *hub,
                      const int32_t *dist, chl_labels **out);
+// free the device copy of a graph (no-op without one)
+void graph_release_device(chl_graph *g);
 int build_labels(const chl_graph *g, const uint32_t *order, uint32_t n,
                  const chl_build_opts *opts, chl_labels **out);
 // build a graph from unique undirected edges (u < v), symmetric CSR

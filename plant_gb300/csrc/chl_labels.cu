@@ -173,6 +173,33 @@ __global__ void query_kernel(const uint64_t *__restrict__ off, const uint2 *__re
     }
 }
 
+__device__ __forceinline__ uint64_t qmix(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// Uniform random pairs generated on the device (query benchmark input).
+__global__ void gen_pairs(uint32_t *pairs, size_t k, uint32_t n, uint64_t seed) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < 2 * k;
+         i += (size_t)gridDim.x * blockDim.x)
+        pairs[i] = (uint32_t)(qmix(seed ^ (i * 0xD1B54A32D192ED03ull)) % n);
+}
+
+// Algorithmic bytes of a query batch: 8 (|L(s,1)| + |L(t,0)|) + 8 + 4 per pair.
+__global__ void query_bytes(const uint64_t *off, int sym, const uint32_t *pairs, size_t k,
+                            unsigned long long *bytes) {
+    unsigned long long acc = 0;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < k; q += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t s = pairs[2 * q], t = pairs[2 * q + 1];
+        const uint32_t xa = sym ? s : 2 * s + 1, xb = sym ? t : 2 * t;
+        acc += 8ull * ((off[xa + 1] - off[xa]) + (off[xb + 1] - off[xb])) + 12ull;
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(bytes, acc);
+}
+
 __global__ void hub_count(const uint2 *ent, uint64_t total, uint32_t *cnt) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
          i += (uint64_t)gridDim.x * blockDim.x)
@@ -223,6 +250,26 @@ extern "C" int chl_labels_get(const chl_labels *l, uint32_t v, int side, uint32_
     return CHL_OK;
 }
 
+extern "C" int chl_labels_list_sizes(const chl_labels *l, uint32_t *sizes) {
+    if (!l || !sizes) return CHL_ERR_INVALID;
+    const uint32_t nl = l->nl();
+    std::vector<uint64_t> off;
+    const uint64_t *o;
+    if (l->host_valid) {
+        o = l->h_off.data();
+    } else {
+        off.resize((size_t)nl + 1);
+        CHL_CUDA(cudaMemcpy(off.data(), l->d_off, ((size_t)nl + 1) * 8, cudaMemcpyDeviceToHost));
+        o = off.data();
+    }
+    for (uint32_t v = 0; v < l->n; ++v)
+        for (int side = 0; side < 2; ++side) {
+            const uint32_t x = l->list(v, side);
+            sizes[2 * (size_t)v + side] = (uint32_t)(o[x + 1] - o[x]);
+        }
+    return CHL_OK;
+}
+
 extern "C" int chl_labels_export(const chl_labels *l, uint64_t *off, uint32_t *hubs,
                                  int32_t *dists) {
     if (!l || !off) return CHL_ERR_INVALID;
@@ -254,7 +301,11 @@ extern "C" int chl_labels_hub_freq(const chl_labels *l, const uint32_t *order, u
     if (rc) return rc;
     uint32_t *d_cnt = nullptr;
     CHL_CUDA(cudaMalloc(&d_cnt, (size_t)std::max<uint32_t>(l->n, 1) * 4));
-    cudaMemset(d_cnt, 0, (size_t)l->n * 4);
+    cudaError_t em = cudaMemset(d_cnt, 0, (size_t)l->n * 4);
+    if (em != cudaSuccess) {
+        cudaFree(d_cnt);
+        return cuda_status(em, "cudaMemset", __FILE__, __LINE__);
+    }
     if (l->total)
         hub_count<<<device_sms() * 8, 256>>>((const uint2 *)l->d_ent, l->total, d_cnt);
     std::vector<uint32_t> cnt(l->n);
@@ -276,6 +327,51 @@ extern "C" int chl_query_batch_device(const chl_labels *l, const uint32_t *d_pai
                                       int32_t *d_out, void *stream) {
     if (!l || (k && (!d_pairs || !d_out))) return CHL_ERR_INVALID;
     return query_launch(l, d_pairs, k, d_out, (cudaStream_t)stream);
+}
+
+extern "C" int chl_query_bench(const chl_labels *l, size_t k, uint64_t seed, int iters,
+                               double *ms_per_iter, uint64_t *bytes_per_iter) {
+    if (!l || !ms_per_iter || k == 0 || iters < 1 || l->n == 0) return CHL_ERR_INVALID;
+    int rc = labels_ensure_device(l);
+    if (rc) return rc;
+    uint32_t *dp = nullptr;
+    int32_t *dout = nullptr;
+    unsigned long long *dbytes = nullptr;
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaMalloc(&dp, k * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&dout, k * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&dbytes, 8);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    float ms = 0;
+    unsigned long long bytes = 0;
+    if (e == cudaSuccess) {
+        gen_pairs<<<device_sms() * 8, 256, 0, st>>>(dp, k, l->n, seed);
+        cudaMemsetAsync(dbytes, 0, 8, st);
+        query_bytes<<<device_sms() * 8, 256, 0, st>>>(l->d_off, l->sym ? 1 : 0, dp, k, dbytes);
+        rc = query_launch(l, dp, k, dout, st);   // warm-up
+        if (rc == CHL_OK) {
+            cudaEventRecord(e0, st);
+            for (int i = 0; i < iters && rc == CHL_OK; ++i) rc = query_launch(l, dp, k, dout, st);
+            cudaEventRecord(e1, st);
+        }
+        e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e == cudaSuccess) e = cudaMemcpy(&bytes, dbytes, 8, cudaMemcpyDeviceToHost);
+    }
+    if (e != cudaSuccess && rc == CHL_OK) rc = cuda_status(e, "query bench", __FILE__, __LINE__);
+    cudaFree(dp);
+    cudaFree(dout);
+    cudaFree(dbytes);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (st) cudaStreamDestroy(st);
+    if (rc) return rc;
+    *ms_per_iter = ms / iters;
+    if (bytes_per_iter) *bytes_per_iter = bytes;
+    return CHL_OK;
 }
 
 extern "C" int chl_query_batch(const chl_labels *l, const uint32_t *pairs, size_t k, int32_t *out,
