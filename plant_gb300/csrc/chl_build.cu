@@ -36,7 +36,7 @@ namespace chl {
 namespace {
 
 constexpr uint32_t kInf = 0xFFFFFFFFu;
-constexpr int kHeapSmem = 128;      // heap slots kept in shared memory per warp
+constexpr int kHeapSmem = 256;      // heap slots kept in shared memory per warp
 constexpr int kWarpsPerBlock = 4;
 constexpr int kStage = 32;          // label staging entries per warp
 
@@ -302,13 +302,30 @@ tree_kernel(TreeArgs a) {
                 } else {
                     if (a.rank[u] < r) continue;   // iteration_gll :92
                 }
-                bool pruned = false;
                 const uint32_t uidx = lidx(u, 1 - f, a.sides);
+                // Issue the independent loads of this step together: the
+                // label list bounds of u, its arc range, and the first chunk
+                // of arcs with the heads' ranks and keys.  They overlap with
+                // the prune test; if u is pruned they are simply unused.
+                const uint64_t ub = a.l_off[uidx], ue = a.l_off[uidx + 1];
+                const uint64_t ab = goff[u], ae = goff[u + 1];
+                uint32_t pw = 0, plen = 0, prank = 0, pkey = kInf;
+                if (ab + lane < ae) {
+                    if (UNIT) {
+                        pw = ghead[ab + lane];
+                        plen = 1;
+                    } else {
+                        const uint2 hl = garc[ab + lane];
+                        pw = hl.x;
+                        plen = hl.y;
+                    }
+                    if (PLANT) prank = a.rank[pw];
+                    pkey = key[pw];
+                }
+                bool pruned = false;
                 if (R > 0) {
-                    const uint64_t ub = a.l_off[uidx], ue = a.l_off[uidx + 1];
                     uint32_t nr = 0;
-                    pruned = prune_test(rh, rd, rstride, R, a.l_ent + ub,
-                                        (uint32_t)(ue - ub), d, nr);
+                    pruned = prune_test(rh, rd, rstride, R, a.l_ent + ub, (uint32_t)(ue - ub), d, nr);
                     c_reads += nr;
                 }
                 if (!pruned) {
@@ -321,29 +338,37 @@ tree_kernel(TreeArgs a) {
                         ++t_lab;
                         if (nstage == kStage) flush();
                     }
-                    const uint64_t ab = goff[u], ae = goff[u + 1];
                     c_arcs += ae - ab;
                     for (uint64_t e0 = ab; e0 < ae; e0 += 32) {
                         const uint64_t e = e0 + lane;
                         bool upd = false;
                         uint32_t w = 0, nk = 0, old = kInf;
                         if (e < ae) {
-                            uint32_t len;
-                            if (UNIT) {
-                                w = ghead[e];
-                                len = 1;
+                            uint32_t len, rk, kw;
+                            if (e0 == ab) {
+                                w = pw;
+                                len = plen;
+                                rk = prank;
+                                kw = pkey;
                             } else {
-                                uint2 hl = garc[e];
-                                w = hl.x;
-                                len = hl.y;
+                                if (UNIT) {
+                                    w = ghead[e];
+                                    len = 1;
+                                } else {
+                                    const uint2 hl = garc[e];
+                                    w = hl.x;
+                                    len = hl.y;
+                                }
+                                rk = PLANT ? a.rank[w] : 0u;
+                                kw = key[w];
                             }
                             const uint64_t dd64 = (uint64_t)d + len;
                             if (dd64 < 0x7FFFFFFFull) {
                                 const uint32_t dd = (uint32_t)dd64;
                                 uint32_t nv = 1u;
-                                if (PLANT) nv = (nonvia && a.rank[w] >= r) ? 1u : 0u;
+                                if (PLANT) nv = (nonvia && rk >= r) ? 1u : 0u;
                                 nk = dd * 2u + nv;
-                                old = key[w];
+                                old = kw;
                                 upd = nk < old;
                                 if (upd) key[w] = nk;
                             } else {
@@ -813,6 +838,22 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         if ((rc = dalloc(&b.ws_pos, slots * n)) || (rc = dalloc(&b.ws_heap, slots * n))) return rc;
     }
 
+    // Schedule defaults from graph statistics: heavy-tailed degree
+    // distributions (scale-free) start with few roots so the hubs commit
+    // before the bulk of the trees; bounded-degree (road-like) graphs start
+    // with one root per resident warp.
+    uint32_t auto_first;
+    double auto_growth;
+    {
+        uint64_t arcs_out = g->off[1][n];
+        uint64_t maxdeg = 0;
+        for (uint32_t v = 0; v < n; ++v) maxdeg = std::max<uint64_t>(maxdeg, g->off[1][v + 1] - g->off[1][v]);
+        const double avgdeg = n ? (double)arcs_out / n : 0.0;
+        const bool heavy = maxdeg > 32.0 * std::max(1.0, avgdeg);
+        auto_first = heavy ? 64u : std::max<uint32_t>(64u, b.warps);
+        auto_growth = heavy ? 1.0 : 0.5;
+    }
+
     // superstep loop
     const double sf = opts.sf > 0 ? opts.sf : 32.0;
     // label_limit = sf * N counts both sides' labels (shared_memory/hhl.cpp:65);
@@ -827,10 +868,18 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     unsigned long long visits = 0, reads = 0, arcs = 0, launches = 0, kernels = 0;
     double tree_ms = 0, sort_ms = 0, commit_ms = 0;
     uint32_t max_list = 0;   // longest committed list
+    // Superstep schedule: superstep k covers roots [r0, r0 + size) with
+    // size = clamp(growth * r0, first, n) -- small while the top hubs are not
+    // yet committed (their labels prune everything later), geometric after.
+    // The label budget sf * n (the reference's label_limit) also ends a
+    // superstep early.
+    const uint32_t first = opts.first_superstep ? opts.first_superstep : auto_first;
+    const double growth = opts.growth > 0 ? opts.growth : auto_growth;
     while (r0 < n) {
         const bool plant_now = do_plant;
         const unsigned long long budget = budget_base;
-        uint32_t r_end = n;
+        uint64_t size = std::max<uint64_t>(first, (uint64_t)(growth * (double)r0));
+        uint32_t r_end = (uint32_t)std::min<uint64_t>(n, (uint64_t)r0 + size);
         BuildCtl hc;
         bool rerun = false;
         // root label staging capacity: longest committed list, bounded by smem
