@@ -160,7 +160,8 @@ typedef struct chl_build_opts {
     uint32_t first_superstep; /* roots in the first superstep, 0 = auto       */
     double growth;        /* superstep growth factor, 0 = auto                */
     uint32_t max_warps;   /* cap on concurrent trees, 0 = auto                */
-    uint32_t reserved[8];
+    int32_t tree_algo;    /* 0: batched settle (default), 1: binary heap      */
+    uint32_t reserved[7];
 } chl_build_opts;
 
 /* Fill opts with the defaults (hybrid, sf 32, ps 1024, autotune on). */

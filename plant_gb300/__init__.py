@@ -49,7 +49,7 @@ class BuildOpts(C.Structure):
     _fields_ = [("mode", C.c_int32), ("sf", C.c_double), ("ps", C.c_double),
                 ("autotune", C.c_int32), ("use_graphs", C.c_int32), ("verbose", C.c_int32),
                 ("first_superstep", C.c_uint32), ("growth", C.c_double),
-                ("max_warps", C.c_uint32), ("reserved", C.c_uint32 * 8)]
+                ("max_warps", C.c_uint32), ("tree_algo", C.c_int32), ("reserved", C.c_uint32 * 7)]
 
 
 class BuildStats(C.Structure):
@@ -374,7 +374,8 @@ class Labeling:
 
 
 def build(g: Graph, order, mode: int = MODE_HYBRID, sf: float = 32.0, ps: float = 1024.0,
-          verbose: int = 0, max_warps: int = 0, autotune: int = 1) -> Labeling:
+          verbose: int = 0, max_warps: int = 0, autotune: int = 1, tree_algo: int = 0,
+          first_superstep: int = 0, growth: float = 0.0) -> Labeling:
     o = _u32(order)
     opts = BuildOpts()
     lib().chl_build_opts_default(C.byref(opts))
@@ -384,6 +385,9 @@ def build(g: Graph, order, mode: int = MODE_HYBRID, sf: float = 32.0, ps: float 
     opts.verbose = verbose
     opts.max_warps = max_warps
     opts.autotune = autotune
+    opts.tree_algo = tree_algo
+    opts.first_superstep = first_superstep
+    opts.growth = growth
     h = C.c_void_p()
     _check(lib().chl_build(g._h, _ptr(o, _U32P), len(o), C.byref(opts), C.byref(h)), "build")
     return Labeling(h)

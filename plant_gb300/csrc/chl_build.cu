@@ -77,6 +77,8 @@ struct TreeArgs {
     uint64_t *ws_heap;
     BuildCtl *ctl;
     uint32_t rcap;                  // root label entries staged in smem
+    const uint32_t *win[2];         // [f]: shortest arc into v along direction f
+    uint32_t *ws_front;             // per warp slot: queued (unsettled) vertices
 };
 
 __device__ __forceinline__ uint32_t lidx(uint32_t v, int side, int sides) {
@@ -430,6 +432,322 @@ tree_kernel(TreeArgs a) {
     if (lane == 0) atomicAdd(&a.ctl->label_reads, c_reads);
 }
 
+// ------------------------------------------------------ batch tree kernel
+//
+// One tree per warp, settled in batches.  A queued vertex v is final (its
+// distance AND its via flag) once d(v) < dmin + win(v), where dmin is the
+// smallest queued distance and win(v) the shortest arc into v: every
+// predecessor p on a shortest path then has d(p) <= d(v) - win(v) < dmin and
+// is already settled (the IN criterion of Crauser et al.).  All qualifying
+// vertices are settled together:
+//   * the queue is an unordered frontier array scanned by the whole warp;
+//   * prune tests run in 8-lane groups, 4 vertices at a time, each lane
+//     reading 4 consecutive label entries (256 contiguous bytes per group);
+//   * the arcs of the batch are flattened over the lanes and relaxed with
+//     atomicMin on the packed (distance, via) key.
+// With unit lengths a batch is exactly one BFS level.  Relaxations from a
+// batch cannot improve a batch vertex, so batch order never matters.
+constexpr int kBatch = 128;
+
+__host__ __device__ constexpr size_t batch_smem_per_warp(uint32_t rcap) {
+    return ((size_t)8 * kBatch + (size_t)8 * kStage + (size_t)4 * (2 * rcap + 4 * kBatch + 1 + kStage) + 15) &
+           ~(size_t)15;
+}
+
+__device__ __forceinline__ uint32_t bsearch_hub(const uint32_t *rh, int rstride, uint32_t R, uint32_t h) {
+    uint32_t lo = 0, hi = R;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (rh[(size_t)mid * rstride] < h) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <bool UNIT, bool PLANT>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+batch_kernel(TreeArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
+    const uint32_t slot = blockIdx.x * kWarpsPerBlock + wib;
+    unsigned char *base = smem + wib * batch_smem_per_warp(a.rcap);
+    uint64_t *s_ba = (uint64_t *)base;                 // arc begin of batch vertex
+    uint64_t *s_sk = s_ba + kBatch;                    // (unused staging, kept for layout)
+    uint32_t *s_rh = (uint32_t *)(s_sk + kStage);
+    uint32_t *s_rd = s_rh + a.rcap;
+    uint32_t *s_bv = s_rd + a.rcap;                    // batch vertex
+    uint32_t *s_bk = s_bv + kBatch;                    // batch key
+    uint32_t *s_bp = s_bk + kBatch;                    // 1: pruned or skipped
+    uint32_t *s_bx = s_bp + kBatch;                    // arc prefix (kBatch + 1)
+
+    uint32_t *key = a.ws_key + (size_t)slot * a.n;
+    uint32_t *vis = a.ws_vis + (size_t)slot * a.n;
+    uint32_t *front = a.ws_front + (size_t)slot * a.n;
+    unsigned long long c_vis = 0, c_reads = 0, c_arcs = 0;
+    const uint32_t g = lane >> 3, sub = lane & 7;
+    const uint32_t gmask = 0xFFu << (8 * g);
+
+    while (true) {
+        uint32_t r = kInf;
+        if (lane == 0) {
+            unsigned long long used = *(volatile unsigned long long *)&a.ctl->nlab;
+            if (used < a.budget) {
+                unsigned long long t = atomicAdd(&a.ctl->next_root, 1ull);
+                if (t < a.r_end) r = (uint32_t)t;
+            }
+        }
+        r = __shfl_sync(kFull, r, 0);
+        if (r == kInf) break;
+        uint32_t t_size = 0, t_lab = 0;
+        const uint32_t v = a.order[r];
+        for (int sd = 0; sd < a.sides; ++sd) {
+            const int f = (a.sides == 1) ? 1 : sd;
+            const uint64_t *goff = a.g_off[f];
+            const uint2 *garc = a.g_arc[f];
+            const uint32_t *ghead = a.g_head[f];
+            const uint32_t *win = a.win[f];
+            const uint32_t ridx = lidx(v, f, a.sides);
+            const uint64_t rb = a.l_off[ridx], re = a.l_off[ridx + 1];
+            const uint32_t R = (uint32_t)(re - rb);
+            const uint32_t *rh, *rd;
+            int rstride;
+            if (R <= a.rcap) {
+                for (uint32_t k = lane; k < R; k += 32) {
+                    const uint2 e = a.l_ent[rb + k];
+                    s_rh[k] = e.x;
+                    s_rd[k] = e.y;
+                }
+                rh = s_rh;
+                rd = s_rd;
+                rstride = 1;
+            } else {
+                rh = (const uint32_t *)(a.l_ent + rb);
+                rd = rh + 1;
+                rstride = 2;
+            }
+            if (lane == 0) {
+                __stcg(&key[v], 1u);
+                vis[0] = v;
+                front[0] = v;
+            }
+            __syncwarp();
+            uint32_t nvis = 1, nf = 1;
+            int ql = 1;
+            while (nf > 0) {
+                // ---- dmin over the frontier
+                uint32_t dmin = kInf;
+                for (uint32_t i = lane; i < nf; i += 32) dmin = min(dmin, __ldcg(&key[front[i]]) >> 1);
+                dmin = __reduce_min_sync(kFull, dmin);
+                // ---- move the final vertices into the batch, compact the rest
+                uint32_t nb = 0, keep = 0;
+                for (uint32_t b0 = 0; b0 < nf; b0 += 32) {
+                    const uint32_t i = b0 + lane;
+                    const bool valid = i < nf;
+                    const uint32_t x = valid ? front[i] : 0u;
+                    const uint32_t kx = valid ? __ldcg(&key[x]) : kInf;
+                    bool take = valid && (uint64_t)(kx >> 1) < (uint64_t)dmin + win[x];
+                    const uint32_t tm = __ballot_sync(kFull, take);
+                    const uint32_t at = nb + __popc(tm & lanemask_lt());
+                    take = take && at < (uint32_t)kBatch;
+                    if (take) {
+                        s_bv[at] = x;
+                        s_bk[at] = kx;
+                    }
+                    nb = min(nb + __popc(tm), (uint32_t)kBatch);
+                    const bool kp = valid && !take;
+                    const uint32_t km = __ballot_sync(kFull, kp);
+                    if (kp) front[keep + __popc(km & lanemask_lt())] = x;
+                    keep += __popc(km);
+                }
+                nf = keep;
+                __syncwarp();
+                t_size += nb;
+                // ---- settle: via bookkeeping (PLaNT) or rank skip (GLL)
+                int nv_batch = 0;
+                for (uint32_t j = lane; j < nb; j += 32) {
+                    const uint32_t kx = s_bk[j];
+                    uint32_t skip = 0;
+                    if (PLANT) {
+                        nv_batch += (int)(kx & 1u);
+                    } else {
+                        skip = a.rank[s_bv[j]] < r ? 1u : 0u;   // iteration_gll :92
+                    }
+                    s_bp[j] = skip;
+                }
+                if (PLANT) ql -= __reduce_add_sync(kFull, nv_batch);
+                __syncwarp();
+                // ---- prune tests: 4 vertices per step, 8 lanes x 4 entries each
+                if (R > 0) {
+                    for (uint32_t j0 = 0; j0 < nb; j0 += 4) {
+                        const uint32_t j = j0 + g;
+                        const bool has = j < nb && s_bp[j] == 0;
+                        uint64_t lb = 0, le = 0;
+                        uint32_t dj = 0;
+                        if (has) {
+                            const uint32_t xu = lidx(s_bv[j], 1 - f, a.sides);
+                            lb = a.l_off[xu];
+                            le = a.l_off[xu + 1];
+                            dj = s_bk[j] >> 1;
+                        }
+                        const uint64_t st = lb & ~1ull;   // 16-byte aligned start
+                        bool found = false;
+                        uint32_t nread = 0;
+                        for (uint64_t c = st; ; c += 32) {
+                            const bool act = has && !found && c < le;
+                            if (!__any_sync(kFull, act)) break;
+                            bool hit = false;
+                            if (act) {
+                                const uint64_t e0 = c + 4 * sub;
+                                uint4 q0 = make_uint4(0, 0, 0, 0), q1 = make_uint4(0, 0, 0, 0);
+                                if (e0 < le) q0 = *(const uint4 *)(a.l_ent + e0);
+                                if (e0 + 2 < le) q1 = *(const uint4 *)(a.l_ent + e0 + 2);
+                                const uint32_t hh[4] = {q0.x, q0.z, q1.x, q1.z};
+                                const uint32_t dd[4] = {q0.y, q0.w, q1.y, q1.w};
+#pragma unroll
+                                for (int t = 0; t < 4; ++t) {
+                                    const uint64_t e = e0 + t;
+                                    if (e >= lb && e < le) {
+                                        const uint32_t p = bsearch_hub(rh, rstride, R, hh[t]);
+                                        if (p < R && rh[(size_t)p * rstride] == hh[t] &&
+                                            rd[(size_t)p * rstride] + dd[t] <= dj)
+                                            hit = true;
+                                    }
+                                }
+                                nread += 4;
+                            }
+                            const uint32_t hm = __ballot_sync(kFull, hit) & gmask;
+                            if (act && hm) found = true;
+                        }
+                        c_reads += nread;
+                        if (has && sub == 0 && found) s_bp[j] = 1;
+                    }
+                    __syncwarp();
+                }
+                // ---- labels of the unpruned (and, for PLaNT, not via) vertices
+                for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
+                    const uint32_t j = j0 + lane;
+                    bool emit = false;
+                    uint32_t xu = 0, dj = 0;
+                    if (j < nb && s_bp[j] == 0) {
+                        const uint32_t kx = s_bk[j];
+                        emit = !PLANT || (kx & 1u);
+                        xu = lidx(s_bv[j], 1 - f, a.sides);
+                        dj = kx >> 1;
+                    }
+                    const uint32_t em = __ballot_sync(kFull, emit);
+                    if (em) {
+                        unsigned long long b = 0;
+                        if (lane == 0) b = atomicAdd(&a.ctl->nlab, (unsigned long long)__popc(em));
+                        b = __shfl_sync(kFull, b, 0);
+                        if (emit) {
+                            const unsigned long long p = b + __popc(em & lanemask_lt());
+                            if (p < a.out_cap) {
+                                a.out_key[p] = ((uint64_t)xu << a.hub_bits) | (uint64_t)(r - a.r0);
+                                a.out_val[p] = dj;
+                            } else {
+                                a.ctl->overflow = 1;
+                            }
+                        }
+                        t_lab += __popc(em);
+                    }
+                }
+                // ---- arcs of the unpruned batch vertices (prefix over degrees)
+                uint32_t total = 0;
+                for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
+                    const uint32_t j = j0 + lane;
+                    uint32_t deg = 0;
+                    if (j < nb && s_bp[j] == 0) {
+                        const uint32_t x = s_bv[j];
+                        const uint64_t ab = goff[x];
+                        deg = (uint32_t)(goff[x + 1] - ab);
+                        s_ba[j] = ab;
+                    }
+                    uint32_t incl = deg;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t y = __shfl_up_sync(kFull, incl, o);
+                        if (lane >= (uint32_t)o) incl += y;
+                    }
+                    if (j < nb) s_bx[j] = total + incl - deg;
+                    total += __shfl_sync(kFull, incl, 31);
+                }
+                if (lane == 0) s_bx[nb] = total;
+                __syncwarp();
+                c_arcs += total;
+                for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+                    const uint32_t t = t0 + lane;
+                    bool upd = false;
+                    uint32_t w = 0, nk = 0, old = kInf;
+                    if (t < total) {
+                        // batch vertex owning arc t: last j with s_bx[j] <= t
+                        uint32_t lo = 0, hi = nb;
+                        while (hi - lo > 1) {
+                            const uint32_t mid = (lo + hi) >> 1;
+                            if (s_bx[mid] <= t) lo = mid;
+                            else hi = mid;
+                        }
+                        const uint64_t e = s_ba[lo] + (t - s_bx[lo]);
+                        uint32_t len;
+                        if (UNIT) {
+                            w = ghead[e];
+                            len = 1;
+                        } else {
+                            const uint2 hl = garc[e];
+                            w = hl.x;
+                            len = hl.y;
+                        }
+                        const uint32_t kx = s_bk[lo];
+                        const uint64_t dd64 = (uint64_t)(kx >> 1) + len;
+                        if (dd64 < 0x7FFFFFFFull) {
+                            uint32_t nv = 1u;
+                            if (PLANT) nv = ((kx & 1u) && a.rank[w] >= r) ? 1u : 0u;
+                            nk = (uint32_t)dd64 * 2u + nv;
+                            old = atomicMin(&key[w], nk);
+                            upd = nk < old;
+                        } else {
+                            a.ctl->err = 1;   // the reference asserts dd < infty
+                        }
+                    }
+                    const bool fresh = upd && old == kInf;
+                    const uint32_t fm = __ballot_sync(kFull, fresh);
+                    if (fresh) {
+                        const uint32_t o = __popc(fm & lanemask_lt());
+                        if (nf + o < a.n && nvis + o < a.n) {
+                            front[nf + o] = w;
+                            vis[nvis + o] = w;
+                        } else {
+                            a.ctl->err = 2;
+                        }
+                    }
+                    nf = min(nf + __popc(fm), a.n);
+                    nvis = min(nvis + __popc(fm), a.n);
+                    if (PLANT) {
+                        int dq = 0;
+                        if (upd) dq = (int)(nk & 1u) - (old == kInf ? 0 : (int)(old & 1u));
+                        ql += __reduce_add_sync(kFull, dq);
+                    }
+                }
+                __syncwarp();
+                if (PLANT && ql == 0) break;   // plant :95 early exit
+            }
+            c_vis += t_size;
+            for (uint32_t k = lane; k < nvis; k += 32) __stcg(&key[vis[k]], kInf);
+            __syncwarp();
+        }
+        if (lane == 0) {
+            a.tree_size[r - a.r0] = t_size;
+            a.tree_labels[r - a.r0] = t_lab;
+        }
+    }
+    if (lane == 0) {
+        atomicAdd(&a.ctl->visits, c_vis);
+        atomicAdd(&a.ctl->arcs, c_arcs);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c_reads += __shfl_xor_sync(kFull, c_reads, o);
+    if (lane == 0) atomicAdd(&a.ctl->label_reads, c_reads);
+}
+
 // ---------------------------------------------------------- commit chain
 
 // Count new labels per label list (sorted keys).
@@ -589,18 +907,22 @@ struct DevGraph {
     uint64_t *off[2] = {nullptr, nullptr};
     uint2 *arc[2] = {nullptr, nullptr};
     uint32_t *head[2] = {nullptr, nullptr};
+    uint32_t *win[2] = {nullptr, nullptr};   // shortest arc into v, per direction
     void release() {
         // side 1 may alias side 0 (symmetric graphs): free each buffer once
         if (off[1] != off[0]) cudaFree(off[1]);
         if (arc[1] != arc[0]) cudaFree(arc[1]);
         if (head[1] != head[0]) cudaFree(head[1]);
+        if (win[1] != win[0]) cudaFree(win[1]);
         cudaFree(off[0]);
         cudaFree(arc[0]);
         cudaFree(head[0]);
+        cudaFree(win[0]);
         for (int s = 0; s < 2; ++s) {
             off[s] = nullptr;
             arc[s] = nullptr;
             head[s] = nullptr;
+            win[s] = nullptr;
         }
     }
 };
@@ -628,10 +950,23 @@ int upload_graph(const chl_graph *g, DevGraph &dg, cudaStream_t st) {
             CHL_CUDA(cudaMemcpy(dg.arc[s], pk.data(), m * 8, cudaMemcpyHostToDevice));
         }
     }
+    for (int s = 0; s < nsides; ++s) {
+        const int src = g->symmetric ? 1 : s;
+        std::vector<uint32_t> w(g->n, 0x7FFFFFFFu);
+        const uint64_t m = g->off[src][g->n];
+        for (uint64_t i = 0; i < m; ++i) {
+            const uint32_t h = g->head[src][i];
+            w[h] = std::min<uint32_t>(w[h], (uint32_t)g->len[src][i]);
+        }
+        int rc = dalloc(&dg.win[s], (size_t)g->n);
+        if (rc) return rc;
+        CHL_CUDA(cudaMemcpy(dg.win[s], w.data(), (size_t)g->n * 4, cudaMemcpyHostToDevice));
+    }
     if (nsides == 1) {
         dg.off[1] = dg.off[0];
         dg.arc[1] = dg.arc[0];
         dg.head[1] = dg.head[0];
+        dg.win[1] = dg.win[0];
     }
     return CHL_OK;
 }
@@ -671,7 +1006,7 @@ struct Build {
     uint32_t *keep = nullptr;
     uint64_t *kpre = nullptr;
     uint32_t *tsize = nullptr, *tlab = nullptr;
-    uint32_t *ws_key = nullptr, *ws_vis = nullptr, *ws_pos = nullptr;
+    uint32_t *ws_key = nullptr, *ws_vis = nullptr, *ws_pos = nullptr, *ws_front = nullptr;
     uint64_t *ws_heap = nullptr;
     BuildCtl *ctl = nullptr;
     void *tmp = nullptr;
@@ -701,6 +1036,7 @@ struct Build {
         cudaFree(ws_key);
         cudaFree(ws_vis);
         cudaFree(ws_pos);
+        cudaFree(ws_front);
         cudaFree(ws_heap);
         cudaFree(ctl);
         cudaFree(tmp);
@@ -741,7 +1077,8 @@ int ensure_ent(uint2 **p, uint64_t *cap, uint64_t need) {
     uint64_t c = std::max<uint64_t>(need, *cap + *cap / 2);
     cudaFree(*p);
     *p = nullptr;
-    int rc = dalloc(p, c);
+    // 4 spare entries: the prune test reads 16-byte pairs of entries
+    int rc = dalloc(p, c + 4);
     if (rc) return rc;
     *cap = c;
     return CHL_OK;
@@ -824,7 +1161,8 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     const bool plant_mode = opts.mode != CHL_MODE_GLL;
     size_t free_b = 0, total_b = 0;
     CHL_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    const size_t per_slot = (size_t)n * (unit ? 8 : 20);
+    const bool use_batch = opts.tree_algo == 0;
+    const size_t per_slot = (size_t)n * (use_batch ? 12 : (unit ? 8 : 20));
     uint32_t want = (uint32_t)sms * 48;   // 12 blocks of 4 warps per SM at most
     if (opts.max_warps) want = std::min<uint32_t>(want, opts.max_warps);
     const size_t ws_budget = free_b / 3;
@@ -834,7 +1172,9 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     const size_t slots = b.warps;
     if ((rc = dalloc(&b.ws_key, slots * n)) || (rc = dalloc(&b.ws_vis, slots * n))) return rc;
     CHL_CUDA(cudaMemsetAsync(b.ws_key, 0xFF, slots * n * 4, b.st));
-    if (!unit) {
+    if (use_batch) {
+        if ((rc = dalloc(&b.ws_front, slots * n))) return rc;
+    } else if (!unit) {
         if ((rc = dalloc(&b.ws_pos, slots * n)) || (rc = dalloc(&b.ws_heap, slots * n))) return rc;
     }
 
@@ -885,13 +1225,14 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         // root label staging capacity: longest committed list, bounded by smem
         int max_smem = 0;
         CHL_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0));
-        const size_t fixed = (unit ? 0 : kHeapSmem * 8) + kStage * 12;
+        const size_t fixed = use_batch ? batch_smem_per_warp(0) : (unit ? 0 : kHeapSmem * 8) + kStage * 12;
         size_t rcap = std::min<uint32_t>(std::max<uint32_t>(max_list, 32), 2048);
         const size_t smem_cap = std::min<size_t>((size_t)max_smem, 96 * 1024);
         if (kWarpsPerBlock * (rcap * 8 + fixed) > smem_cap)
             rcap = (smem_cap / kWarpsPerBlock - fixed) / 8;
         b.rcap = (uint32_t)rcap;
-        const size_t smem = kWarpsPerBlock * ((size_t)b.rcap * 8 + fixed);
+        const size_t smem = use_batch ? kWarpsPerBlock * batch_smem_per_warp(b.rcap)
+                                      : kWarpsPerBlock * ((size_t)b.rcap * 8 + fixed);
         while (true) {
             std::memset(&hc, 0, sizeof(hc));
             hc.next_root = r0;
@@ -924,9 +1265,17 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             ta.ctl = b.ctl;
             ta.rcap = b.rcap;
             const int blocks = (int)(b.warps / kWarpsPerBlock);
+            for (int s2 = 0; s2 < 2; ++s2) ta.win[s2] = b.dg->win[s2];
+            ta.ws_front = b.ws_front;
             void (*kern)(TreeArgs);
-            if (unit) kern = plant_now ? tree_kernel<true, true> : tree_kernel<true, false>;
-            else kern = plant_now ? tree_kernel<false, true> : tree_kernel<false, false>;
+            if (use_batch) {
+                if (unit) kern = plant_now ? batch_kernel<true, true> : batch_kernel<true, false>;
+                else kern = plant_now ? batch_kernel<false, true> : batch_kernel<false, false>;
+            } else if (unit) {
+                kern = plant_now ? tree_kernel<true, true> : tree_kernel<true, false>;
+            } else {
+                kern = plant_now ? tree_kernel<false, true> : tree_kernel<false, false>;
+            }
             CHL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             CHL_CUDA(cudaEventRecord(ev_a, b.st));
             kern<<<blocks, kWarpsPerBlock * 32, smem, b.st>>>(ta);

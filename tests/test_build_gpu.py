@@ -15,6 +15,7 @@ from conftest import label_case
 pytestmark = pytest.mark.gpu
 
 MODES = {"hybrid": 0, "gll": 1, "plant": 2}
+ALGOS = {"batch": 0, "heap": 1}
 CASES = ["grid12", "grid20hw", "rmat8", "directed60", "unit_path"]
 
 
@@ -29,11 +30,12 @@ def same_labels(L, ref, n):
 
 @pytest.mark.parametrize("case", CASES)
 @pytest.mark.parametrize("mode", list(MODES))
-def test_golden_label_files(P, case, mode, tmp_path):
+@pytest.mark.parametrize("algo", list(ALGOS))
+def test_golden_label_files(P, case, mode, algo, tmp_path):
     c = label_case(case)
     g = P.Graph.read(c["gr"])
     order = P.Order.read(c["order"])
-    L = P.build(g, order, mode=MODES[mode])
+    L = P.build(g, order, mode=MODES[mode], tree_algo=ALGOS[algo], first_superstep=7, growth=0.3)
     out = str(tmp_path / "gpu.labels")
     L.write(out)
     assert filecmp.cmp(out, c["labels"], shallow=False)
@@ -41,31 +43,34 @@ def test_golden_label_files(P, case, mode, tmp_path):
 
 @pytest.mark.parametrize("mode", list(MODES))
 @pytest.mark.parametrize("sf", [32.0, 0.05])
-def test_config1_grid_matches_oracle(P, O, mode, sf):
+@pytest.mark.parametrize("algo", list(ALGOS))
+def test_config1_grid_matches_oracle(P, O, mode, sf, algo):
     g = P.Graph.grid(100, 100, seed=1)
     order = P.Order.degree(g, seed=1)
     off, head, ln = g.csr(True)
     og = O.OGraph.from_csr(g.get_n(), off, head, ln)
     ref, _ = O.gll(og, order)
-    L = P.build(g, order, mode=MODES[mode], sf=sf)
+    L = P.build(g, order, mode=MODES[mode], sf=sf, tree_algo=ALGOS[algo])
     assert same_labels(L, ref, g.get_n())
     st = L.stats()
     assert st["supersteps"] >= 1 and st["labels"] == ref.total()
 
 
 @pytest.mark.parametrize("mode", list(MODES))
-def test_rmat_unit_lengths_matches_oracle(P, O, mode):
+@pytest.mark.parametrize("algo", list(ALGOS))
+def test_rmat_unit_lengths_matches_oracle(P, O, mode, algo):
     g = P.Graph.rmat(12, 16, seed=5)
     order = P.Order.degree(g, seed=2)
     off, head, ln = g.csr(True)
     og = O.OGraph.from_csr(g.get_n(), off, head, ln)
     ref, _ = O.gll(og, order)
-    L = P.build(g, order, mode=MODES[mode], sf=1.0)
+    L = P.build(g, order, mode=MODES[mode], sf=1.0, tree_algo=ALGOS[algo])
     assert same_labels(L, ref, g.get_n())
 
 
 @pytest.mark.parametrize("mode", list(MODES))
-def test_directed_weighted_matches_oracle(P, O, mode, tmp_path):
+@pytest.mark.parametrize("algo", list(ALGOS))
+def test_directed_weighted_matches_oracle(P, O, mode, algo, tmp_path):
     rng = np.random.default_rng(7)
     n, m = 700, 4000
     src = rng.integers(0, n, m).astype(np.uint32)
@@ -79,7 +84,7 @@ def test_directed_weighted_matches_oracle(P, O, mode, tmp_path):
     og = O.OGraph.read_dimacs(p)
     order = og.degree_order(3)
     ref, _ = O.gll(og, order)
-    L = P.build(g, order, mode=MODES[mode], sf=0.5)
+    L = P.build(g, order, mode=MODES[mode], sf=0.5, tree_algo=ALGOS[algo])
     assert same_labels(L, ref, n)
 
 
@@ -118,9 +123,11 @@ def test_build_is_deterministic(P):
     g = P.Graph.grid(60, 60, highways=40, hw_steps=16, seed=9)
     order = P.Order.degree(g, seed=4)
     a = P.build(g, order, sf=0.2).export()
-    b = P.build(g, order, sf=0.2, max_warps=64).export()
-    for x, y in zip(a, b):
-        assert np.array_equal(x, y)
+    for kw in ({"max_warps": 64}, {"first_superstep": 1, "growth": 0.05},
+               {"first_superstep": 5000, "growth": 4.0}, {"tree_algo": 1, "max_warps": 8}):
+        b = P.build(g, order, sf=0.2, **kw).export()
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y), kw
 
 
 def test_sampled_queries_equal_dijkstra(P, O):
