@@ -233,6 +233,23 @@ void chl_labels_free(chl_labels *l);
  * pointers (copied in and out on `stream`, a cudaStream_t or NULL). */
 int chl_query_batch(const chl_labels *l, const uint32_t *pairs, size_t k,
                     int32_t *out, void *stream);
+/* Allocation-free variant of chl_query_batch (no counterpart in the
+ * reference).  For callers that cannot let a library allocate device memory:
+ * processes whose HBM is already divided up by their own pool allocator, and
+ * latency-critical request loops that cannot afford cudaMalloc/cudaFree and
+ * their implicit synchronisation.  Same inputs, outputs and answers as
+ * chl_query_batch, but the pairs and answers are staged through one
+ * file-scope device array of CHL_NOALLOC_MAX_PAIRS pairs (12 MiB, held by
+ * every GPU that loads the library until exit); larger k is rejected with
+ * CHL_ERR_INVALID.  The labels must already be resident on the device (any
+ * build, chl_query_batch or chl_server_create makes them so), else
+ * CHL_ERR_INVALID.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  All calls share the array: calls whose work overlaps on the GPU
+ * race.  Synchronises `stream` before returning. */
+#define CHL_NOALLOC_MAX_PAIRS (1u << 20)
+int chl_query_batch_noalloc(const chl_labels *l, const uint32_t *pairs, size_t k,
+                            int32_t *out, void *stream);
 /* Same, with DEVICE pointers; returns after the launch (asynchronous). */
 int chl_query_batch_device(const chl_labels *l, const uint32_t *d_pairs,
                            size_t k, int32_t *d_out, void *stream);

@@ -118,6 +118,7 @@ SIGNATURES = {
     "chl_labels_hub_freq": (C.c_int, [_P, _U32P, _U32P]),
     "chl_labels_free": (None, [_P]),
     "chl_query_batch": (C.c_int, [_P, _U32P, C.c_size_t, _I32P, _P]),
+    "chl_query_batch_noalloc": (C.c_int, [_P, _U32P, C.c_size_t, _I32P, _P]),
     "chl_query_batch_device": (C.c_int, [_P, _P, C.c_size_t, _P, _P]),
     "chl_query_bench": (C.c_int, [_P, C.c_size_t, C.c_uint64, C.c_int, C.POINTER(C.c_double), _U64P]),
     "chl_query_generate": (C.c_int, [_U32P, C.c_size_t, C.c_uint32, C.c_uint64]),

@@ -374,6 +374,79 @@ extern "C" int chl_query_bench(const chl_labels *l, size_t k, uint64_t seed, int
     return CHL_OK;
 }
 
+// ------------------------------------------------- allocation-free queries
+//
+// chl_query_batch stages the pairs and the answers in device memory it
+// allocates per call.  Some callers cannot let a library allocate device
+// memory: serving processes whose HBM is already carved up by their own
+// pool allocator (a cudaMalloc here would fail or fragment it), and
+// latency-critical request loops where cudaMalloc/cudaFree and their
+// implicit synchronisation are not acceptable.  chl_query_batch_noalloc
+// answers the same queries with the same kernel, staging through one
+// file-scope device array instead.
+//
+// The array holds CHL_NOALLOC_MAX_PAIRS pairs (8 B) plus as many answers
+// (4 B): 12 MiB, resident on every GPU that loads this library until the
+// process exits.  All calls share it and it keeps the last call's contents;
+// nothing in it needs to start at zero (each call overwrites the pairs and
+// answers it uses).  Calls whose work overlaps on the GPU race on it.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[(size_t)CHL_NOALLOC_MAX_PAIRS * 12];
+
+namespace {
+std::mutex g_noalloc_mu;
+std::vector<void *> g_noalloc_ptr;   // device address of the array, per device
+}  // namespace
+
+// Host code may not use g_noalloc_scratch as an address (it is a host-side
+// stand-in); the device address comes from cudaGetSymbolAddress, once per
+// device, with that device current.
+static int noalloc_scratch(void **ptr) {
+    int dev = 0;
+    CHL_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> g(g_noalloc_mu);
+    if ((int)g_noalloc_ptr.size() <= dev) g_noalloc_ptr.resize(dev + 1, nullptr);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        CHL_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_ptr[dev] = p;
+    }
+    *ptr = g_noalloc_ptr[dev];
+    return CHL_OK;
+}
+
+extern "C" int chl_query_batch_noalloc(const chl_labels *l, const uint32_t *pairs, size_t k,
+                                       int32_t *out, void *stream) {
+    if (!l || (k && (!pairs || !out))) return CHL_ERR_INVALID;
+    if (k > CHL_NOALLOC_MAX_PAIRS) {
+        set_error("chl_query_batch_noalloc: more than CHL_NOALLOC_MAX_PAIRS pairs in one call");
+        return CHL_ERR_INVALID;
+    }
+    if (!l->d_off) {
+        // uploading the labels would allocate; the caller must make them
+        // resident first (any build, chl_query_batch or chl_server_create)
+        set_error("chl_query_batch_noalloc: labels are not resident on the device");
+        return CHL_ERR_INVALID;
+    }
+    for (size_t i = 0; i < 2 * k; ++i)
+        if (pairs[i] >= l->n) {
+            set_error("query vertex out of range");
+            return CHL_ERR_INVALID;
+        }
+    if (k == 0) return CHL_OK;
+    void *base = nullptr;
+    int rc = noalloc_scratch(&base);
+    if (rc) return rc;
+    uint32_t *d_pairs = (uint32_t *)base;
+    int32_t *d_out = (int32_t *)((unsigned char *)base + (size_t)CHL_NOALLOC_MAX_PAIRS * 8);
+    cudaStream_t s = (cudaStream_t)stream;
+    CHL_CUDA(cudaMemcpyAsync(d_pairs, pairs, k * 8, cudaMemcpyHostToDevice, s));
+    rc = query_launch(l, d_pairs, k, d_out, s);
+    if (rc) return rc;
+    CHL_CUDA(cudaMemcpyAsync(out, d_out, k * 4, cudaMemcpyDeviceToHost, s));
+    CHL_CUDA(cudaStreamSynchronize(s));
+    return CHL_OK;
+}
+
 extern "C" int chl_query_batch(const chl_labels *l, const uint32_t *pairs, size_t k, int32_t *out,
                                void *stream) {
     if (!l || (k && (!pairs || !out))) return CHL_ERR_INVALID;
