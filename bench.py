@@ -41,6 +41,7 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 METRIC = "CHL label build throughput (canonical labels, 1024x1024 road-like grid, betweenness order)"
+METRIC_RMAT = "CHL label build throughput (canonical labels, RMAT scale 20, degree order)"
 UNIT = "labels/s"
 
 
@@ -55,6 +56,17 @@ def parse():
     ap.add_argument("--sources", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-full", action="store_true",
+                    help="also time the CPU GLL restatement on the WHOLE build (minutes) and "
+                         "check its labels against the GPU's")
+    ap.add_argument("--workload", default="grid", choices=["grid", "rmat"],
+                    help="grid: 1024x1024 road-like grid (default); rmat: RMAT scale 20, degree order")
+    ap.add_argument("--scale", type=int, default=20)
+    ap.add_argument("--verbose", type=int, default=0, help="2: per-superstep lines on stderr")
+    ap.add_argument("--serve", action="store_true",
+                    help="also run the open-loop serving test (Poisson arrivals) on the built labels")
+    ap.add_argument("--serve-qps", type=float, default=2e8, help="offered pair rate (pairs/s)")
+    ap.add_argument("--serve-seconds", type=float, default=5.0)
     return ap.parse_args()
 
 
@@ -137,10 +149,33 @@ def profile_traffic():
 
 
 def make_workload(P, args):
+    if args.workload == "rmat":
+        g = P.Graph.rmat(args.scale, 16, 0.57, 0.19, 0.19, seed=1)
+        order = P.Order.degree(g, seed=1)
+        return g, order
     g = P.Graph.grid(args.side, args.side, del_frac=0.05, diag_frac=0.01, wmin=1, wmax=1000,
                      highways=args.highways, hw_steps=64, hw_factor=150.0, seed=1)
     order = P.Order.betweenness(g, args.sources, seed=1)
     return g, order
+
+
+def workload_name(args):
+    if args.workload == "rmat":
+        return f"rmat{args.scale} ef16 (0.57,0.19,0.19,0.05), degree order"
+    return f"grid{args.side}x{args.side}+hw{args.highways}, betweenness({args.sources})"
+
+
+def cpu_full(g, order, L):
+    """Whole CPU GLL build (restatement of run_paraPLL, all host cores);
+    returns (seconds, labels, identical_to_gpu)."""
+    from oracle import oracle as O
+    off, head, ln = g.csr(True)
+    og = O.OGraph.from_csr(g.get_n(), off, head, ln)
+    ref, secs = O.gll(og, order, threads=os.cpu_count() or 1)
+    a = L.export()
+    b = ref.export(g.get_n())
+    same = all(np.array_equal(np.asarray(x), np.asarray(y)) for x, y in zip(a, b))
+    return secs, int(ref.total()), bool(same)
 
 
 def cpu_sample(g, order, seconds, threads=None):
@@ -171,6 +206,70 @@ def build_work_bytes(L, g):
     return tot
 
 
+def serve_test(P, L, n, qps, seconds, seed=11):
+    """Open-loop Poisson request stream against the continuous-batching
+    server: request sizes log-uniform in [1, 65536] pairs, 10% of the pairs
+    drawn from a fixed hot set of 1,000 pairs.  Arrivals follow the offered
+    pair rate; latency is submit-to-completion measured by the server."""
+    rng = np.random.default_rng(seed)
+    hot = rng.integers(0, n, (1000, 2)).astype(np.uint32)
+    srv = P.Server(L, max_inflight_pairs=1 << 24, max_requests=1 << 16, max_batch_pairs=1 << 21)
+    sizes, reqs = [], []
+    total = 0
+    while total < qps * seconds:
+        k = int(np.exp(rng.uniform(0, np.log(65536.0))))
+        k = max(1, min(65536, k))
+        q = rng.integers(0, n, (k, 2)).astype(np.uint32)
+        nh = rng.binomial(k, 0.1)
+        if nh:
+            q[:nh] = hot[rng.integers(0, 1000, nh)]
+        reqs.append(q)
+        sizes.append(k)
+        total += k
+        if len(reqs) >= 200000:
+            break
+    mean_k = float(np.mean(sizes))
+    rate = qps / mean_k                       # requests per second
+    gaps = rng.exponential(1.0 / rate, len(reqs))
+    lat = [None] * len(reqs)
+    ids = [None] * len(reqs)
+    import queue as _q
+    pend = _q.Queue()
+
+    def waiter():
+        while True:
+            item = pend.get()
+            if item is None:
+                return
+            i, rid = item
+            out, l = srv.wait(rid, len(reqs[i]))
+            lat[i] = l
+
+    th = threading.Thread(target=waiter, daemon=True)
+    th.start()
+    t0 = time.perf_counter()
+    nxt = t0
+    for i, q in enumerate(reqs):
+        nxt += gaps[i]
+        while True:
+            now = time.perf_counter()
+            if now >= nxt:
+                break
+            time.sleep(min(0.0005, nxt - now))
+        ids[i] = srv.submit(q)
+        pend.put((i, ids[i]))
+    pend.put(None)
+    th.join()
+    t1 = time.perf_counter()
+    st = srv.stats()
+    srv.close()
+    la = np.array(lat, np.float64)
+    return {"offered_pairs_per_s": qps, "requests": len(reqs), "pairs": int(total),
+            "achieved_pairs_per_s": total / (t1 - t0), "p50_ms": float(np.percentile(la, 50)),
+            "p99_ms": float(np.percentile(la, 99)), "mean_request_pairs": mean_k,
+            "launches": st["launches"], "hot_fraction": 0.1}
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -191,8 +290,7 @@ def run_reference(args, ws, rank):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean([labels / x for x in vals])),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic",
-            "config": {"workload": f"grid{args.side}x{args.side}+hw{args.highways}, betweenness({args.sources})",
-                       "sample_roots": r},
+            "config": {"workload": workload_name(args), "sample_roots": r},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"first {r} of {len(order)} roots (both sides), GLL restatement"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -224,7 +322,7 @@ def run_ours(args, ws, rank):
     t0 = time.time()
     with Clocks() as ck:
         for _ in range(args.steps):
-            L = P.build(g, order)
+            L = P.build(g, order, verbose=args.verbose)
             stats.append(L.stats())
     wall = time.time() - t0
     barrier()
@@ -270,7 +368,7 @@ def run_ours(args, ws, rank):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
-        "config": {"workload": f"grid{args.side}x{args.side}+hw{args.highways}, betweenness({args.sources}), full build",
+        "config": {"workload": workload_name(args) + ", full build",
                    "vertices": n, "arcs": int(g.out_arcs()), "l2": "inputs larger than L2 (label CSR of several GB)",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "clocks": ck.summary(),
@@ -295,6 +393,14 @@ def run_ours(args, ws, rank):
         line["cpu_baseline"] = {"value": lab / secs, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": f"GLL restatement on the first {r} of {n} roots (both sides)",
                                 "seconds": secs}
+    if rank == 0 and args.serve:
+        line["serving"] = serve_test(P, L, n, args.serve_qps, args.serve_seconds)
+    if rank == 0 and args.cpu_full:
+        L3 = P.build(g, order)
+        secs, lab, same = cpu_full(g, order, L3)
+        line["cpu_full_build"] = {"seconds": secs, "labels": lab, "labels_per_s": lab / secs,
+                                  "cores": os.cpu_count(), "identical_to_gpu": same,
+                                  "what": "CPU GLL restatement (run_paraPLL, sf 32), whole build"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -303,6 +409,9 @@ def run_ours(args, ws, rank):
 
 def main():
     args = parse()
+    global METRIC
+    if args.workload == "rmat":
+        METRIC = METRIC_RMAT
     ws, rank = dist_info()
     if args.impl == "reference":
         run_reference(args, ws, rank)

@@ -39,6 +39,10 @@ constexpr uint32_t kInf = 0xFFFFFFFFu;
 constexpr int kHeapSmem = 256;      // heap slots kept in shared memory per warp
 constexpr int kWarpsPerBlock = 4;
 constexpr int kStage = 32;          // label staging entries per warp
+#ifndef CHL_PHASE_TIMING
+#define CHL_PHASE_TIMING 0              // 1: per-phase clock64 counters (diagnostic builds)
+#endif
+constexpr bool kPhaseTiming = CHL_PHASE_TIMING != 0;
 
 struct BuildCtl {
     unsigned long long next_root;   // root fetch counter (absolute rank)
@@ -51,6 +55,8 @@ struct BuildCtl {
     unsigned int err;               // 1: distance overflow, 2: workspace bound
     unsigned long long max_ratio_num;  // (tree, labels) of the worst root
     unsigned long long max_ratio_den;
+    unsigned long long cyc[8];      // per-phase SM cycles summed over warps (diagnostics)
+    unsigned long long cnt[4];      // frontier entries scanned, rounds, settle calls, arcs relaxed
 };
 
 struct TreeArgs {
@@ -79,6 +85,12 @@ struct TreeArgs {
     uint32_t rcap;                  // root label entries staged in smem
     const uint32_t *win[2];         // [f]: shortest arc into v along direction f
     uint32_t *ws_front;             // per warp slot: queued (unsettled) vertices
+    int scan_back;                  // prune tests read label lists from the end
+    uint32_t r_big;                 // roots below r_big: one block per tree
+    uint32_t smem_block;            // dynamic shared memory of a block (bytes)
+    const uint16_t *win16[2];       // win clamped to 65535 (a valid lower bound)
+    uint2 *ws_fq;                   // per warp slot: queue log (vertex, distance)
+    uint32_t fq_cap;                // log entries per slot
 };
 
 __device__ __forceinline__ uint32_t lidx(uint32_t v, int side, int sides) {
@@ -325,7 +337,9 @@ tree_kernel(TreeArgs a) {
                     pkey = key[pw];
                 }
                 bool pruned = false;
-                if (R > 0) {
+                if (PLANT && R > 0 && a.rank[u] < a.r0) {
+                    pruned = true;   // committed vertex: a committed witness always exists
+                } else if (R > 0) {
                     uint32_t nr = 0;
                     pruned = prune_test(rh, rd, rstride, R, a.l_ent + ub, (uint32_t)(ue - ub), d, nr);
                     c_reads += nr;
@@ -450,7 +464,7 @@ tree_kernel(TreeArgs a) {
 constexpr int kBatch = 128;
 
 __host__ __device__ constexpr size_t batch_smem_per_warp(uint32_t rcap) {
-    return ((size_t)8 * kBatch + (size_t)8 * kStage + (size_t)4 * (2 * rcap + 4 * kBatch + 1 + kStage) + 15) &
+    return ((size_t)8 * kBatch + (size_t)8 * kStage + (size_t)4 * (2 * rcap + 5 * kBatch + 1 + kStage) + 15) &
            ~(size_t)15;
 }
 
@@ -462,6 +476,403 @@ __device__ __forceinline__ uint32_t bsearch_hub(const uint32_t *rh, int rstride,
         else hi = mid;
     }
     return lo;
+}
+
+// Lower bound of h in rh[p0..R), knowing rh[p0-1] < h (or p0 == 0):
+// exponential steps, then a binary search inside the last step.
+__device__ __forceinline__ uint32_t gallop_hub(const uint32_t *rh, int rstride, uint32_t R, uint32_t p0,
+                                               uint32_t h) {
+    uint32_t lo = p0, step = 1;
+    while (lo < R && rh[(size_t)lo * rstride] < h) {
+        const uint32_t nxt = lo + step;
+        if (nxt >= R || rh[(size_t)nxt * rstride] >= h) {
+            uint32_t l2 = lo + 1, h2 = nxt < R ? nxt : R;
+            while (l2 < h2) {
+                const uint32_t mid = (l2 + h2) >> 1;
+                if (rh[(size_t)mid * rstride] < h) l2 = mid + 1;
+                else h2 = mid;
+            }
+            return l2;
+        }
+        lo = nxt;
+        step <<= 1;
+    }
+    return lo;
+}
+
+// ------------------------------------------------- CTA-cooperative trees
+//
+// The largest trees of a superstep (its first roots: roots go in rank
+// order) set its length.  For them the whole block (kWarpsPerBlock warps)
+// works on one tree: one shared root label (kWarpsPerBlock times the
+// capacity of a warp's), frontier scans, prune tests and relaxations split
+// over all threads, the settle list in global memory.  Same rounds and the
+// same IN criterion as the per-warp trees.
+constexpr int kBatchC = 512;
+
+struct CtaShared {
+    uint32_t nf;       // current frontier size
+    uint32_t nnext;    // entries written to the next frontier
+    uint32_t ns;       // settle-list size of the round
+    uint32_t nvis;     // touched vertices
+    int ql;            // queued vertices without a higher-ranked ancestor
+    uint32_t dnext;    // minimum queued distance after the round
+    uint32_t stop;
+    uint32_t total;    // arcs of the current batch
+    uint32_t t_size, t_lab;
+    uint32_t root;
+    uint32_t pad[5];
+};
+
+__host__ __device__ constexpr size_t cta_fixed_bytes() {
+    return sizeof(CtaShared) + (size_t)8 * kBatchC + (size_t)4 * (4 * kBatchC + 4);
+}
+
+template <bool UNIT, bool PLANT>
+__device__ void cta_tree(const TreeArgs &a, uint32_t r, unsigned char *smem, size_t smem_bytes, uint32_t *key,
+                         uint32_t *vis, uint32_t *fa, uint32_t *fb, uint32_t *S, unsigned long long &c_vis,
+                         unsigned long long &c_reads, unsigned long long &c_arcs, uint32_t &t_size_out,
+                         uint32_t &t_lab_out) {
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr uint32_t NT = kWarpsPerBlock * 32;
+    CtaShared &sh = *(CtaShared *)smem;
+    uint64_t *s_ba = (uint64_t *)(smem + sizeof(CtaShared));
+    uint32_t *s_bv = (uint32_t *)(s_ba + kBatchC);
+    uint32_t *s_bk = s_bv + kBatchC;
+    uint32_t *s_bp = s_bk + kBatchC;
+    uint32_t *s_bx = s_bp + kBatchC;                      // kBatchC + 1 (+3 pad)
+    uint32_t *s_rh = s_bx + kBatchC + 4;
+    const uint32_t rcapC = (uint32_t)((smem_bytes - cta_fixed_bytes()) / 8);
+    uint32_t *s_rd = s_rh + rcapC;
+    const uint32_t g = lane >> 2, sub = lane & 3;
+    const uint32_t gmask = 0xFu << (4 * g);
+    const uint32_t v = a.order[r];
+    if (tid == 0) {
+        sh.t_size = 0;
+        sh.t_lab = 0;
+    }
+    for (int sd = 0; sd < a.sides; ++sd) {
+        const int f = (a.sides == 1) ? 1 : sd;
+        const uint64_t *goff = a.g_off[f];
+        const uint2 *garc = a.g_arc[f];
+        const uint32_t *ghead = a.g_head[f];
+        const uint32_t *win = a.win[f];
+        const uint32_t ridx = lidx(v, f, a.sides);
+        const uint64_t rb = a.l_off[ridx], re = a.l_off[ridx + 1];
+        const uint32_t R = (uint32_t)(re - rb);
+        const uint32_t *rh, *rd;
+        int rstride;
+        __syncthreads();
+        if (R <= rcapC) {
+            for (uint32_t k = tid; k < R; k += NT) {
+                const uint2 e = a.l_ent[rb + k];
+                s_rh[k] = e.x;
+                s_rd[k] = e.y;
+            }
+            rh = s_rh;
+            rd = s_rd;
+            rstride = 1;
+        } else {
+            rh = (const uint32_t *)(a.l_ent + rb);
+            rd = rh + 1;
+            rstride = 2;
+        }
+        if (tid == 0) {
+            __stcg(&key[v], 1u);
+            vis[0] = v;
+            fa[0] = v;
+            sh.nf = 1;
+            sh.nvis = 1;
+            sh.ql = 1;
+            sh.stop = 0;
+        }
+        __syncthreads();
+        uint32_t dmin = 0;
+        uint32_t *cur = fa, *nxt = fb;
+        while (true) {
+            const uint32_t nf = sh.nf;
+            if (nf == 0 || sh.stop) break;
+            __syncthreads();
+            if (tid == 0) {
+                sh.ns = 0;
+                sh.nnext = 0;
+                sh.dnext = kInf;
+            }
+            __syncthreads();
+            // ---- phase 1: split the frontier into settle list and next frontier
+            uint32_t dn = kInf;
+            for (uint32_t c0 = warp * 32; c0 < nf; c0 += NT) {
+                const uint32_t i = c0 + lane;
+                const bool valid = i < nf;
+                const uint32_t x = valid ? cur[i] : 0u;
+                const uint32_t kx = valid ? __ldcg(&key[x]) : kInf;
+                const bool take = valid && (uint64_t)(kx >> 1) < (uint64_t)dmin + win[x];
+                const bool kp = valid && !take;
+                const uint32_t tm = __ballot_sync(kFull, take), km = __ballot_sync(kFull, kp);
+                uint32_t bs = 0, bk = 0;
+                if (lane == 0) {
+                    if (tm) bs = atomicAdd(&sh.ns, (uint32_t)__popc(tm));
+                    if (km) bk = atomicAdd(&sh.nnext, (uint32_t)__popc(km));
+                }
+                bs = __shfl_sync(kFull, bs, 0);
+                bk = __shfl_sync(kFull, bk, 0);
+                if (take) S[bs + __popc(tm & lanemask_lt())] = x;
+                if (kp) {
+                    nxt[bk + __popc(km & lanemask_lt())] = x;
+                    dn = min(dn, kx >> 1);
+                }
+            }
+            dn = __reduce_min_sync(kFull, dn);
+            if (lane == 0 && dn != kInf) atomicMin(&sh.dnext, dn);
+            __syncthreads();
+            const uint32_t ns = sh.ns;
+            // ---- phase 2: settle the list in batches of kBatchC
+            for (uint32_t b0 = 0; b0 < ns; b0 += kBatchC) {
+                const uint32_t nb = min((uint32_t)kBatchC, ns - b0);
+                int nvb = 0;
+                for (uint32_t j = tid; j < nb; j += NT) {
+                    const uint32_t x = S[b0 + j];
+                    const uint32_t kx = __ldcg(&key[x]);
+                    const uint32_t rx = a.rank[x];
+                    s_bv[j] = x;
+                    s_bk[j] = kx;
+                    if (PLANT) {
+                        nvb += (int)(kx & 1u);
+                        s_bp[j] = rx < a.r0 ? 1u : 0u;
+                    } else {
+                        s_bp[j] = rx < r ? 1u : 0u;
+                    }
+                }
+                if (PLANT) {
+                    nvb = __reduce_add_sync(kFull, nvb);
+                    if (lane == 0 && nvb) atomicSub(&sh.ql, nvb);
+                }
+                if (tid == 0) sh.t_size += nb;
+                __syncthreads();
+                if (R > 0) {
+                    // 32 groups of 4 lanes: 32 vertices per block step
+                    for (uint32_t j0 = warp * 8; j0 < nb; j0 += 8 * kWarpsPerBlock) {
+                        const uint32_t j = j0 + g;
+                        const bool has = j < nb && s_bp[j] == 0;
+                        uint64_t lb = 0, le = 0;
+                        uint32_t dj = 0;
+                        if (has) {
+                            const uint32_t xu = lidx(s_bv[j], 1 - f, a.sides);
+                            lb = a.l_off[xu];
+                            le = a.l_off[xu + 1];
+                            dj = s_bk[j] >> 1;
+                        }
+                        const uint64_t st = lb & ~1ull;
+                        const uint32_t nch = has ? (uint32_t)((le - st + 31) >> 5) : 0u;
+                        bool found = false;
+                        uint32_t nread = 0;
+                        for (uint32_t k = 0;; ++k) {
+                            const bool act = !found && k < nch;
+                            if (!__any_sync(kFull, act)) break;
+                            bool hit = false;
+                            if (act) {
+                                const uint32_t ck = a.scan_back ? nch - 1 - k : k;
+                                const uint64_t e0 = st + 32ull * ck + 8 * sub;
+                                uint4 q[4];
+#pragma unroll
+                                for (int t = 0; t < 4; ++t) {
+                                    q[t] = make_uint4(0, 0, 0, 0);
+                                    if (e0 + 2 * t < le) q[t] = *(const uint4 *)(a.l_ent + e0 + 2 * t);
+                                }
+                                uint32_t p = 0;
+                                bool first = true;
+#pragma unroll
+                                for (int t = 0; t < 8; ++t) {
+                                    const uint64_t e = e0 + t;
+                                    const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
+                                    const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
+                                    if (e >= lb && e < le) {
+                                        if (first) {
+                                            p = bsearch_hub(rh, rstride, R, hh);
+                                            first = false;
+                                        } else {
+                                            p = gallop_hub(rh, rstride, R, p, hh);
+                                        }
+                                        if (p < R && rh[(size_t)p * rstride] == hh &&
+                                            rd[(size_t)p * rstride] + dd <= dj)
+                                            hit = true;
+                                    }
+                                }
+                                nread += 8;
+                            }
+                            const uint32_t hm = __ballot_sync(kFull, hit) & gmask;
+                            if (act && hm) found = true;
+                        }
+                        c_reads += nread;
+                        if (has && sub == 0 && found) s_bp[j] = 1;
+                    }
+                    __syncthreads();
+                }
+                // labels
+                for (uint32_t j0 = warp * 32; j0 < nb; j0 += NT) {
+                    const uint32_t j = j0 + lane;
+                    bool emit = false;
+                    uint32_t xu = 0, dj = 0;
+                    if (j < nb && s_bp[j] == 0) {
+                        const uint32_t kx = s_bk[j];
+                        emit = !PLANT || (kx & 1u);
+                        xu = lidx(s_bv[j], 1 - f, a.sides);
+                        dj = kx >> 1;
+                    }
+                    const uint32_t em = __ballot_sync(kFull, emit);
+                    if (em) {
+                        unsigned long long bb = 0;
+                        if (lane == 0) {
+                            bb = atomicAdd(&a.ctl->nlab, (unsigned long long)__popc(em));
+                            atomicAdd(&sh.t_lab, (uint32_t)__popc(em));
+                        }
+                        bb = __shfl_sync(kFull, bb, 0);
+                        if (emit) {
+                            const unsigned long long p = bb + __popc(em & lanemask_lt());
+                            if (p < a.out_cap) {
+                                a.out_key[p] = ((uint64_t)xu << a.hub_bits) | (uint64_t)(r - a.r0);
+                                a.out_val[p] = dj;
+                            } else {
+                                a.ctl->overflow = 1;
+                            }
+                        }
+                    }
+                }
+                // degree prefix over the batch: each thread owns 4 consecutive entries
+                {
+                    uint32_t dl[4];
+                    uint32_t sum = 0;
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        const uint32_t j = tid * 4 + t;
+                        uint32_t deg = 0;
+                        if (j < nb && s_bp[j] == 0) {
+                            const uint32_t x = s_bv[j];
+                            const uint64_t ab = goff[x];
+                            deg = (uint32_t)(goff[x + 1] - ab);
+                            s_ba[j] = ab;
+                        }
+                        dl[t] = deg;
+                        sum += deg;
+                    }
+                    uint32_t incl = sum;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t y = __shfl_up_sync(kFull, incl, o);
+                        if (lane >= (uint32_t)o) incl += y;
+                    }
+                    // warp totals through the settle-list slots past the batch
+                    __shared__ uint32_t wtot[kWarpsPerBlock];
+                    if (lane == 31) wtot[warp] = incl;
+                    __syncthreads();
+                    uint32_t off = 0;
+                    for (uint32_t w2 = 0; w2 < warp; ++w2) off += wtot[w2];
+                    uint32_t run = off + incl - sum;
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        const uint32_t j = tid * 4 + t;
+                        if (j < nb) s_bx[j] = run;
+                        run += dl[t];
+                    }
+                    if (tid == NT - 1) {
+                        uint32_t tot = 0;
+                        for (uint32_t w2 = 0; w2 < kWarpsPerBlock; ++w2) tot += wtot[w2];
+                        s_bx[nb] = tot;
+                        sh.total = tot;
+                    }
+                    __syncthreads();
+                }
+                const uint32_t total = sh.total;
+                if (tid == 0) c_arcs += total;
+                // relaxations, flattened over all threads
+                uint32_t dn2 = kInf;
+                for (uint32_t t0 = warp * 32; t0 < total; t0 += NT) {
+                    const uint32_t t = t0 + lane;
+                    bool upd = false;
+                    uint32_t w = 0, nk = 0, old = kInf;
+                    if (t < total) {
+                        uint32_t lo = 0, hi = nb;
+                        while (hi - lo > 1) {
+                            const uint32_t mid = (lo + hi) >> 1;
+                            if (s_bx[mid] <= t) lo = mid;
+                            else hi = mid;
+                        }
+                        const uint64_t e = s_ba[lo] + (t - s_bx[lo]);
+                        uint32_t len;
+                        if (UNIT) {
+                            w = ghead[e];
+                            len = 1;
+                        } else {
+                            const uint2 hl = garc[e];
+                            w = hl.x;
+                            len = hl.y;
+                        }
+                        const uint32_t kx = s_bk[lo];
+                        const uint64_t dd64 = (uint64_t)(kx >> 1) + len;
+                        if (dd64 < 0x7FFFFFFFull) {
+                            uint32_t nv = 1u;
+                            if (PLANT) nv = ((kx & 1u) && a.rank[w] >= r) ? 1u : 0u;
+                            nk = (uint32_t)dd64 * 2u + nv;
+                            old = atomicMin(&key[w], nk);
+                            upd = nk < old;
+                            if (upd) dn2 = min(dn2, nk >> 1);
+                        } else {
+                            a.ctl->err = 1;
+                        }
+                    }
+                    const bool fresh = upd && old == kInf;
+                    const uint32_t fm = __ballot_sync(kFull, fresh);
+                    if (fm) {
+                        uint32_t bn = 0, bv = 0;
+                        if (lane == 0) {
+                            bn = atomicAdd(&sh.nnext, (uint32_t)__popc(fm));
+                            bv = atomicAdd(&sh.nvis, (uint32_t)__popc(fm));
+                        }
+                        bn = __shfl_sync(kFull, bn, 0);
+                        bv = __shfl_sync(kFull, bv, 0);
+                        if (fresh) {
+                            const uint32_t o = __popc(fm & lanemask_lt());
+                            if (bn + o < a.n && bv + o < a.n) {
+                                nxt[bn + o] = w;
+                                vis[bv + o] = w;
+                            } else {
+                                a.ctl->err = 2;
+                            }
+                        }
+                    }
+                    if (PLANT) {
+                        int dq = 0;
+                        if (upd) dq = (int)(nk & 1u) - (old == kInf ? 0 : (int)(old & 1u));
+                        dq = __reduce_add_sync(kFull, dq);
+                        if (lane == 0 && dq) atomicAdd(&sh.ql, dq);
+                    }
+                }
+                dn2 = __reduce_min_sync(kFull, dn2);
+                if (lane == 0 && dn2 != kInf) atomicMin(&sh.dnext, dn2);
+                __syncthreads();
+                if (tid == 0 && PLANT && sh.ql == 0) sh.stop = 1;
+                __syncthreads();
+                if (sh.stop) break;
+            }
+            if (sh.stop) break;
+            uint32_t *tmp = cur;
+            cur = nxt;
+            nxt = tmp;
+            dmin = sh.dnext;
+            __syncthreads();
+            if (tid == 0) sh.nf = min(sh.nnext, a.n);
+            __syncthreads();
+        }
+        __syncthreads();
+        const uint32_t nvis = min(sh.nvis, a.n);
+        for (uint32_t k = tid; k < nvis; k += NT) __stcg(&key[vis[k]], kInf);
+        __syncthreads();
+    }
+    if (tid == 0) {
+        c_vis += sh.t_size;
+        t_size_out = sh.t_size;
+        t_lab_out = sh.t_lab;
+    }
 }
 
 template <bool UNIT, bool PLANT>
@@ -479,28 +890,77 @@ batch_kernel(TreeArgs a) {
     uint32_t *s_bk = s_bv + kBatch;                    // batch key
     uint32_t *s_bp = s_bk + kBatch;                    // 1: pruned or skipped
     uint32_t *s_bx = s_bp + kBatch;                    // arc prefix (kBatch + 1)
+    uint32_t *s_tl = s_bx + kBatch + 1;                // batch indices still to test
 
     uint32_t *key = a.ws_key + (size_t)slot * a.n;
     uint32_t *vis = a.ws_vis + (size_t)slot * a.n;
     uint32_t *front = a.ws_front + (size_t)slot * a.n;
     unsigned long long c_vis = 0, c_reads = 0, c_arcs = 0;
-    const uint32_t g = lane >> 3, sub = lane & 7;
-    const uint32_t gmask = 0xFFu << (8 * g);
+    long long cyc[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // phase cycles (diagnostics)
+    unsigned long long dcnt[4] = {0, 0, 0, 0};      // scanned, rounds, settles, arcs
+    const long long k_start = clock64();
+    const uint32_t g = lane >> 2, sub = lane & 3;
+    const uint32_t gmask = 0xFu << (4 * g);
 
-    while (true) {
-        uint32_t r = kInf;
-        if (lane == 0) {
-            unsigned long long used = *(volatile unsigned long long *)&a.ctl->nlab;
-            if (used < a.budget) {
-                unsigned long long t = atomicAdd(&a.ctl->next_root, 1ull);
-                if (t < a.r_end) r = (uint32_t)t;
+    // ---- block-per-tree phase for the superstep's first (largest) roots
+    uint32_t pending = kInf;
+    if (a.r_big > a.r0) {
+        CtaShared &sh = *(CtaShared *)smem;
+        const size_t s0 = (size_t)blockIdx.x * kWarpsPerBlock;
+        uint32_t *key0 = a.ws_key + s0 * a.n;
+        uint32_t *vis0 = a.ws_vis + s0 * a.n;
+        uint32_t *f0 = a.ws_front + s0 * a.n;
+        uint32_t *f1 = a.ws_front + (s0 + 1) * a.n;
+        uint32_t *f2 = a.ws_front + (s0 + 2) * a.n;
+        while (true) {
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                uint32_t rr = kInf;
+                unsigned long long used = *(volatile unsigned long long *)&a.ctl->nlab;
+                if (used < a.budget) {
+                    unsigned long long t = atomicAdd(&a.ctl->next_root, 1ull);
+                    if (t < a.r_end) rr = (uint32_t)t;
+                }
+                sh.root = rr;
+            }
+            __syncthreads();
+            const uint32_t rc = sh.root;
+            if (rc == kInf) break;
+            if (rc >= a.r_big) {
+                if (wib == 0) pending = rc;   // warp 0 builds this one alone
+                break;
+            }
+            uint32_t ts = 0, tl = 0;
+            cta_tree<UNIT, PLANT>(a, rc, smem, a.smem_block, key0, vis0, f0, f1, f2, c_vis, c_reads, c_arcs, ts,
+                                  tl);
+            if (threadIdx.x == 0) {
+                a.tree_size[rc - a.r0] = ts;
+                a.tree_labels[rc - a.r0] = tl;
             }
         }
-        r = __shfl_sync(kFull, r, 0);
+        __syncthreads();   // the block leaves the shared layout before warps reuse it
+    }
+    // ---- warp-per-tree phase
+    while (true) {
+        uint32_t r = kInf;
+        if (pending != kInf) {
+            r = pending;
+            pending = kInf;
+        } else {
+            if (lane == 0) {
+                unsigned long long used = *(volatile unsigned long long *)&a.ctl->nlab;
+                if (used < a.budget) {
+                    unsigned long long t = atomicAdd(&a.ctl->next_root, 1ull);
+                    if (t < a.r_end) r = (uint32_t)t;
+                }
+            }
+            r = __shfl_sync(kFull, r, 0);
+        }
         if (r == kInf) break;
         uint32_t t_size = 0, t_lab = 0;
         const uint32_t v = a.order[r];
         for (int sd = 0; sd < a.sides; ++sd) {
+            const long long tr0 = clock64();
             const int f = (a.sides == 1) ? 1 : sd;
             const uint64_t *goff = a.g_off[f];
             const uint2 *garc = a.g_arc[f];
@@ -531,99 +991,130 @@ batch_kernel(TreeArgs a) {
                 front[0] = v;
             }
             __syncwarp();
+            cyc[5] += clock64() - tr0;
             uint32_t nvis = 1, nf = 1;
             int ql = 1;
-            while (nf > 0) {
-                // ---- dmin over the frontier
-                uint32_t dmin = kInf;
-                for (uint32_t i = lane; i < nf; i += 32) dmin = min(dmin, __ldcg(&key[front[i]]) >> 1);
-                dmin = __reduce_min_sync(kFull, dmin);
-                // ---- move the final vertices into the batch, compact the rest
-                uint32_t nb = 0, keep = 0;
-                for (uint32_t b0 = 0; b0 < nf; b0 += 32) {
-                    const uint32_t i = b0 + lane;
-                    const bool valid = i < nf;
-                    const uint32_t x = valid ? front[i] : 0u;
-                    const uint32_t kx = valid ? __ldcg(&key[x]) : kInf;
-                    bool take = valid && (uint64_t)(kx >> 1) < (uint64_t)dmin + win[x];
-                    const uint32_t tm = __ballot_sync(kFull, take);
-                    const uint32_t at = nb + __popc(tm & lanemask_lt());
-                    take = take && at < (uint32_t)kBatch;
-                    if (take) {
-                        s_bv[at] = x;
-                        s_bk[at] = kx;
-                    }
-                    nb = min(nb + __popc(tm), (uint32_t)kBatch);
-                    const bool kp = valid && !take;
-                    const uint32_t km = __ballot_sync(kFull, kp);
-                    if (kp) front[keep + __popc(km & lanemask_lt())] = x;
-                    keep += __popc(km);
-                }
-                nf = keep;
-                __syncwarp();
+            uint32_t dmin = 0;          // smallest queued distance (exact, see below)
+            bool stop = false;
+            uint32_t nb = 0;            // vertices in the smem batch
+
+            // Settle the batch held in smem: prune tests, labels, relaxations.
+            // New vertices are appended at front[nf..]; every key decrease of
+            // a queued vertex lowers dnext, so dnext is the exact minimum of
+            // the queue after the round.
+            uint32_t dnext = kInf;
+            auto settle = [&]() {
+                long long tc0 = clock64();
+                if (kPhaseTiming) dcnt[2]++;
                 t_size += nb;
-                // ---- settle: via bookkeeping (PLaNT) or rank skip (GLL)
                 int nv_batch = 0;
                 for (uint32_t j = lane; j < nb; j += 32) {
                     const uint32_t kx = s_bk[j];
-                    uint32_t skip = 0;
+                    const uint32_t rx = a.rank[s_bv[j]];
+                    uint32_t skip;
                     if (PLANT) {
                         nv_batch += (int)(kx & 1u);
+                        // a committed vertex (rank < r0) always has a committed
+                        // witness: pruned without reading its labels
+                        skip = rx < a.r0 ? 1u : 0u;
                     } else {
-                        skip = a.rank[s_bv[j]] < r ? 1u : 0u;   // iteration_gll :92
+                        skip = rx < r ? 1u : 0u;   // iteration_gll :92
                     }
                     s_bp[j] = skip;
                 }
                 if (PLANT) ql -= __reduce_add_sync(kFull, nv_batch);
                 __syncwarp();
-                // ---- prune tests: 4 vertices per step, 8 lanes x 4 entries each
+                long long tc1 = clock64();
+                cyc[1] += tc1 - tc0;
                 if (R > 0) {
-                    for (uint32_t j0 = 0; j0 < nb; j0 += 4) {
-                        const uint32_t j = j0 + g;
-                        const bool has = j < nb && s_bp[j] == 0;
-                        uint64_t lb = 0, le = 0;
-                        uint32_t dj = 0;
-                        if (has) {
-                            const uint32_t xu = lidx(s_bv[j], 1 - f, a.sides);
-                            lb = a.l_off[xu];
-                            le = a.l_off[xu + 1];
-                            dj = s_bk[j] >> 1;
-                        }
-                        const uint64_t st = lb & ~1ull;   // 16-byte aligned start
-                        bool found = false;
-                        uint32_t nread = 0;
-                        for (uint64_t c = st; ; c += 32) {
-                            const bool act = has && !found && c < le;
-                            if (!__any_sync(kFull, act)) break;
-                            bool hit = false;
-                            if (act) {
-                                const uint64_t e0 = c + 4 * sub;
-                                uint4 q0 = make_uint4(0, 0, 0, 0), q1 = make_uint4(0, 0, 0, 0);
-                                if (e0 < le) q0 = *(const uint4 *)(a.l_ent + e0);
-                                if (e0 + 2 < le) q1 = *(const uint4 *)(a.l_ent + e0 + 2);
-                                const uint32_t hh[4] = {q0.x, q0.z, q1.x, q1.z};
-                                const uint32_t dd[4] = {q0.y, q0.w, q1.y, q1.w};
-#pragma unroll
-                                for (int t = 0; t < 4; ++t) {
-                                    const uint64_t e = e0 + t;
-                                    if (e >= lb && e < le) {
-                                        const uint32_t p = bsearch_hub(rh, rstride, R, hh[t]);
-                                        if (p < R && rh[(size_t)p * rstride] == hh[t] &&
-                                            rd[(size_t)p * rstride] + dd[t] <= dj)
-                                            hit = true;
-                                    }
-                                }
-                                nread += 4;
-                            }
-                            const uint32_t hm = __ballot_sync(kFull, hit) & gmask;
-                            if (act && hm) found = true;
-                        }
-                        c_reads += nread;
-                        if (has && sub == 0 && found) s_bp[j] = 1;
+                    // Prune tests, dynamically scheduled over 8 lane groups:
+                    // a group of 4 lanes scans one vertex's list, each lane
+                    // reading 8 consecutive entries (256 contiguous bytes per
+                    // group and step); a group that finds a witness or reaches
+                    // the end of its list takes the next untested vertex at
+                    // once, so one long list does not hold the other groups.
+                    uint32_t ntest = 0;
+                    for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
+                        const uint32_t j = j0 + lane;
+                        const bool t = j < nb && s_bp[j] == 0;
+                        const uint32_t m = __ballot_sync(kFull, t);
+                        if (t) s_tl[ntest + __popc(m & lanemask_lt())] = j;
+                        ntest += __popc(m);
                     }
                     __syncwarp();
+                    const uint32_t gbase = lane & ~3u;
+                    uint32_t gj = kInf, gk = 0, gnch = 0, gdj = 0, handed = 0, nread = 0;
+                    uint64_t glb = 0, gle = 0, gst = 0;
+                    while (true) {
+                        const bool need = gj == kInf || gk >= gnch;
+                        if (need) gj = kInf;
+                        const uint32_t nm = __ballot_sync(kFull, need && sub == 0);
+                        if (need) {
+                            const uint32_t idx = handed + __popc(nm & ((1u << gbase) - 1u));
+                            if (idx < ntest) {
+                                gj = s_tl[idx];
+                                const uint32_t xu = lidx(s_bv[gj], 1 - f, a.sides);
+                                glb = a.l_off[xu];
+                                gle = a.l_off[xu + 1];
+                                gdj = s_bk[gj] >> 1;
+                                gst = glb & ~1ull;   // 16-byte aligned start
+                                gnch = (uint32_t)((gle - gst + 31) >> 5);
+                                gk = 0;
+                            }
+                        }
+                        handed = min(handed + (uint32_t)__popc(nm), ntest);
+                        const bool act = gj != kInf && gk < gnch;
+                        if (!__any_sync(kFull, act) && handed >= ntest) break;
+                        bool hit = false;
+                        if (act) {
+                            // chunk order: from the end of the list when
+                            // a.scan_back (recent, local hubs first)
+                            const uint32_t ck = a.scan_back ? gnch - 1 - gk : gk;
+                            const uint64_t e0 = gst + 32ull * ck + 8 * sub;
+                            uint4 q[4];
+#pragma unroll
+                            for (int t = 0; t < 4; ++t) {
+                                q[t] = make_uint4(0, 0, 0, 0);
+                                if (e0 + 2 * t < gle) q[t] = *(const uint4 *)(a.l_ent + e0 + 2 * t);
+                            }
+                            // the lane's 8 hubs ascend: one binary search, then
+                            // short gallops from the previous lower bound
+                            uint32_t p = 0;
+                            bool first = true;
+#pragma unroll
+                            for (int t = 0; t < 8; ++t) {
+                                const uint64_t e = e0 + t;
+                                const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
+                                const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
+                                if (e >= glb && e < gle) {
+                                    if (first) {
+                                        p = bsearch_hub(rh, rstride, R, hh);
+                                        first = false;
+                                    } else {
+                                        p = gallop_hub(rh, rstride, R, p, hh);
+                                    }
+                                    if (p < R && rh[(size_t)p * rstride] == hh &&
+                                        rd[(size_t)p * rstride] + dd <= gdj)
+                                        hit = true;
+                                }
+                            }
+                            nread += 8;
+                        }
+                        const uint32_t hm = __ballot_sync(kFull, hit) & gmask;
+                        if (act) {
+                            if (hm) {
+                                if (sub == 0) s_bp[gj] = 1;
+                                gk = gnch;   // released next step
+                            } else {
+                                ++gk;
+                            }
+                        }
+                    }
+                    c_reads += nread;
+                    __syncwarp();
                 }
-                // ---- labels of the unpruned (and, for PLaNT, not via) vertices
+                long long tc2 = clock64();
+                cyc[2] += tc2 - tc1;
                 for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
                     const uint32_t j = j0 + lane;
                     bool emit = false;
@@ -651,7 +1142,8 @@ batch_kernel(TreeArgs a) {
                         t_lab += __popc(em);
                     }
                 }
-                // ---- arcs of the unpruned batch vertices (prefix over degrees)
+                long long tc3 = clock64();
+                cyc[3] += tc3 - tc2;
                 uint32_t total = 0;
                 for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
                     const uint32_t j = j0 + lane;
@@ -679,7 +1171,424 @@ batch_kernel(TreeArgs a) {
                     bool upd = false;
                     uint32_t w = 0, nk = 0, old = kInf;
                     if (t < total) {
-                        // batch vertex owning arc t: last j with s_bx[j] <= t
+                        uint32_t lo = 0, hi = nb;
+                        while (hi - lo > 1) {
+                            const uint32_t mid = (lo + hi) >> 1;
+                            if (s_bx[mid] <= t) lo = mid;
+                            else hi = mid;
+                        }
+                        const uint64_t e = s_ba[lo] + (t - s_bx[lo]);
+                        uint32_t len;
+                        if (UNIT) {
+                            w = ghead[e];
+                            len = 1;
+                        } else {
+                            const uint2 hl = garc[e];
+                            w = hl.x;
+                            len = hl.y;
+                        }
+                        const uint32_t kx = s_bk[lo];
+                        const uint64_t dd64 = (uint64_t)(kx >> 1) + len;
+                        if (dd64 < 0x7FFFFFFFull) {
+                            uint32_t nv = 1u;
+                            if (PLANT) nv = ((kx & 1u) && a.rank[w] >= r) ? 1u : 0u;
+                            nk = (uint32_t)dd64 * 2u + nv;
+                            old = atomicMin(&key[w], nk);
+                            upd = nk < old;
+                            if (upd) dnext = min(dnext, nk >> 1);
+                        } else {
+                            a.ctl->err = 1;   // the reference asserts dd < infty
+                        }
+                    }
+                    const bool fresh = upd && old == kInf;
+                    const uint32_t fm = __ballot_sync(kFull, fresh);
+                    if (fresh) {
+                        const uint32_t o = __popc(fm & lanemask_lt());
+                        if (nf + o < a.n && nvis + o < a.n) {
+                            front[nf + o] = w;
+                            vis[nvis + o] = w;
+                        } else {
+                            a.ctl->err = 2;
+                        }
+                    }
+                    nf = min(nf + __popc(fm), a.n);
+                    nvis = min(nvis + __popc(fm), a.n);
+                    if (PLANT) {
+                        int dq = 0;
+                        if (upd) dq = (int)(nk & 1u) - (old == kInf ? 0 : (int)(old & 1u));
+                        ql += __reduce_add_sync(kFull, dq);
+                    }
+                }
+                __syncwarp();
+                nb = 0;
+                if (PLANT && ql == 0) stop = true;   // plant :95 early exit
+                cyc[4] += clock64() - tc3;
+            };
+
+            while (nf > 0 && !stop) {
+                // One round: walk the queue once.  Vertices with
+                // d < dmin + win are final and go to the batch (settled
+                // whenever it fills); the rest are compacted in place.
+                // Vertices appended during the round cannot qualify in it
+                // (their d >= dmin + win), so the walk stops at nf0.
+                const uint32_t nf0 = nf;
+                uint32_t keep = 0;
+                dnext = kInf;
+                if (kPhaseTiming) {
+                    dcnt[0] += nf0;
+                    dcnt[1]++;
+                }
+                for (uint32_t b0 = 0; b0 < nf0 && !stop; b0 += 32) {
+                    if (nb > (uint32_t)kBatch - 32) settle();
+                    if (stop) break;
+                    const long long ts0 = clock64();
+                    const uint32_t i = b0 + lane;
+                    const bool valid = i < nf0;
+                    const uint32_t x = valid ? front[i] : 0u;
+                    const uint32_t kx = valid ? __ldcg(&key[x]) : kInf;
+                    const bool take = valid && (uint64_t)(kx >> 1) < (uint64_t)dmin + win[x];
+                    const uint32_t tm = __ballot_sync(kFull, take);
+                    if (take) {
+                        const uint32_t at = nb + __popc(tm & lanemask_lt());
+                        s_bv[at] = x;
+                        s_bk[at] = kx;
+                    }
+                    nb += __popc(tm);
+                    const bool kp = valid && !take;
+                    const uint32_t km = __ballot_sync(kFull, kp);
+                    if (kp) {
+                        front[keep + __popc(km & lanemask_lt())] = x;
+                        dnext = min(dnext, kx >> 1);
+                    }
+                    keep += __popc(km);
+                    __syncwarp();
+                    cyc[0] += clock64() - ts0;
+                }
+                if (nb && !stop) settle();
+                if (stop) break;
+                // close the gap between the kept part and the appended part
+                const uint32_t app = nf - nf0;
+                for (uint32_t t0 = 0; t0 < app; t0 += 32) {
+                    const uint32_t t = t0 + lane;
+                    uint32_t x = 0;
+                    if (t < app) x = front[nf0 + t];
+                    __syncwarp();
+                    if (t < app) front[keep + t] = x;
+                    __syncwarp();
+                }
+                nf = keep + app;
+                dmin = __reduce_min_sync(kFull, dnext);
+            }
+            c_vis += t_size;
+            const long long tz0 = clock64();
+            for (uint32_t k = lane; k < nvis; k += 32) __stcg(&key[vis[k]], kInf);
+            cyc[6] += clock64() - tz0;
+            __syncwarp();
+        }
+        if (lane == 0) {
+            a.tree_size[r - a.r0] = t_size;
+            a.tree_labels[r - a.r0] = t_lab;
+        }
+    }
+    if (lane == 0) {
+        atomicAdd(&a.ctl->visits, c_vis);
+        atomicAdd(&a.ctl->arcs, c_arcs);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c_reads += __shfl_xor_sync(kFull, c_reads, o);
+    if (lane == 0) {
+        atomicAdd(&a.ctl->label_reads, c_reads);
+        if (kPhaseTiming) {
+            cyc[7] = clock64() - k_start;   // whole residency of the warp
+#pragma unroll
+            for (int i = 0; i < 8; ++i) atomicAdd(&a.ctl->cyc[i], (unsigned long long)cyc[i]);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) atomicAdd(&a.ctl->cnt[i], dcnt[i]);
+        }
+    }
+}
+
+// ------------------------------------------------------ settle kernel (v3)
+//
+// Per-warp trees like batch_kernel, with two changes that remove most of its
+// dependent memory round trips:
+//  * the queue is a log of (vertex, distance snapshot) entries; a key
+//    decrease appends a new entry instead of updating one in place.  The
+//    round's scan reads the log sequentially plus a 16-bit copy of win
+//    (L2-resident); only candidates read their key, and an entry whose
+//    snapshot differs from the key is stale and dropped.  The minimum
+//    snapshot over the log is the minimum queued distance (a stale entry
+//    always has a larger snapshot than its vertex's current entry).
+//  * prune tests stage the label lists of the whole batch into shared
+//    memory with cp.async, up to kStageEnt entries per fill (kStageCap per
+//    vertex per fill, round robin), so a round costs a few memory round
+//    trips instead of one per 32-entry step of every vertex.
+constexpr int kSB = 64;           // batch capacity (vertices)
+constexpr int kStageEnt = 512;    // label entries staged per fill
+constexpr int kStageCap = 128;    // entries per vertex per fill
+constexpr int kSeg = 32;          // segments (vertex pieces) per fill
+
+__host__ __device__ constexpr size_t settle_smem_per_warp(uint32_t rcap) {
+    return ((size_t)8 * kStageEnt + (size_t)8 * 4 * kSB + (size_t)8 * kSeg +
+            (size_t)4 * (4 * kSB + kSB + 1 + 3 * kSeg + 2 * rcap) + 64 + 15) &
+           ~(size_t)15;
+}
+
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+template <bool UNIT, bool PLANT>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+settle_kernel(TreeArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
+    const uint32_t slot = blockIdx.x * kWarpsPerBlock + wib;
+    unsigned char *base = smem + wib * settle_smem_per_warp(a.rcap);
+    uint2 *s_buf = (uint2 *)base;                                  // staged label entries
+    uint64_t *s_ba = (uint64_t *)(s_buf + kStageEnt);              // arc begin
+    uint64_t *s_lo = s_ba + kSB;                                   // next entry to stage
+    uint64_t *s_le = s_lo + kSB;                                   // list end
+    uint64_t *s_lb = s_le + kSB;                                   // list begin
+    uint64_t *s_sge = s_lb + kSB;                                  // segment: first entry
+    uint32_t *s_bv = (uint32_t *)(s_sge + kSeg);
+    uint32_t *s_bk = s_bv + kSB;
+    uint32_t *s_bp = s_bk + kSB;
+    uint32_t *s_tl = s_bp + kSB;
+    uint32_t *s_bx = s_tl + kSB;                                   // kSB + 1
+    uint32_t *s_sgb = s_bx + kSB + 1;                              // segment: buffer start
+    uint32_t *s_sgn = s_sgb + kSeg;                                // segment: entries
+    uint32_t *s_sgj = s_sgn + kSeg;                                // segment: batch index
+    uint32_t *s_rh = s_sgj + kSeg;
+    uint32_t *s_rd = s_rh + a.rcap;
+
+    uint32_t *key = a.ws_key + (size_t)slot * a.n;
+    uint32_t *vis = a.ws_vis + (size_t)slot * a.n;
+    uint2 *fq = a.ws_fq + (size_t)slot * a.fq_cap;
+    unsigned long long c_vis = 0, c_reads = 0, c_arcs = 0;
+
+    while (true) {
+        uint32_t r = kInf;
+        if (lane == 0) {
+            unsigned long long used = *(volatile unsigned long long *)&a.ctl->nlab;
+            if (used < a.budget) {
+                unsigned long long t = atomicAdd(&a.ctl->next_root, 1ull);
+                if (t < a.r_end) r = (uint32_t)t;
+            }
+        }
+        r = __shfl_sync(kFull, r, 0);
+        if (r == kInf) break;
+        uint32_t t_size = 0, t_lab = 0;
+        const uint32_t v = a.order[r];
+        for (int sd = 0; sd < a.sides; ++sd) {
+            const int f = (a.sides == 1) ? 1 : sd;
+            const uint64_t *goff = a.g_off[f];
+            const uint2 *garc = a.g_arc[f];
+            const uint32_t *ghead = a.g_head[f];
+            const uint16_t *win = a.win16[f];
+            const uint32_t ridx = lidx(v, f, a.sides);
+            const uint64_t rb = a.l_off[ridx], re = a.l_off[ridx + 1];
+            const uint32_t R = (uint32_t)(re - rb);
+            const uint32_t *rh, *rd;
+            int rstride;
+            if (R <= a.rcap) {
+                for (uint32_t k = lane; k < R; k += 32) {
+                    const uint2 e = a.l_ent[rb + k];
+                    s_rh[k] = e.x;
+                    s_rd[k] = e.y;
+                }
+                rh = s_rh;
+                rd = s_rd;
+                rstride = 1;
+            } else {
+                rh = (const uint32_t *)(a.l_ent + rb);
+                rd = rh + 1;
+                rstride = 2;
+            }
+            if (lane == 0) {
+                __stcg(&key[v], 1u);
+                vis[0] = v;
+                fq[0] = make_uint2(v, 0u);
+            }
+            __syncwarp();
+            uint32_t nvis = 1, nf = 1;
+            int ql = 1;
+            uint32_t dmin = 0, dnext = kInf;
+            bool stop = false;
+            uint32_t nb = 0;
+
+            auto settle = [&]() {
+                t_size += nb;
+                int nv_batch = 0;
+                for (uint32_t j = lane; j < nb; j += 32) {
+                    const uint32_t kx = s_bk[j];
+                    const uint32_t rx = a.rank[s_bv[j]];
+                    uint32_t skip;
+                    if (PLANT) {
+                        nv_batch += (int)(kx & 1u);
+                        skip = rx < a.r0 ? 1u : 0u;   // committed: always pruned
+                    } else {
+                        skip = rx < r ? 1u : 0u;      // iteration_gll :92
+                    }
+                    s_bp[j] = skip;
+                }
+                if (PLANT) ql -= __reduce_add_sync(kFull, nv_batch);
+                __syncwarp();
+                if (R > 0) {
+                    // list bounds of the vertices to test
+                    uint32_t ntest = 0;
+                    for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
+                        const uint32_t j = j0 + lane;
+                        const bool t = j < nb && s_bp[j] == 0;
+                        const uint32_t m = __ballot_sync(kFull, t);
+                        if (t) {
+                            s_tl[ntest + __popc(m & lanemask_lt())] = j;
+                            const uint32_t xu = lidx(s_bv[j], 1 - f, a.sides);
+                            const uint64_t lb = a.l_off[xu], le = a.l_off[xu + 1];
+                            s_lb[j] = lb;
+                            s_le[j] = le;
+                            s_lo[j] = lb & ~1ull;   // 16-byte aligned
+                        }
+                        ntest += __popc(m);
+                    }
+                    __syncwarp();
+                    uint32_t cursor = 0;
+                    while (true) {
+                        // plan one fill (lane 0): round robin over open vertices
+                        uint32_t pos = 0, nseg = 0;
+                        if (lane == 0) {
+                            uint32_t scanned = 0;
+                            while (pos < (uint32_t)kStageEnt && nseg < (uint32_t)kSeg && scanned < ntest) {
+                                const uint32_t j = s_tl[cursor];
+                                cursor = cursor + 1 == ntest ? 0 : cursor + 1;
+                                ++scanned;
+                                const uint64_t lo = s_lo[j], le = s_le[j];
+                                if (s_bp[j] || lo >= le) continue;
+                                uint64_t take = le - lo;
+                                if (take > (uint64_t)kStageCap) take = kStageCap;
+                                if (take > (uint64_t)(kStageEnt - pos)) take = kStageEnt - pos;
+                                take = (take + 1) & ~1ull;   // whole 16-byte pairs
+                                s_sgb[nseg] = pos;
+                                s_sgn[nseg] = (uint32_t)take;
+                                s_sge[nseg] = lo;
+                                s_sgj[nseg] = j;
+                                s_lo[j] = lo + take;
+                                pos += (uint32_t)take;
+                                ++nseg;
+                            }
+                        }
+                        pos = __shfl_sync(kFull, pos, 0);
+                        nseg = __shfl_sync(kFull, nseg, 0);
+                        if (pos == 0) break;
+                        __syncwarp();
+                        // issue the copies: 16 bytes (two entries) per lane op
+                        for (uint32_t sgi = 0; sgi < nseg; ++sgi) {
+                            const uint32_t bs = s_sgb[sgi], cnt = s_sgn[sgi];
+                            const uint2 *src = a.l_ent + s_sge[sgi];
+                            for (uint32_t k = 2 * lane; k < cnt; k += 64) cp_async16(s_buf + bs + k, src + k);
+                        }
+                        cp_async_wait_all();
+                        __syncwarp();
+                        // search: each lane takes 16 consecutive staged entries
+                        const uint32_t b0 = lane * (kStageEnt / 32);
+                        const uint32_t b1 = min(b0 + (uint32_t)(kStageEnt / 32), pos);
+                        uint32_t sg = 0;
+                        {
+                            uint32_t lo = 0, hi = nseg;
+                            while (hi - lo > 1) {
+                                const uint32_t mid = (lo + hi) >> 1;
+                                if (s_sgb[mid] <= b0) lo = mid;
+                                else hi = mid;
+                            }
+                            sg = lo;
+                        }
+                        uint32_t p = 0;
+                        bool fresh_seg = true;
+                        uint32_t nread = 0;
+                        for (uint32_t b = b0; b < b1; ++b) {
+                            while (sg + 1 < nseg && s_sgb[sg + 1] <= b) {
+                                ++sg;
+                                fresh_seg = true;
+                            }
+                            const uint32_t j = s_sgj[sg];
+                            const uint64_t e = s_sge[sg] + (b - s_sgb[sg]);
+                            if (e < s_lb[j] || e >= s_le[j] || s_bp[j]) continue;
+                            const uint2 ent = s_buf[b];
+                            if (fresh_seg) {
+                                p = bsearch_hub(rh, rstride, R, ent.x);
+                                fresh_seg = false;
+                            } else {
+                                p = gallop_hub(rh, rstride, R, p, ent.x);
+                            }
+                            ++nread;
+                            if (p < R && rh[(size_t)p * rstride] == ent.x &&
+                                rd[(size_t)p * rstride] + ent.y <= (s_bk[j] >> 1))
+                                s_bp[j] = 1;
+                        }
+                        c_reads += nread;
+                        __syncwarp();
+                    }
+                }
+                // labels of unpruned (PLaNT: and not via) vertices
+                for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
+                    const uint32_t j = j0 + lane;
+                    bool emit = false;
+                    uint32_t xu = 0, dj = 0;
+                    if (j < nb && s_bp[j] == 0) {
+                        const uint32_t kx = s_bk[j];
+                        emit = !PLANT || (kx & 1u);
+                        xu = lidx(s_bv[j], 1 - f, a.sides);
+                        dj = kx >> 1;
+                    }
+                    const uint32_t em = __ballot_sync(kFull, emit);
+                    if (em) {
+                        unsigned long long bb = 0;
+                        if (lane == 0) bb = atomicAdd(&a.ctl->nlab, (unsigned long long)__popc(em));
+                        bb = __shfl_sync(kFull, bb, 0);
+                        if (emit) {
+                            const unsigned long long q = bb + __popc(em & lanemask_lt());
+                            if (q < a.out_cap) {
+                                a.out_key[q] = ((uint64_t)xu << a.hub_bits) | (uint64_t)(r - a.r0);
+                                a.out_val[q] = dj;
+                            } else {
+                                a.ctl->overflow = 1;
+                            }
+                        }
+                        t_lab += __popc(em);
+                    }
+                }
+                // arcs of the unpruned batch vertices
+                uint32_t total = 0;
+                for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
+                    const uint32_t j = j0 + lane;
+                    uint32_t deg = 0;
+                    if (j < nb && s_bp[j] == 0) {
+                        const uint32_t x = s_bv[j];
+                        const uint64_t ab = goff[x];
+                        deg = (uint32_t)(goff[x + 1] - ab);
+                        s_ba[j] = ab;
+                    }
+                    uint32_t incl = deg;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t y = __shfl_up_sync(kFull, incl, o);
+                        if (lane >= (uint32_t)o) incl += y;
+                    }
+                    if (j < nb) s_bx[j] = total + incl - deg;
+                    total += __shfl_sync(kFull, incl, 31);
+                }
+                if (lane == 0) s_bx[nb] = total;
+                __syncwarp();
+                c_arcs += total;
+                for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+                    const uint32_t t = t0 + lane;
+                    bool upd = false;
+                    uint32_t w = 0, nk = 0, old = kInf;
+                    if (t < total) {
                         uint32_t lo = 0, hi = nb;
                         while (hi - lo > 1) {
                             const uint32_t mid = (lo + hi) >> 1;
@@ -708,18 +1617,24 @@ batch_kernel(TreeArgs a) {
                             a.ctl->err = 1;   // the reference asserts dd < infty
                         }
                     }
+                    // a new distance (fresh vertex or a strict decrease) gets
+                    // a log entry; a via flip at equal distance does not
                     const bool fresh = upd && old == kInf;
+                    const bool logit = upd && (old == kInf || (old >> 1) != (nk >> 1));
+                    const uint32_t lm = __ballot_sync(kFull, logit);
+                    if (logit) {
+                        const uint32_t o = __popc(lm & lanemask_lt());
+                        if (nf + o < a.fq_cap) fq[nf + o] = make_uint2(w, nk >> 1);
+                        else a.ctl->err = 2;
+                        dnext = min(dnext, nk >> 1);
+                    }
+                    nf = min(nf + __popc(lm), a.fq_cap);
                     const uint32_t fm = __ballot_sync(kFull, fresh);
                     if (fresh) {
                         const uint32_t o = __popc(fm & lanemask_lt());
-                        if (nf + o < a.n && nvis + o < a.n) {
-                            front[nf + o] = w;
-                            vis[nvis + o] = w;
-                        } else {
-                            a.ctl->err = 2;
-                        }
+                        if (nvis + o < a.n) vis[nvis + o] = w;
+                        else a.ctl->err = 2;
                     }
-                    nf = min(nf + __popc(fm), a.n);
                     nvis = min(nvis + __popc(fm), a.n);
                     if (PLANT) {
                         int dq = 0;
@@ -728,7 +1643,58 @@ batch_kernel(TreeArgs a) {
                     }
                 }
                 __syncwarp();
-                if (PLANT && ql == 0) break;   // plant :95 early exit
+                nb = 0;
+                if (PLANT && ql == 0) stop = true;   // plant :95 early exit
+            };
+
+            while (nf > 0 && !stop) {
+                const uint32_t nf0 = nf;
+                uint32_t keep = 0;
+                dnext = kInf;
+                for (uint32_t c0 = 0; c0 < nf0 && !stop; c0 += 32) {
+                    if (nb > (uint32_t)kSB - 32) settle();
+                    if (stop) break;
+                    const uint32_t i = c0 + lane;
+                    const bool valid = i < nf0;
+                    uint2 ent = make_uint2(0u, kInf);
+                    if (valid) ent = fq[i];
+                    bool cand = false;
+                    if (valid) cand = (uint64_t)ent.y < (uint64_t)dmin + win[ent.x];
+                    bool take = false;
+                    uint32_t kx = kInf;
+                    if (cand) {
+                        kx = __ldcg(&key[ent.x]);
+                        take = (kx >> 1) == ent.y;   // else a stale entry: dropped
+                    }
+                    const uint32_t tm = __ballot_sync(kFull, take);
+                    if (take) {
+                        const uint32_t at = nb + __popc(tm & lanemask_lt());
+                        s_bv[at] = ent.x;
+                        s_bk[at] = kx;
+                    }
+                    nb += __popc(tm);
+                    const bool kp = valid && !cand;
+                    const uint32_t km = __ballot_sync(kFull, kp);
+                    if (kp) {
+                        fq[keep + __popc(km & lanemask_lt())] = ent;
+                        dnext = min(dnext, ent.y);
+                    }
+                    keep += __popc(km);
+                    __syncwarp();
+                }
+                if (nb && !stop) settle();
+                if (stop) break;
+                const uint32_t app = nf - nf0;
+                for (uint32_t t0 = 0; t0 < app; t0 += 32) {
+                    const uint32_t t = t0 + lane;
+                    uint2 x = make_uint2(0u, 0u);
+                    if (t < app) x = fq[nf0 + t];
+                    __syncwarp();
+                    if (t < app) fq[keep + t] = x;
+                    __syncwarp();
+                }
+                nf = keep + app;
+                dmin = __reduce_min_sync(kFull, dnext);
             }
             c_vis += t_size;
             for (uint32_t k = lane; k < nvis; k += 32) __stcg(&key[vis[k]], kInf);
@@ -884,6 +1850,23 @@ __global__ void max_list_len(const uint64_t *off, uint32_t nl, unsigned long lon
     if ((threadIdx.x & 31) == 0) atomicMax(out, mx);
 }
 
+// max and sum of per-root tree sizes of a superstep (diagnostics)
+__global__ void tree_stats(const uint32_t *tsize, uint32_t cnt, unsigned long long *out2) {
+    unsigned long long mx = 0, sm = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+        mx = max(mx, (unsigned long long)tsize[i]);
+        sm += tsize[i];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = max(mx, __shfl_xor_sync(kFull, mx, o));
+        sm += __shfl_xor_sync(kFull, sm, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&out2[0], mx);
+        atomicAdd(&out2[1], sm);
+    }
+}
+
 inline int bits_for(uint64_t x) {   // bits needed to represent values < x
     int b = 0;
     while (b < 64 && (1ull << b) < x) ++b;
@@ -908,12 +1891,15 @@ struct DevGraph {
     uint2 *arc[2] = {nullptr, nullptr};
     uint32_t *head[2] = {nullptr, nullptr};
     uint32_t *win[2] = {nullptr, nullptr};   // shortest arc into v, per direction
+    uint16_t *win16[2] = {nullptr, nullptr};
     void release() {
         // side 1 may alias side 0 (symmetric graphs): free each buffer once
         if (off[1] != off[0]) cudaFree(off[1]);
         if (arc[1] != arc[0]) cudaFree(arc[1]);
         if (head[1] != head[0]) cudaFree(head[1]);
         if (win[1] != win[0]) cudaFree(win[1]);
+        if (win16[1] != win16[0]) cudaFree(win16[1]);
+        cudaFree(win16[0]);
         cudaFree(off[0]);
         cudaFree(arc[0]);
         cudaFree(head[0]);
@@ -923,6 +1909,7 @@ struct DevGraph {
             arc[s] = nullptr;
             head[s] = nullptr;
             win[s] = nullptr;
+            win16[s] = nullptr;
         }
     }
 };
@@ -961,12 +1948,18 @@ int upload_graph(const chl_graph *g, DevGraph &dg, cudaStream_t st) {
         int rc = dalloc(&dg.win[s], (size_t)g->n);
         if (rc) return rc;
         CHL_CUDA(cudaMemcpy(dg.win[s], w.data(), (size_t)g->n * 4, cudaMemcpyHostToDevice));
+        std::vector<uint16_t> w16(g->n);
+        for (uint32_t v = 0; v < g->n; ++v) w16[v] = (uint16_t)std::min<uint32_t>(w[v], 65535u);
+        rc = dalloc(&dg.win16[s], (size_t)g->n);
+        if (rc) return rc;
+        CHL_CUDA(cudaMemcpy(dg.win16[s], w16.data(), (size_t)g->n * 2, cudaMemcpyHostToDevice));
     }
     if (nsides == 1) {
         dg.off[1] = dg.off[0];
         dg.arc[1] = dg.arc[0];
         dg.head[1] = dg.head[0];
         dg.win[1] = dg.win[0];
+        dg.win16[1] = dg.win16[0];
     }
     return CHL_OK;
 }
@@ -1007,6 +2000,8 @@ struct Build {
     uint64_t *kpre = nullptr;
     uint32_t *tsize = nullptr, *tlab = nullptr;
     uint32_t *ws_key = nullptr, *ws_vis = nullptr, *ws_pos = nullptr, *ws_front = nullptr;
+    uint2 *ws_fq = nullptr;
+    uint32_t fq_cap = 0;
     uint64_t *ws_heap = nullptr;
     BuildCtl *ctl = nullptr;
     void *tmp = nullptr;
@@ -1037,6 +2032,7 @@ struct Build {
         cudaFree(ws_vis);
         cudaFree(ws_pos);
         cudaFree(ws_front);
+        cudaFree(ws_fq);
         cudaFree(ws_heap);
         cudaFree(ctl);
         cudaFree(tmp);
@@ -1161,8 +2157,11 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     const bool plant_mode = opts.mode != CHL_MODE_GLL;
     size_t free_b = 0, total_b = 0;
     CHL_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    const bool use_batch = opts.tree_algo == 0;
-    const size_t per_slot = (size_t)n * (use_batch ? 12 : (unit ? 8 : 20));
+    // tree kernels: 0/2 batch_kernel (default; also used when block-per-tree
+    // roots are requested), 1 tree_kernel (binary heap), 3 settle_kernel
+    const bool use_settle = opts.tree_algo == 3 && opts.cta_roots <= 0;
+    const bool use_batch = opts.tree_algo == 0 || opts.tree_algo == 2 || (opts.tree_algo == 3 && opts.cta_roots > 0);
+    const size_t per_slot = (size_t)n * (use_settle ? 24 : use_batch ? 12 : (unit ? 8 : 20));
     uint32_t want = (uint32_t)sms * 48;   // 12 blocks of 4 warps per SM at most
     if (opts.max_warps) want = std::min<uint32_t>(want, opts.max_warps);
     const size_t ws_budget = free_b / 3;
@@ -1172,7 +2171,10 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     const size_t slots = b.warps;
     if ((rc = dalloc(&b.ws_key, slots * n)) || (rc = dalloc(&b.ws_vis, slots * n))) return rc;
     CHL_CUDA(cudaMemsetAsync(b.ws_key, 0xFF, slots * n * 4, b.st));
-    if (use_batch) {
+    if (use_settle) {
+        b.fq_cap = (uint32_t)std::min<uint64_t>(2ull * n + 64, 0xFFFFFFF0ull);
+        if ((rc = dalloc(&b.ws_fq, slots * b.fq_cap))) return rc;
+    } else if (use_batch) {
         if ((rc = dalloc(&b.ws_front, slots * n))) return rc;
     } else if (!unit) {
         if ((rc = dalloc(&b.ws_pos, slots * n)) || (rc = dalloc(&b.ws_heap, slots * n))) return rc;
@@ -1208,6 +2210,8 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     unsigned long long visits = 0, reads = 0, arcs = 0, launches = 0, kernels = 0;
     double tree_ms = 0, sort_ms = 0, commit_ms = 0;
     uint32_t max_list = 0;   // longest committed list
+    float step_tree_ms = 0;
+    unsigned long long prev_max_tree = 0;
     // Superstep schedule: superstep k covers roots [r0, r0 + size) with
     // size = clamp(growth * r0, first, n) -- small while the top hubs are not
     // yet committed (their labels prune everything later), geometric after.
@@ -1216,6 +2220,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     const uint32_t first = opts.first_superstep ? opts.first_superstep : auto_first;
     const double growth = opts.growth > 0 ? opts.growth : auto_growth;
     while (r0 < n) {
+        const uint32_t r_begin = r0;
         const bool plant_now = do_plant;
         const unsigned long long budget = budget_base;
         uint64_t size = std::max<uint64_t>(first, (uint64_t)(growth * (double)r0));
@@ -1225,14 +2230,17 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         // root label staging capacity: longest committed list, bounded by smem
         int max_smem = 0;
         CHL_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0));
-        const size_t fixed = use_batch ? batch_smem_per_warp(0) : (unit ? 0 : kHeapSmem * 8) + kStage * 12;
+        const size_t fixed = use_settle ? settle_smem_per_warp(0)
+                             : use_batch ? batch_smem_per_warp(0)
+                                         : (unit ? 0 : kHeapSmem * 8) + kStage * 12;
         size_t rcap = std::min<uint32_t>(std::max<uint32_t>(max_list, 32), 2048);
         const size_t smem_cap = std::min<size_t>((size_t)max_smem, 96 * 1024);
         if (kWarpsPerBlock * (rcap * 8 + fixed) > smem_cap)
             rcap = (smem_cap / kWarpsPerBlock - fixed) / 8;
         b.rcap = (uint32_t)rcap;
-        const size_t smem = use_batch ? kWarpsPerBlock * batch_smem_per_warp(b.rcap)
-                                      : kWarpsPerBlock * ((size_t)b.rcap * 8 + fixed);
+        const size_t smem = use_settle  ? kWarpsPerBlock * settle_smem_per_warp(b.rcap)
+                            : use_batch ? kWarpsPerBlock * batch_smem_per_warp(b.rcap)
+                                        : kWarpsPerBlock * ((size_t)b.rcap * 8 + fixed);
         while (true) {
             std::memset(&hc, 0, sizeof(hc));
             hc.next_root = r0;
@@ -1267,8 +2275,25 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             const int blocks = (int)(b.warps / kWarpsPerBlock);
             for (int s2 = 0; s2 < 2; ++s2) ta.win[s2] = b.dg->win[s2];
             ta.ws_front = b.ws_front;
-            void (*kern)(TreeArgs);
+            ta.scan_back = opts.scan_order == 1 ? 1 : 0;
+            ta.smem_block = (uint32_t)smem;
+            ta.r_big = r0;
             if (use_batch) {
+                // block-per-tree for the superstep's first roots, on request
+                // only (measured slower than warp-per-tree on the road-like and
+                // scale-free benchmarks)
+                uint32_t kb = 0;
+                if (opts.cta_roots > 0) kb = (uint32_t)opts.cta_roots;
+                ta.r_big = (uint32_t)std::min<uint64_t>((uint64_t)r0 + kb, r_end);
+            }
+            for (int s2 = 0; s2 < 2; ++s2) ta.win16[s2] = b.dg->win16[s2];
+            ta.ws_fq = b.ws_fq;
+            ta.fq_cap = b.fq_cap;
+            void (*kern)(TreeArgs);
+            if (use_settle) {
+                if (unit) kern = plant_now ? settle_kernel<true, true> : settle_kernel<true, false>;
+                else kern = plant_now ? settle_kernel<false, true> : settle_kernel<false, false>;
+            } else if (use_batch) {
                 if (unit) kern = plant_now ? batch_kernel<true, true> : batch_kernel<true, false>;
                 else kern = plant_now ? batch_kernel<false, true> : batch_kernel<false, false>;
             } else if (unit) {
@@ -1288,6 +2313,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             float ms = 0;
             CHL_CUDA(cudaEventElapsedTime(&ms, ev_a, ev_b));
             tree_ms += ms;
+            step_tree_ms = ms;
             uint32_t r1 = (uint32_t)std::min<unsigned long long>(hc.next_root, r_end);
             if (hc.err) {
                 set_error(hc.err == 1 ? "a shortest-path distance reaches INT_MAX (the reference asserts dd < infty)"
@@ -1388,10 +2414,34 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         commit_ms += ms1;
         ++supersteps;
         r0 = r1;
+        unsigned long long tstat[2] = {0, 0};
+        if (use_batch || use_settle) {
+            CHL_CUDA(cudaMemsetAsync(&b.ctl->max_ratio_num, 0, 16, b.st));
+            tree_stats<<<sms, 256, 0, b.st>>>(b.tsize, r1 - r_begin, &b.ctl->max_ratio_num);
+            CHL_CUDA(cudaMemcpyAsync(tstat, &b.ctl->max_ratio_num, 16, cudaMemcpyDeviceToHost, b.st));
+            CHL_CUDA(cudaStreamSynchronize(b.st));
+        }
+        prev_max_tree = tstat[0];
+        if (opts.verbose >= 2) {
+            const double tot = (double)std::max<unsigned long long>(1, hc.cyc[7]);
+            fprintf(stderr, "  warp cycles: scan %.1f%% flags %.1f%% prune %.1f%% emit %.1f%% relax %.1f%% "
+                            "stage %.1f%% reset %.1f%% (sum of warp residencies %.3g cycles)\n",
+                    100 * hc.cyc[0] / tot, 100 * hc.cyc[1] / tot, 100 * hc.cyc[2] / tot, 100 * hc.cyc[3] / tot,
+                    100 * hc.cyc[4] / tot, 100 * hc.cyc[5] / tot, 100 * hc.cyc[6] / tot, tot);
+            fprintf(stderr, "  frontier entries scanned %llu rounds %llu settles %llu (per visit: scanned %.2f)\n",
+                    hc.cnt[0], hc.cnt[1], hc.cnt[2], (double)hc.cnt[0] / std::max<unsigned long long>(1, hc.visits));
+        }
         if (opts.verbose >= 2)
-            fprintf(stderr, "superstep %u: roots [%u,%u) %s labels %llu committed %llu\n", supersteps,
-                    r1 - (r1 - r0), r1, plant_now ? "plant" : "gll", (unsigned long long)M,
-                    (unsigned long long)committed);
+            fprintf(stderr, "  tree size max %llu mean %.1f\n", tstat[0],
+                    (double)tstat[1] / std::max<uint32_t>(1, r1 - r_begin));
+        if (opts.verbose >= 2)
+            fprintf(stderr,
+                    "superstep %u: roots [%u,%u) %s tree_ms %.2f labels %llu visits %llu reads %llu arcs %llu "
+                    "committed %llu max_list %u rcap %u\n",
+                    supersteps, r_begin, r1, plant_now ? "plant" : "gll",
+                    step_tree_ms, (unsigned long long)M, (unsigned long long)hc.visits,
+                    (unsigned long long)hc.label_reads, (unsigned long long)hc.arcs, (unsigned long long)committed,
+                    max_list, b.rcap);
     }
     CHL_CUDA(cudaEventRecord(ev1, b.st));
     CHL_CUDA(cudaStreamSynchronize(b.st));

@@ -15,7 +15,7 @@ from conftest import label_case
 pytestmark = pytest.mark.gpu
 
 MODES = {"hybrid": 0, "gll": 1, "plant": 2}
-ALGOS = {"batch": 0, "heap": 1}
+ALGOS = {"batch": 0, "heap": 1, "settle": 3}
 CASES = ["grid12", "grid20hw", "rmat8", "directed60", "unit_path"]
 
 
@@ -35,7 +35,8 @@ def test_golden_label_files(P, case, mode, algo, tmp_path):
     c = label_case(case)
     g = P.Graph.read(c["gr"])
     order = P.Order.read(c["order"])
-    L = P.build(g, order, mode=MODES[mode], tree_algo=ALGOS[algo], first_superstep=7, growth=0.3)
+    L = P.build(g, order, mode=MODES[mode], tree_algo=ALGOS[algo], first_superstep=7, growth=0.3,
+                cta_roots=3)
     out = str(tmp_path / "gpu.labels")
     L.write(out)
     assert filecmp.cmp(out, c["labels"], shallow=False)
@@ -65,6 +66,8 @@ def test_rmat_unit_lengths_matches_oracle(P, O, mode, algo):
     og = O.OGraph.from_csr(g.get_n(), off, head, ln)
     ref, _ = O.gll(og, order)
     L = P.build(g, order, mode=MODES[mode], sf=1.0, tree_algo=ALGOS[algo])
+    assert same_labels(L, ref, g.get_n())
+    L = P.build(g, order, mode=MODES[mode], sf=1.0, tree_algo=ALGOS[algo], cta_roots=1 << 30)
     assert same_labels(L, ref, g.get_n())
 
 
@@ -124,7 +127,10 @@ def test_build_is_deterministic(P):
     order = P.Order.degree(g, seed=4)
     a = P.build(g, order, sf=0.2).export()
     for kw in ({"max_warps": 64}, {"first_superstep": 1, "growth": 0.05},
-               {"first_superstep": 5000, "growth": 4.0}, {"tree_algo": 1, "max_warps": 8}):
+               {"first_superstep": 5000, "growth": 4.0}, {"tree_algo": 1, "max_warps": 8},
+               {"tree_algo": 3}, {"tree_algo": 3, "first_superstep": 3},
+               {"cta_roots": -1}, {"cta_roots": 1 << 30}, {"cta_roots": 7, "first_superstep": 50},
+               {"cta_roots": 1 << 30, "mode": 1}, {"scan_order": 1}, {"scan_order": 2}):
         b = P.build(g, order, sf=0.2, **kw).export()
         for x, y in zip(a, b):
             assert np.array_equal(x, y), kw
