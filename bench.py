@@ -67,6 +67,14 @@ def parse():
                     help="also run the open-loop serving test (Poisson arrivals) on the built labels")
     ap.add_argument("--serve-qps", type=float, default=2e8, help="offered pair rate (pairs/s)")
     ap.add_argument("--serve-seconds", type=float, default=5.0)
+    ap.add_argument("--rank", action="store_true",
+                    help="learned ranking: train on small labelings, evaluate against the plain order")
+    ap.add_argument("--rank-graphs", type=int, default=256)
+    ap.add_argument("--rank-epochs", type=int, default=12)
+    ap.add_argument("--rank-eval", default="rmat21,grid1448",
+                    help="comma list of evaluation graphs: rmatS or gridSIDE")
+    ap.add_argument("--rank-save", default="", help="write the trained parameters (.npy) here")
+    ap.add_argument("--rank-load", default="", help="skip training: load parameters (.npy)")
     return ap.parse_args()
 
 
@@ -377,7 +385,7 @@ def run_ours(args, ws, rank):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": (traffic or {}).get("bytes_per_unit_scaled"),
-                     "kernel": "tree_kernel", "algorithmic_bytes_per_build": work,
+                     "kernel": "batch_kernel", "algorithmic_bytes_per_build": work,
                      "tree_ms_per_build": avg_tree_ms, "tree_launches": stats[-1]["tree_launches"],
                      "ms_per_launch": per_launch_tree},
         "build": {"build_s": ms_step / 1e3, "avg_label": stats[-1]["avg_label"], "labels": labels,
@@ -407,8 +415,87 @@ def run_ours(args, ws, rank):
         dist.destroy_process_group()
 
 
+def eval_graph(P, spec):
+    """Evaluation graph by name: rmatS (ef 16) or gridSIDE (highways n/500)."""
+    if spec.startswith("rmat"):
+        return P.Graph.rmat(int(spec[4:]), 16, 0.57, 0.19, 0.19, seed=2021)
+    side = int(spec[4:])
+    return P.Graph.grid(side, side, highways=side * side // 500, hw_steps=64, hw_factor=150.0, seed=2021)
+
+
+def run_rank(args):
+    """Learned ranking: hub-frequency targets from GPU labelings of seeded
+    small graphs, GPU training, then the learned and the plain order compared
+    on unseen large graphs (labels exact under both)."""
+    import plant_gb300 as P
+    from plant_gb300 import ranking
+    from oracle import oracle as O
+    out = {"metric": "learned ranking vs plain order (average label size, GPU build time)",
+           "unit": "avg label entries per vertex side", "higher_is_better": False,
+           "data": "synthetic (seeded generators)", "n_gpus": 1}
+    if args.rank_load:
+        net = P.RankNet.load(args.rank_load)
+        out["training"] = {"loaded": os.path.basename(args.rank_load)}
+    else:
+        t0 = time.time()
+        samples = ranking.training_set(args.rank_graphs, seed=1)
+        t_label = time.time() - t0
+        net = P.RankNet(3, seed=1)
+        rep = ranking.train(net, samples, epochs=args.rank_epochs)
+        out["training"] = {"graphs": len(samples), "label_s": t_label, "epochs": rep.epochs,
+                           "steps": rep.steps, "train_s": rep.seconds,
+                           "loss_first_epoch": rep.first_epoch_loss, "loss_last_epoch": rep.last_epoch_loss,
+                           "vertices": int(sum(s_.graph.get_n() for s_ in samples))}
+        del samples
+        if args.rank_save:
+            net.save(args.rank_save)
+    evals = []
+    for spec in [x for x in args.rank_eval.split(",") if x]:
+        g = eval_graph(P, spec)
+        n = g.get_n()
+        g.to_device()
+        t = time.time()
+        plain = ranking.plain_order(g, seed=1)
+        t_plain = time.time() - t
+        t = time.time()
+        learned = net.order(g, seed=1)
+        t_learned = time.time() - t
+        Lp = P.build(g, plain)
+        sp = Lp.stats()
+        Ll = P.build(g, learned)
+        sl = Ll.stats()
+        # exactness: both labelings answer 1M sampled pairs identically, and a
+        # few pairs equal plain Dijkstra on the CPU
+        pairs = P.generate_query(1 << 20, n, seed=5)
+        same = bool(np.array_equal(P.query(Lp, pairs), P.query(Ll, pairs)))
+        off, head, ln = g.csr(True)
+        og = O.OGraph.from_csr(n, off, head, ln)
+        few = pairs[:8]
+        dj = [og.dijkstra(int(u))[int(v)] for u, v in few]
+        dq = P.query(Ll, few)
+        dj_ok = bool(all(int(a) == int(b) for a, b in zip(dj, dq)))
+        evals.append({"graph": spec, "vertices": n, "arcs": int(g.out_arcs()),
+                      "plain": {"kind": "degree" if ranking.is_heavy_tailed(g) else "betweenness(256)",
+                                "avg_label": sp["avg_label"], "build_ms": sp["build_ms"], "order_s": t_plain},
+                      "learned": {"avg_label": sl["avg_label"], "build_ms": sl["build_ms"], "order_s": t_learned},
+                      "label_ratio": sl["avg_label"] / sp["avg_label"],
+                      "build_ratio": sl["build_ms"] / sp["build_ms"],
+                      "used": "learned" if sl["avg_label"] <= sp["avg_label"] else "plain",
+                      "queries_agree_1M": same, "dijkstra_pairs_agree": dj_ok})
+        del Lp, Ll
+        g.release_device()
+        print(json.dumps(evals[-1]), file=sys.stderr, flush=True)
+    out["evaluation"] = evals
+    out["value"] = float(np.mean([e["label_ratio"] for e in evals])) if evals else None
+    out["value_meaning"] = "mean learned/plain average-label ratio (<= 1: the learned order is used)"
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.rank:
+        run_rank(args)
+        return
     global METRIC
     if args.workload == "rmat":
         METRIC = METRIC_RMAT

@@ -46,6 +46,7 @@ enum chl_status {
 typedef struct chl_graph chl_graph;
 typedef struct chl_labels chl_labels;
 typedef struct chl_server chl_server;
+typedef struct chl_gnn chl_gnn;
 
 /* Human-readable text for a status code (static storage). */
 const char *chl_status_str(int status);
@@ -160,18 +161,29 @@ typedef struct chl_build_opts {
     uint32_t first_superstep; /* roots in the first superstep, 0 = auto       */
     double growth;        /* superstep growth factor, 0 = auto                */
     uint32_t max_warps;   /* cap on concurrent trees, 0 = auto                */
-    int32_t tree_algo;    /* 0: batched settle (default), 1: binary heap      */
-    uint32_t reserved[7];
+    int32_t tree_algo;    /* 0 or 2: batched settle (default), 1: binary
+                             heap, 3: settle rounds over a logged frontier
+                             with staged prune tests                      */
+    int32_t scan_order;   /* prune-test list order: 0 auto, 1 from the end,
+                             2 from the start                              */
+    int32_t cta_roots;    /* roots per superstep built by a whole block:
+                             0 auto, -1 none, > 0 that many                */
+    uint32_t root_limit;  /* > 0: build the trees of ranks < root_limit only
+                             (the labels of those hubs, which are final;
+                             used to time schedules on a prefix)            */
+    uint32_t reserved[4];
 } chl_build_opts;
 
-/* Fill opts with the defaults (hybrid, sf 32, ps 1024, autotune on). */
+/* Fill opts with the defaults (hybrid, sf 32, ps 1024, autotune on,
+ * commit chain captured in a CUDA graph). */
 void chl_build_opts_default(chl_build_opts *opts);
 
 typedef struct chl_build_stats {
     double build_ms;       /* device time of the whole build (CUDA events)  */
     double tree_ms;        /* tree kernels                                  */
-    double sort_ms;        /* sort of new labels                            */
-    double commit_ms;      /* merge into the committed label arrays         */
+    double sort_ms;        /* 0: the sort is timed within commit_ms         */
+    double commit_ms;      /* sort, clean and merge of each superstep's new
+                              labels into the committed label arrays      */
     double h2d_ms;         /* graph/order upload                            */
     uint64_t labels;       /* total label entries (both sides)              */
     uint64_t visits;       /* vertices settled over all trees               */
@@ -293,11 +305,39 @@ int chl_server_submit(chl_server *s, const uint32_t *pairs, size_t k,
  * it.  timeout_ms < 0 waits forever; CHL_ERR_TIMEOUT if it expires. */
 int chl_server_wait(chl_server *s, uint64_t req_id, int32_t *out,
                     double timeout_ms, double *latency_ms);
-/* Drive the server loop once (admit + launch + complete); returns the
- * number of requests completed.  The server also runs its own thread. */
+/* Totals since creation: launches, pairs answered, requests completed. */
 int chl_server_stats(chl_server *s, uint64_t *launches, uint64_t *pairs,
                      uint64_t *requests);
 void chl_server_free(chl_server *s);
+
+/* ------------------------------------------------------- learned ranking */
+
+/* Message-passing ranking network (no reference counterpart; the reference
+ * reads its vertex order from a file, shared_memory/hhl.cpp:36-37).
+ * x_v = standardised [log1p deg, log1p 2-hop degree sum, sampled clustering];
+ * h_0 = relu(x W_0 + b_0); h_l = relu([h_{l-1}, mean_{out-nbrs} h_{l-1}] W_l
+ * + b_l) for l = 1..layers (BF16 tensor-core GEMMs, FP32 accumulation);
+ * score = h_L w + b.  Parameters are FP32, layout W_0[3x64] b_0[64] |
+ * per layer W_l[128x64] b_l[64] | w[64] b[1]. */
+int chl_gnn_create(uint32_t layers, uint64_t seed, chl_gnn **out);
+size_t chl_gnn_param_count(const chl_gnn *m);
+int chl_gnn_get_params(const chl_gnn *m, float *out);
+int chl_gnn_set_params(chl_gnn *m, const float *in);
+/* The n x 3 standardised input features (row-major). */
+int chl_gnn_features(const chl_graph *g, uint64_t seed, float *x);
+/* n scores (higher = more central). */
+int chl_gnn_predict(chl_gnn *m, const chl_graph *g, uint64_t seed, float *score);
+/* Mean squared error to target[n] and its gradient (param_count floats,
+ * may be NULL). */
+int chl_gnn_grad(chl_gnn *m, const chl_graph *g, uint64_t seed, const float *target,
+                 double *loss, float *grads);
+/* One Adam step (beta 0.9/0.999, eps 1e-8) on the gradient of chl_gnn_grad. */
+int chl_gnn_train_step(chl_gnn *m, const chl_graph *g, uint64_t seed, const float *target,
+                       float lr, double *loss);
+/* Order (rank -> vertex) by score descending, ties by the seeded tie key
+ * of chl_order_degree. */
+int chl_gnn_order(chl_gnn *m, const chl_graph *g, uint64_t seed, uint32_t *order);
+void chl_gnn_free(chl_gnn *m);
 
 #ifdef __cplusplus
 }

@@ -49,7 +49,8 @@ class BuildOpts(C.Structure):
     _fields_ = [("mode", C.c_int32), ("sf", C.c_double), ("ps", C.c_double),
                 ("autotune", C.c_int32), ("use_graphs", C.c_int32), ("verbose", C.c_int32),
                 ("first_superstep", C.c_uint32), ("growth", C.c_double),
-                ("max_warps", C.c_uint32), ("tree_algo", C.c_int32), ("reserved", C.c_uint32 * 7)]
+                ("max_warps", C.c_uint32), ("tree_algo", C.c_int32), ("scan_order", C.c_int32),
+                ("cta_roots", C.c_int32), ("root_limit", C.c_uint32), ("reserved", C.c_uint32 * 4)]
 
 
 class BuildStats(C.Structure):
@@ -75,6 +76,7 @@ _P = C.c_void_p
 _U32P = C.POINTER(C.c_uint32)
 _I32P = C.POINTER(C.c_int32)
 _U64P = C.POINTER(C.c_uint64)
+_F32P = C.POINTER(C.c_float)
 
 # name -> (restype, argtypes)
 SIGNATURES = {
@@ -129,6 +131,16 @@ SIGNATURES = {
     "chl_server_wait": (C.c_int, [_P, C.c_uint64, _I32P, C.c_double, C.POINTER(C.c_double)]),
     "chl_server_stats": (C.c_int, [_P, _U64P, _U64P, _U64P]),
     "chl_server_free": (None, [_P]),
+    "chl_gnn_create": (C.c_int, [C.c_uint32, C.c_uint64, C.POINTER(_P)]),
+    "chl_gnn_param_count": (C.c_size_t, [_P]),
+    "chl_gnn_get_params": (C.c_int, [_P, _F32P]),
+    "chl_gnn_set_params": (C.c_int, [_P, _F32P]),
+    "chl_gnn_features": (C.c_int, [_P, C.c_uint64, _F32P]),
+    "chl_gnn_predict": (C.c_int, [_P, _P, C.c_uint64, _F32P]),
+    "chl_gnn_grad": (C.c_int, [_P, _P, C.c_uint64, _F32P, C.POINTER(C.c_double), _F32P]),
+    "chl_gnn_train_step": (C.c_int, [_P, _P, C.c_uint64, _F32P, C.c_float, C.POINTER(C.c_double)]),
+    "chl_gnn_order": (C.c_int, [_P, _P, C.c_uint64, _U32P]),
+    "chl_gnn_free": (None, [_P]),
 }
 
 
@@ -376,7 +388,8 @@ class Labeling:
 
 def build(g: Graph, order, mode: int = MODE_HYBRID, sf: float = 32.0, ps: float = 1024.0,
           verbose: int = 0, max_warps: int = 0, autotune: int = 1, tree_algo: int = 0,
-          first_superstep: int = 0, growth: float = 0.0) -> Labeling:
+          first_superstep: int = 0, growth: float = 0.0, scan_order: int = 0,
+          cta_roots: int = 0, use_graphs: Optional[int] = None, root_limit: int = 0) -> Labeling:
     o = _u32(order)
     opts = BuildOpts()
     lib().chl_build_opts_default(C.byref(opts))
@@ -389,6 +402,11 @@ def build(g: Graph, order, mode: int = MODE_HYBRID, sf: float = 32.0, ps: float 
     opts.tree_algo = tree_algo
     opts.first_superstep = first_superstep
     opts.growth = growth
+    opts.scan_order = scan_order
+    opts.cta_roots = cta_roots
+    if use_graphs is not None:
+        opts.use_graphs = use_graphs
+    opts.root_limit = root_limit
     h = C.c_void_p()
     _check(lib().chl_build(g._h, _ptr(o, _U32P), len(o), C.byref(opts), C.byref(h)), "build")
     return Labeling(h)
@@ -471,6 +489,91 @@ class Server:
     def close(self):
         if self._h:
             lib().chl_server_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class RankNet:
+    """Learned vertex ranking (message-passing network on the GPU).
+
+    No reference counterpart: the reference reads its order from a file
+    (shared_memory/hhl.cpp:36-37) made by outside tools (README.md:24).
+    """
+
+    HIDDEN = 64
+    FEATURES = 3
+
+    def __init__(self, layers: int = 3, seed: int = 1):
+        self.layers = layers
+        self._h = C.c_void_p()
+        _check(lib().chl_gnn_create(layers, seed, C.byref(self._h)), "gnn create")
+
+    def param_count(self) -> int:
+        return int(lib().chl_gnn_param_count(self._h))
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(self.param_count(), np.float32)
+        _check(lib().chl_gnn_get_params(self._h, _ptr(p, _F32P)), "gnn get params")
+        return p
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        if p.size != self.param_count():
+            raise ValueError("parameter vector has the wrong length")
+        _check(lib().chl_gnn_set_params(self._h, _ptr(p, _F32P)), "gnn set params")
+
+    @staticmethod
+    def features(g: Graph, seed: int = 1) -> np.ndarray:
+        x = np.zeros((g.get_n(), RankNet.FEATURES), np.float32)
+        _check(lib().chl_gnn_features(g._h, seed, _ptr(x, _F32P)), "gnn features")
+        return x
+
+    def predict(self, g: Graph, seed: int = 1) -> np.ndarray:
+        s = np.zeros(g.get_n(), np.float32)
+        _check(lib().chl_gnn_predict(self._h, g._h, seed, _ptr(s, _F32P)), "gnn predict")
+        return s
+
+    def grad(self, g: Graph, target, seed: int = 1):
+        t = np.ascontiguousarray(target, np.float32)
+        if t.size != g.get_n():
+            raise ValueError("target must have one value per vertex")
+        loss = C.c_double()
+        gr = np.zeros(self.param_count(), np.float32)
+        _check(lib().chl_gnn_grad(self._h, g._h, seed, _ptr(t, _F32P), C.byref(loss), _ptr(gr, _F32P)), "gnn grad")
+        return loss.value, gr
+
+    def train_step(self, g: Graph, target, lr: float = 1e-3, seed: int = 1) -> float:
+        t = np.ascontiguousarray(target, np.float32)
+        if t.size != g.get_n():
+            raise ValueError("target must have one value per vertex")
+        loss = C.c_double()
+        _check(lib().chl_gnn_train_step(self._h, g._h, seed, _ptr(t, _F32P), lr, C.byref(loss)), "gnn train")
+        return loss.value
+
+    def save(self, path: str) -> None:
+        """Parameters as a .npy float32 vector (load with the same layer count)."""
+        np.save(path, self.get_params())
+
+    @classmethod
+    def load(cls, path: str, layers: int = 3) -> "RankNet":
+        p = np.load(path).astype(np.float32)
+        net = cls(layers)
+        net.set_params(p)
+        return net
+
+    def order(self, g: Graph, seed: int = 1) -> np.ndarray:
+        o = np.zeros(g.get_n(), np.uint32)
+        _check(lib().chl_gnn_order(self._h, g._h, seed, _ptr(o, _U32P)), "gnn order")
+        return o
+
+    def close(self):
+        if self._h:
+            lib().chl_gnn_free(self._h)
             self._h = None
 
     def __del__(self):

@@ -26,11 +26,16 @@ SOURCES = [
     "chl_labels.cu",
     "chl_order.cu",
     "chl_server.cu",
+    "chl_gnn.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp,-ffp-contract=off",
           "-I" + os.path.join(HERE, "..", "include")]
+
+
+# extra nvcc flags for diagnostic builds, e.g. CHL_NVCC_FLAGS=-DCHL_PHASE_TIMING=1
+EXTRA = os.environ.get("CHL_NVCC_FLAGS", "").split()
 
 
 def _nvcc() -> str:
@@ -66,7 +71,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         o = os.path.join(OUT, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            cmd = [nvcc] + ARCH + COMMON + ["-c", s, "-o", o]
+            cmd = [nvcc] + ARCH + COMMON + EXTRA + ["-c", s, "-o", o]
             if src.endswith(".cu"):
                 cmd += ["-Xptxas", "-v"] if verbose else []
             else:

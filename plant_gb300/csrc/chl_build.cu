@@ -2009,8 +2009,11 @@ struct Build {
     cudaStream_t st = nullptr;
     uint32_t warps = 0;
     uint32_t rcap = 0;
+    cudaGraphExec_t commit_exec = nullptr;   // captured commit chain
+    uint64_t graph_launches = 0;
 
     ~Build() {
+        if (commit_exec) cudaGraphExecDestroy(commit_exec);
         own.release();
         cudaFree(order);
         cudaFree(rank);
@@ -2154,7 +2157,6 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     // workspace: one slot per resident warp
     const int sms = device_sms();
     const bool unit = g->unit;
-    const bool plant_mode = opts.mode != CHL_MODE_GLL;
     size_t free_b = 0, total_b = 0;
     CHL_CUDA(cudaMemGetInfo(&free_b, &total_b));
     // tree kernels: 0/2 batch_kernel (default; also used when block-per-tree
@@ -2180,10 +2182,12 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         if ((rc = dalloc(&b.ws_pos, slots * n)) || (rc = dalloc(&b.ws_heap, slots * n))) return rc;
     }
 
-    // Schedule defaults from graph statistics: heavy-tailed degree
-    // distributions (scale-free) start with few roots so the hubs commit
-    // before the bulk of the trees; bounded-degree (road-like) graphs start
-    // with one root per resident warp.
+    // Schedule defaults from graph statistics (measured on RMAT scale 18 and
+    // 512/1024-square grids): heavy-tailed degree distributions start with
+    // 1024 roots and double, so the hubs commit before the bulk of the trees
+    // while the early supersteps still fill the GPU; bounded-degree
+    // (road-like) graphs start with one root per resident warp and grow by
+    // half of the committed prefix.
     uint32_t auto_first;
     double auto_growth;
     {
@@ -2192,8 +2196,8 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         for (uint32_t v = 0; v < n; ++v) maxdeg = std::max<uint64_t>(maxdeg, g->off[1][v + 1] - g->off[1][v]);
         const double avgdeg = n ? (double)arcs_out / n : 0.0;
         const bool heavy = maxdeg > 32.0 * std::max(1.0, avgdeg);
-        auto_first = heavy ? 64u : std::max<uint32_t>(64u, b.warps);
-        auto_growth = heavy ? 1.0 : 0.5;
+        auto_first = heavy ? 1024u : std::max<uint32_t>(64u, b.warps);
+        auto_growth = heavy ? 2.0 : 0.5;
     }
 
     // superstep loop
@@ -2211,7 +2215,6 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     double tree_ms = 0, sort_ms = 0, commit_ms = 0;
     uint32_t max_list = 0;   // longest committed list
     float step_tree_ms = 0;
-    unsigned long long prev_max_tree = 0;
     // Superstep schedule: superstep k covers roots [r0, r0 + size) with
     // size = clamp(growth * r0, first, n) -- small while the top hubs are not
     // yet committed (their labels prune everything later), geometric after.
@@ -2219,12 +2222,13 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     // superstep early.
     const uint32_t first = opts.first_superstep ? opts.first_superstep : auto_first;
     const double growth = opts.growth > 0 ? opts.growth : auto_growth;
-    while (r0 < n) {
+    while (r0 < n && (opts.root_limit == 0 || r0 < opts.root_limit)) {
         const uint32_t r_begin = r0;
         const bool plant_now = do_plant;
         const unsigned long long budget = budget_base;
         uint64_t size = std::max<uint64_t>(first, (uint64_t)(growth * (double)r0));
         uint32_t r_end = (uint32_t)std::min<uint64_t>(n, (uint64_t)r0 + size);
+        if (opts.root_limit) r_end = std::min<uint32_t>(r_end, opts.root_limit);
         BuildCtl hc;
         bool rerun = false;
         // root label staging capacity: longest committed list, bounded by smem
@@ -2352,76 +2356,109 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
                 switch_open = false;
             }
         }
-        CHL_CUDA(cudaEventRecord(ev_a, b.st));
-        // --- sort the new labels by (list, hub)
-        int parity = 0;
-        if ((rc = radix_sort_pairs(b.nk0, b.nv0, b.nk1, b.nv1, (const uint64_t *)&b.ctl->nlab,
-                                   b.new_cap, b.key_bits, b.tmp, b.tmp_bytes, b.st, &parity)))
-            return rc;
-        kernels += 3 * ((b.key_bits + 7) / 8);
-        uint64_t *sk = parity ? b.nk1 : b.nk0;
-        uint32_t *sv = parity ? b.nv1 : b.nv0;
-        uint64_t *ak = parity ? b.nk0 : b.nk1;
-        uint32_t *av = parity ? b.nv0 : b.nv1;
-        const int cgrid = sms * 8;
-        const unsigned long long *d_count = &b.ctl->nlab;
-        // --- GLL clean
-        if (!plant_now && M > 0) {
+        // Sort, GLL clean and merge of the new labels, then the longest
+        // committed list: one stream-ordered chain with no host round trip,
+        // captured as a CUDA graph when opts.use_graphs is set.  The entry
+        // array is sized for every new label before the chain (the clean
+        // only removes labels).
+        if ((rc = ensure_ent(&b.ent_b, &b.ent_cap_b, committed + M))) return rc;
+        const bool clean_now = !plant_now && M > 0;
+        auto chain = [&]() -> int {
+            int rc2;
+            // --- sort the new labels by (list, hub)
+            int parity = 0;
+            if ((rc2 = radix_sort_pairs(b.nk0, b.nv0, b.nk1, b.nv1, (const uint64_t *)&b.ctl->nlab, b.new_cap,
+                                        b.key_bits, b.tmp, b.tmp_bytes, b.st, &parity)))
+                return rc2;
+            uint64_t *sk = parity ? b.nk1 : b.nk0;
+            uint32_t *sv = parity ? b.nv1 : b.nv0;
+            uint64_t *ak = parity ? b.nk0 : b.nk1;
+            uint32_t *av = parity ? b.nv0 : b.nv1;
+            const int cgrid = sms * 8;
+            const unsigned long long *d_count = &b.ctl->nlab;
+            // --- GLL clean (drops labels covered through a higher-ranked hub)
+            if (clean_now) {
+                CHL_CUDA(cudaMemsetAsync(b.cnt, 0, ((size_t)b.nl + 1) * 4, b.st));
+                count_keys<<<cgrid, 256, 0, b.st>>>(sk, d_count, b.new_cap, b.hub_bits, b.cnt);
+                if ((rc2 = scan_u32_excl(b.cnt, b.pre, b.nl, nullptr, b.tmp, b.tmp_bytes, b.st))) return rc2;
+                clean_mark<<<cgrid, 256, 0, b.st>>>(sk, sv, d_count, b.new_cap, b.hub_bits, r0, b.pre, b.order,
+                                                    b.rank, b.sides, b.keep);
+                if ((rc2 = scan_u32_excl(b.keep, b.kpre, b.new_cap, (const uint64_t *)d_count, b.tmp,
+                                         b.tmp_bytes, b.st)))
+                    return rc2;
+                compact_kept<<<cgrid, 256, 0, b.st>>>(sk, sv, b.keep, b.kpre, d_count, b.new_cap, ak, av,
+                                                      &b.ctl->n_keep);
+                CHL_CUDA(cudaMemcpyAsync(&b.ctl->nlab, &b.ctl->n_keep, 8, cudaMemcpyDeviceToDevice, b.st));
+                std::swap(sk, ak);
+                std::swap(sv, av);
+            }
+            // --- commit: merge the sorted new labels into the committed CSR
             CHL_CUDA(cudaMemsetAsync(b.cnt, 0, ((size_t)b.nl + 1) * 4, b.st));
             count_keys<<<cgrid, 256, 0, b.st>>>(sk, d_count, b.new_cap, b.hub_bits, b.cnt);
-            if ((rc = scan_u32_excl(b.cnt, b.pre, b.nl, nullptr, b.tmp, b.tmp_bytes, b.st))) return rc;
-            clean_mark<<<cgrid, 256, 0, b.st>>>(sk, sv, d_count, b.new_cap, b.hub_bits, r0, b.pre,
-                                                b.order, b.rank, b.sides, b.keep);
-            if ((rc = scan_u32_excl(b.keep, b.kpre, b.new_cap, (const uint64_t *)d_count, b.tmp,
-                                    b.tmp_bytes, b.st)))
-                return rc;
-            compact_kept<<<cgrid, 256, 0, b.st>>>(sk, sv, b.keep, b.kpre, d_count, b.new_cap, ak, av,
-                                                  &b.ctl->n_keep);
-            CHL_CUDA(cudaMemcpyAsync(&b.ctl->nlab, &b.ctl->n_keep, 8, cudaMemcpyDeviceToDevice, b.st));
-            kernels += 9;   // count, scan x3, clean, scan x3, compact
-            std::swap(sk, ak);
-            std::swap(sv, av);
-            CHL_CUDA(cudaMemcpyAsync(&M, &b.ctl->n_keep, 8, cudaMemcpyDeviceToHost, b.st));
-            CHL_CUDA(cudaStreamSynchronize(b.st));
+            if ((rc2 = scan_u32_excl(b.cnt, b.pre, b.nl, nullptr, b.tmp, b.tmp_bytes, b.st))) return rc2;
+            merge_offsets<<<cgrid, 256, 0, b.st>>>(b.off_a, b.pre, b.off_b, b.nl);
+            copy_old_lists<<<cgrid, 256, 0, b.st>>>(b.off_a, b.ent_a, b.off_b, b.ent_b, b.nl);
+            place_new<<<cgrid, 256, 0, b.st>>>(sk, sv, d_count, b.new_cap, b.hub_bits, r0, b.pre, b.off_a,
+                                               b.off_b, b.ent_b);
+            // longest committed list, for the next superstep's root staging
+            CHL_CUDA(cudaMemsetAsync(&b.ctl->max_ratio_den, 0, 8, b.st));
+            max_list_len<<<cgrid, 256, 0, b.st>>>(b.off_b, b.nl, &b.ctl->max_ratio_den);
+            CHL_CUDA(cudaGetLastError());
+            return CHL_OK;
+        };
+        kernels += 3 * ((b.key_bits + 7) / 8) + (clean_now ? 9 : 0) + 8;
+        CHL_CUDA(cudaEventRecord(ev_a, b.st));
+        if (opts.use_graphs) {
+            CHL_CUDA(cudaStreamBeginCapture(b.st, cudaStreamCaptureModeThreadLocal));
+            const int crc = chain();
+            cudaGraph_t cg = nullptr;
+            const cudaError_t ce = cudaStreamEndCapture(b.st, &cg);
+            if (crc) {
+                if (cg) cudaGraphDestroy(cg);
+                return crc;
+            }
+            CHL_CUDA(ce);
+            // reuse the executable graph when only kernel arguments changed
+            bool updated = false;
+            if (b.commit_exec) {
+                cudaGraphExecUpdateResultInfo info;
+                updated = cudaGraphExecUpdate(b.commit_exec, cg, &info) == cudaSuccess;
+                if (!updated) {
+                    (void)cudaGetLastError();
+                    cudaGraphExecDestroy(b.commit_exec);
+                    b.commit_exec = nullptr;
+                }
+            }
+            cudaError_t ie = cudaSuccess;
+            if (!updated) ie = cudaGraphInstantiate(&b.commit_exec, cg, 0);
+            cudaGraphDestroy(cg);
+            CHL_CUDA(ie);
+            CHL_CUDA(cudaGraphLaunch(b.commit_exec, b.st));
+            ++b.graph_launches;
+        } else if ((rc = chain())) {
+            return rc;
         }
         CHL_CUDA(cudaEventRecord(ev_b, b.st));
-        // --- commit: merge the sorted new labels into the committed CSR
-        CHL_CUDA(cudaMemsetAsync(b.cnt, 0, ((size_t)b.nl + 1) * 4, b.st));
-        count_keys<<<cgrid, 256, 0, b.st>>>(sk, d_count, b.new_cap, b.hub_bits, b.cnt);
-        if ((rc = scan_u32_excl(b.cnt, b.pre, b.nl, nullptr, b.tmp, b.tmp_bytes, b.st))) return rc;
-        if ((rc = ensure_ent(&b.ent_b, &b.ent_cap_b, committed + M))) return rc;
-        merge_offsets<<<cgrid, 256, 0, b.st>>>(b.off_a, b.pre, b.off_b, b.nl);
-        copy_old_lists<<<cgrid, 256, 0, b.st>>>(b.off_a, b.ent_a, b.off_b, b.ent_b, b.nl);
-        place_new<<<cgrid, 256, 0, b.st>>>(sk, sv, d_count, b.new_cap, b.hub_bits, r0, b.pre, b.off_a,
-                                           b.off_b, b.ent_b);
-        CHL_CUDA(cudaGetLastError());
-        kernels += 7;   // count, scan x3, offsets, copy, place
         std::swap(b.off_a, b.off_b);
         std::swap(b.ent_a, b.ent_b);
         std::swap(b.ent_cap_a, b.ent_cap_b);
-        committed += M;
-        CHL_CUDA(cudaEventRecord(ev_a, b.st));
-        // longest committed list, for the next superstep's root staging
-        CHL_CUDA(cudaMemsetAsync(&b.ctl->max_ratio_den, 0, 8, b.st));
-        max_list_len<<<cgrid, 256, 0, b.st>>>(b.off_a, b.nl, &b.ctl->max_ratio_den);
-        ++kernels;
-        unsigned long long mx = 0;
-        CHL_CUDA(cudaMemcpyAsync(&mx, &b.ctl->max_ratio_den, 8, cudaMemcpyDeviceToHost, b.st));
+        CHL_CUDA(cudaMemcpyAsync(&hc, b.ctl, sizeof(hc), cudaMemcpyDeviceToHost, b.st));
         CHL_CUDA(cudaStreamSynchronize(b.st));
-        max_list = (uint32_t)std::min<unsigned long long>(mx, 0xFFFFFFFFu);
+        M = hc.nlab;
+        committed += M;
+        max_list = (uint32_t)std::min<unsigned long long>(hc.max_ratio_den, 0xFFFFFFFFu);
         float ms1 = 0;
-        CHL_CUDA(cudaEventElapsedTime(&ms1, ev_b, ev_a));
+        CHL_CUDA(cudaEventElapsedTime(&ms1, ev_a, ev_b));
         commit_ms += ms1;
         ++supersteps;
         r0 = r1;
         unsigned long long tstat[2] = {0, 0};
-        if (use_batch || use_settle) {
+        if ((use_batch || use_settle) && opts.verbose >= 2) {
             CHL_CUDA(cudaMemsetAsync(&b.ctl->max_ratio_num, 0, 16, b.st));
             tree_stats<<<sms, 256, 0, b.st>>>(b.tsize, r1 - r_begin, &b.ctl->max_ratio_num);
             CHL_CUDA(cudaMemcpyAsync(tstat, &b.ctl->max_ratio_num, 16, cudaMemcpyDeviceToHost, b.st));
             CHL_CUDA(cudaStreamSynchronize(b.st));
         }
-        prev_max_tree = tstat[0];
         if (opts.verbose >= 2) {
             const double tot = (double)std::max<unsigned long long>(1, hc.cyc[7]);
             fprintf(stderr, "  warp cycles: scan %.1f%% flags %.1f%% prune %.1f%% emit %.1f%% relax %.1f%% "
@@ -2494,7 +2531,7 @@ extern "C" void chl_build_opts_default(chl_build_opts *o) {
     o->sf = 32.0;
     o->ps = 1024.0;
     o->autotune = 1;
-    o->use_graphs = 0;
+    o->use_graphs = 1;
     o->verbose = 0;
 }
 

@@ -48,4 +48,8 @@ int radix_sort_pairs(uint64_t *k0, uint32_t *v0, uint64_t *k1, uint32_t *v1,
                      size_t tmp_bytes, cudaStream_t s, int *parity);
 size_t radix_tmp_bytes();
 
+// Vertices by device score descending, ties by the seeded tie key (the same
+// rule as the degree order); writes the host order array (rank -> vertex).
+int order_by_score(uint32_t n, uint64_t seed, const float *d_score, uint32_t *order_h);
+
 }  // namespace chl

@@ -213,7 +213,24 @@ int order_by(uint32_t n, uint64_t seed, F primary, int primary_bits, uint32_t *o
     return CHL_OK;
 }
 
+// float score descending: order-preserving map of the IEEE bits, then complemented
+__global__ void score_keys(uint32_t n, const float *score, const uint32_t *vals, uint64_t *key) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t b = __float_as_uint(score[vals[i]]);
+        b = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+        key[i] = (uint64_t)(~b);
+    }
+}
+
 }  // namespace
+
+int order_by_score(uint32_t n, uint64_t seed, const float *d_score, uint32_t *order_h) {
+    if (n == 0) return CHL_OK;
+    const int grid = device_sms() * 4;
+    return order_by(
+        n, seed, [&](const uint32_t *vals, uint64_t *key) { score_keys<<<grid, 256>>>(n, d_score, vals, key); }, 32,
+        order_h);
+}
 
 }  // namespace chl
 

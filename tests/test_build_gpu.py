@@ -130,7 +130,8 @@ def test_build_is_deterministic(P):
                {"first_superstep": 5000, "growth": 4.0}, {"tree_algo": 1, "max_warps": 8},
                {"tree_algo": 3}, {"tree_algo": 3, "first_superstep": 3},
                {"cta_roots": -1}, {"cta_roots": 1 << 30}, {"cta_roots": 7, "first_superstep": 50},
-               {"cta_roots": 1 << 30, "mode": 1}, {"scan_order": 1}, {"scan_order": 2}):
+               {"cta_roots": 1 << 30, "mode": 1}, {"scan_order": 1}, {"scan_order": 2},
+               {"use_graphs": 0}, {"use_graphs": 0, "mode": 1}, {"use_graphs": 1, "mode": 1, "tree_algo": 3}):
         b = P.build(g, order, sf=0.2, **kw).export()
         for x, y in zip(a, b):
             assert np.array_equal(x, y), kw
@@ -148,3 +149,22 @@ def test_sampled_queries_equal_dijkstra(P, O):
         d = og.dijkstra(int(s))
         pairs = np.stack([np.full(n, s), np.arange(n)], 1).astype(np.uint32)
         assert np.array_equal(P.query(L, pairs), d)
+
+
+@pytest.mark.parametrize("mode", list(MODES))
+def test_root_limit_gives_the_label_prefix(P, mode):
+    """A build of the roots of rank < R holds exactly the full labeling's
+    entries whose hub rank is below R (labels of committed hubs are final)."""
+    g = P.Graph.grid(50, 50, highways=12, hw_steps=10, seed=13)
+    order = P.Order.betweenness(g, 64, seed=2)
+    full_off, full_hub, full_dist = P.build(g, order, mode=MODES[mode], sf=0.5).export()
+    for limit in (1, 37, 400):
+        off, hub, dist = P.build(g, order, mode=MODES[mode], sf=0.5, first_superstep=16, growth=0.5,
+                                 root_limit=limit).export()
+        top = int(hub.max())
+        assert top == limit - 1
+        for i in range(off.size - 1):
+            a, b = int(full_off[i]), int(full_off[i + 1])
+            keep = full_hub[a:b] <= top
+            assert np.array_equal(hub[off[i]:off[i + 1]], full_hub[a:b][keep])
+            assert np.array_equal(dist[off[i]:off[i + 1]], full_dist[a:b][keep])
