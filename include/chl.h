@@ -213,6 +213,14 @@ int chl_labels_write(const chl_labels *l, const char *path);
 /* Replaces hl::Labeling::read (shared_memory/labeling.hpp:186-208); the
  * labels are uploaded to the device. */
 int chl_labels_read(const char *path, chl_labels **out);
+/* Binary CSR twin of the label file (no reference counterpart): header
+ * "CHLLBL01", u32 n, u32 symmetric, u64 entries, u64 lists, then u64
+ * offsets[lists + 1] and (u32 hub, u32 dist) entries, little-endian; lists
+ * are v (symmetric) or 2v + side.  Streamed from / to device memory. */
+int chl_labels_save(const chl_labels *l, const char *path);
+/* Load a binary label file into device memory; CHL_ERR_FORMAT if the header,
+ * offsets or lists (ascending hubs < n, distances >= 0) are invalid. */
+int chl_labels_load(const char *path, chl_labels **out);
 /* Replaces Labeling::get_avg (shared_memory/labeling.hpp:153-158). */
 double chl_avg_label(const chl_labels *l);
 uint32_t chl_labels_n(const chl_labels *l);

@@ -118,6 +118,8 @@ SIGNATURES = {
     "chl_labels_export": (C.c_int, [_P, _U64P, _U32P, _I32P]),
     "chl_labels_import": (C.c_int, [C.c_uint32, _U64P, _U32P, _I32P, C.POINTER(_P)]),
     "chl_labels_hub_freq": (C.c_int, [_P, _U32P, _U32P]),
+    "chl_labels_save": (C.c_int, [_P, C.c_char_p]),
+    "chl_labels_load": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
     "chl_labels_free": (None, [_P]),
     "chl_query_batch": (C.c_int, [_P, _U32P, C.c_size_t, _I32P, _P]),
     "chl_query_batch_noalloc": (C.c_int, [_P, _U32P, C.c_size_t, _I32P, _P]),
@@ -329,6 +331,16 @@ class Labeling:
 
     def write(self, path: str) -> None:
         _check(lib().chl_labels_write(self._h, os.fsencode(path)), f"write {path}")
+
+    def save(self, path: str) -> None:
+        """Binary CSR file (fast cold start; see load)."""
+        _check(lib().chl_labels_save(self._h, os.fsencode(path)), f"save {path}")
+
+    @classmethod
+    def load(cls, path: str) -> "Labeling":
+        h = C.c_void_p()
+        _check(lib().chl_labels_load(os.fsencode(path), C.byref(h)), f"load {path}")
+        return cls(h)
 
     def get_avg(self) -> float:
         return lib().chl_avg_label(self._h)

@@ -27,6 +27,7 @@ SOURCES = [
     "chl_order.cu",
     "chl_server.cu",
     "chl_gnn.cu",
+    "chl_labelio.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

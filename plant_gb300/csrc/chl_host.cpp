@@ -231,6 +231,9 @@ extern "C" void chl_order_free(uint32_t *order) { free(order); }
 
 extern "C" int chl_labels_write(const chl_labels *l, const char *path) {
     if (!l || !path) return CHL_ERR_INVALID;
+    // labels in HBM are formatted there; labels that only exist in host
+    // memory (read from a file, imported) are written from the host copy
+    if (l->d_off) return write_labels_text_device(l, path);
     return write_labels_text(l, path);
 }
 
