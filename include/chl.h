@@ -171,7 +171,12 @@ typedef struct chl_build_opts {
     uint32_t root_limit;  /* > 0: build the trees of ranks < root_limit only
                              (the labels of those hubs, which are final;
                              used to time schedules on a prefix)            */
-    uint32_t reserved[4];
+    uint32_t root_stage;  /* root-label entries staged in shared memory per
+                             tree (batched settle), 0 = auto: the most that
+                             keeps the register-limited occupancy           */
+    int32_t prune_sched;  /* batched settle prune tests: 0 auto, 1 a lane
+                             group per vertex, 2 (vertex, chunk) items      */
+    uint32_t reserved[2];
 } chl_build_opts;
 
 /* Fill opts with the defaults (hybrid, sf 32, ps 1024, autotune on,

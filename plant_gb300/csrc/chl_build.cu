@@ -86,6 +86,7 @@ struct TreeArgs {
     const uint32_t *win[2];         // [f]: shortest arc into v along direction f
     uint32_t *ws_front;             // per warp slot: queued (unsettled) vertices
     int scan_back;                  // prune tests read label lists from the end
+    int chunk_sched;                // batch kernel: prune tests as (vertex, chunk) items
     uint32_t r_big;                 // roots below r_big: one block per tree
     uint32_t smem_block;            // dynamic shared memory of a block (bytes)
     const uint16_t *win16[2];       // win clamped to 65535 (a valid lower bound)
@@ -464,8 +465,7 @@ tree_kernel(TreeArgs a) {
 constexpr int kBatch = 128;
 
 __host__ __device__ constexpr size_t batch_smem_per_warp(uint32_t rcap) {
-    return ((size_t)8 * kBatch + (size_t)8 * kStage + (size_t)4 * (2 * rcap + 5 * kBatch + 1 + kStage) + 15) &
-           ~(size_t)15;
+    return ((size_t)8 * kBatch + (size_t)4 * (2 * rcap + 7 * kBatch + 1 + 8) + 15) & ~(size_t)15;
 }
 
 __device__ __forceinline__ uint32_t bsearch_hub(const uint32_t *rh, int rstride, uint32_t R, uint32_t h) {
@@ -499,6 +499,51 @@ __device__ __forceinline__ uint32_t gallop_hub(const uint32_t *rh, int rstride, 
     }
     return lo;
 }
+
+// The root's committed label as seen by the batch kernel's prune tests: the
+// first Rs entries staged in shared memory (hubs, distances), the rest read
+// from the global label array.  Lists are ascending by hub, so a probe of
+// index p < Rs never touches global memory.
+struct RootView {
+    const uint32_t *sh, *sd;   // staged prefix
+    const uint2 *g;            // whole list in global memory
+    uint32_t Rs, R;
+    __device__ __forceinline__ uint32_t hub(uint32_t p) const { return p < Rs ? sh[p] : __ldg(&g[p].x); }
+    __device__ __forceinline__ uint32_t dist(uint32_t p) const { return p < Rs ? sd[p] : __ldg(&g[p].y); }
+    // lower bound of h
+    __device__ __forceinline__ uint32_t lower(uint32_t h) const {
+        uint32_t lo = 0, hi = Rs;
+        if (Rs < R && (Rs == 0 || sh[Rs - 1] < h)) {
+            lo = Rs;
+            hi = R;
+        }
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (hub(mid) < h) lo = mid + 1;
+            else hi = mid;
+        }
+        return lo;
+    }
+    // lower bound of h in [p0, R), knowing hub(p0 - 1) < h (or p0 == 0)
+    __device__ __forceinline__ uint32_t gallop(uint32_t p0, uint32_t h) const {
+        uint32_t lo = p0, step = 1;
+        while (lo < R && hub(lo) < h) {
+            const uint32_t nxt = lo + step;
+            if (nxt >= R || hub(nxt) >= h) {
+                uint32_t l2 = lo + 1, h2 = nxt < R ? nxt : R;
+                while (l2 < h2) {
+                    const uint32_t mid = (l2 + h2) >> 1;
+                    if (hub(mid) < h) l2 = mid + 1;
+                    else h2 = mid;
+                }
+                return l2;
+            }
+            lo = nxt;
+            step <<= 1;
+        }
+        return lo;
+    }
+};
 
 // ------------------------------------------------- CTA-cooperative trees
 //
@@ -883,14 +928,16 @@ batch_kernel(TreeArgs a) {
     const uint32_t slot = blockIdx.x * kWarpsPerBlock + wib;
     unsigned char *base = smem + wib * batch_smem_per_warp(a.rcap);
     uint64_t *s_ba = (uint64_t *)base;                 // arc begin of batch vertex
-    uint64_t *s_sk = s_ba + kBatch;                    // (unused staging, kept for layout)
-    uint32_t *s_rh = (uint32_t *)(s_sk + kStage);
+    uint32_t *s_rh = (uint32_t *)(s_ba + kBatch);
     uint32_t *s_rd = s_rh + a.rcap;
     uint32_t *s_bv = s_rd + a.rcap;                    // batch vertex
     uint32_t *s_bk = s_bv + kBatch;                    // batch key
     uint32_t *s_bp = s_bk + kBatch;                    // 1: pruned or skipped
     uint32_t *s_bx = s_bp + kBatch;                    // arc prefix (kBatch + 1)
     uint32_t *s_tl = s_bx + kBatch + 1;                // batch indices still to test
+    uint32_t *s_bl = s_tl + kBatch;                    // label list length (chunk schedule)
+    uint32_t *s_nch = s_bl + kBatch;                   // label list chunks (chunk schedule)
+    uint32_t *s_as = s_nch + kBatch;                   // items of the step (8 groups)
 
     uint32_t *key = a.ws_key + (size_t)slot * a.n;
     uint32_t *vis = a.ws_vis + (size_t)slot * a.n;
@@ -969,21 +1016,16 @@ batch_kernel(TreeArgs a) {
             const uint32_t ridx = lidx(v, f, a.sides);
             const uint64_t rb = a.l_off[ridx], re = a.l_off[ridx + 1];
             const uint32_t R = (uint32_t)(re - rb);
-            const uint32_t *rh, *rd;
-            int rstride;
-            if (R <= a.rcap) {
-                for (uint32_t k = lane; k < R; k += 32) {
-                    const uint2 e = a.l_ent[rb + k];
-                    s_rh[k] = e.x;
-                    s_rd[k] = e.y;
-                }
-                rh = s_rh;
-                rd = s_rd;
-                rstride = 1;
-            } else {
-                rh = (const uint32_t *)(a.l_ent + rb);
-                rd = rh + 1;
-                rstride = 2;
+            RootView root;
+            root.sh = s_rh;
+            root.sd = s_rd;
+            root.g = (const uint2 *)(a.l_ent + rb);
+            root.R = R;
+            root.Rs = min(R, a.rcap);
+            for (uint32_t k = lane; k < root.Rs; k += 32) {
+                const uint2 e = a.l_ent[rb + k];
+                s_rh[k] = e.x;
+                s_rd[k] = e.y;
             }
             if (lane == 0) {
                 __stcg(&key[v], 1u);
@@ -1026,7 +1068,107 @@ batch_kernel(TreeArgs a) {
                 __syncwarp();
                 long long tc1 = clock64();
                 cyc[1] += tc1 - tc0;
-                if (R > 0) {
+                if (R > 0 && a.chunk_sched) {
+                    // Prune tests flattened to (vertex, 32-entry chunk) items,
+                    // chunk-major (chunk 0 of every vertex, then chunk 1, ...),
+                    // 8 lane groups taking the next 8 live items each step: a
+                    // round costs about (total chunks) / 8 steps instead of
+                    // the longest list's chunks, and an item of a vertex that
+                    // already has a witness is skipped.
+                    uint32_t ntest = 0, maxnch = 0;
+                    for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
+                        const uint32_t j = j0 + lane;
+                        const bool t = j < nb && s_bp[j] == 0;
+                        const uint32_t m = __ballot_sync(kFull, t);
+                        uint32_t nch = 0;
+                        if (t) {
+                            s_tl[ntest + __popc(m & lanemask_lt())] = j;
+                            const uint32_t xu = lidx(s_bv[j], 1 - f, a.sides);
+                            const uint64_t lb = a.l_off[xu], le = a.l_off[xu + 1];
+                            s_ba[j] = lb;
+                            s_bl[j] = (uint32_t)(le - lb);
+                            nch = (uint32_t)((le - (lb & ~1ull) + 31) >> 5);
+                            s_nch[j] = nch;
+                        }
+                        maxnch = max(maxnch, __reduce_max_sync(kFull, nch));
+                        ntest += __popc(m);
+                    }
+                    __syncwarp();
+                    const uint32_t nitems = ntest * maxnch;
+                    uint32_t cursor = 0, nread = 0;
+                    while (true) {
+                        // the next (up to) 8 live items, in item order
+                        uint32_t got = 0;
+                        while (got < 8 && cursor < nitems) {
+                            const uint32_t i = cursor + lane;
+                            bool live = false;
+                            uint32_t item = 0;
+                            if (i < nitems) {
+                                const uint32_t c = i / ntest;
+                                const uint32_t j = s_tl[i - c * ntest];
+                                live = s_bp[j] == 0 && c < s_nch[j];
+                                item = (c << 8) | j;
+                            }
+                            const uint32_t lm = __ballot_sync(kFull, live);
+                            const uint32_t nl = (uint32_t)__popc(lm);
+                            const uint32_t take = min(8u - got, nl);
+                            const uint32_t rk = __popc(lm & lanemask_lt());
+                            if (live && rk < take) s_as[got + rk] = item;
+                            if (take < nl) {
+                                // continue just after the last item taken
+                                const uint32_t lastm = __ballot_sync(kFull, live && rk + 1 == take);
+                                cursor += (uint32_t)__ffs(lastm);
+                            } else {
+                                cursor += 32;
+                            }
+                            got += take;
+                        }
+                        __syncwarp();
+                        if (got == 0) break;
+                        const bool act = g < got;
+                        bool hit = false;
+                        uint32_t gj = 0;
+                        if (act) {
+                            const uint32_t item = s_as[g];
+                            gj = item & 0xFFu;
+                            const uint32_t c = item >> 8;
+                            const uint64_t glb = s_ba[gj];
+                            const uint64_t gle = glb + s_bl[gj];
+                            const uint32_t gdj = s_bk[gj] >> 1;
+                            const uint32_t ck = a.scan_back ? s_nch[gj] - 1 - c : c;
+                            const uint64_t e0 = (glb & ~1ull) + 32ull * ck + 8 * sub;
+                            uint4 q[4];
+#pragma unroll
+                            for (int t = 0; t < 4; ++t) {
+                                q[t] = make_uint4(0, 0, 0, 0);
+                                if (e0 + 2 * t < gle) q[t] = *(const uint4 *)(a.l_ent + e0 + 2 * t);
+                            }
+                            uint32_t p = 0;
+                            bool first = true;
+#pragma unroll
+                            for (int t = 0; t < 8; ++t) {
+                                const uint64_t e = e0 + t;
+                                const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
+                                const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
+                                if (e >= glb && e < gle) {
+                                    if (first) {
+                                        p = root.lower(hh);
+                                        first = false;
+                                    } else {
+                                        p = root.gallop(p, hh);
+                                    }
+                                    if (p < R && root.hub(p) == hh && root.dist(p) + dd <= gdj) hit = true;
+                                }
+                            }
+                            nread += 8;
+                        }
+                        const uint32_t hm = __ballot_sync(kFull, hit) & gmask;
+                        if (act && hm && sub == 0) s_bp[gj] = 1;
+                        __syncwarp();
+                    }
+                    c_reads += nread;
+                    __syncwarp();
+                } else if (R > 0) {
                     // Prune tests, dynamically scheduled over 8 lane groups:
                     // a group of 4 lanes scans one vertex's list, each lane
                     // reading 8 consecutive entries (256 contiguous bytes per
@@ -1088,14 +1230,12 @@ batch_kernel(TreeArgs a) {
                                 const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
                                 if (e >= glb && e < gle) {
                                     if (first) {
-                                        p = bsearch_hub(rh, rstride, R, hh);
+                                        p = root.lower(hh);
                                         first = false;
                                     } else {
-                                        p = gallop_hub(rh, rstride, R, p, hh);
+                                        p = root.gallop(p, hh);
                                     }
-                                    if (p < R && rh[(size_t)p * rstride] == hh &&
-                                        rd[(size_t)p * rstride] + dd <= gdj)
-                                        hit = true;
+                                    if (p < R && root.hub(p) == hh && root.dist(p) + dd <= gdj) hit = true;
                                 }
                             }
                             nread += 8;
@@ -2009,6 +2149,7 @@ struct Build {
     cudaStream_t st = nullptr;
     uint32_t warps = 0;
     uint32_t rcap = 0;
+    uint32_t auto_stage = 2048;              // default root-label staging (batch kernel)
     cudaGraphExec_t commit_exec = nullptr;   // captured commit chain
     uint64_t graph_launches = 0;
 
@@ -2182,6 +2323,20 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         if ((rc = dalloc(&b.ws_pos, slots * n)) || (rc = dalloc(&b.ws_heap, slots * n))) return rc;
     }
 
+    if (use_batch) {
+        // staging capacity that keeps the register-limited block count per SM
+        int smem_sm = 0, reserved = 0, nb = 0;
+        CHL_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, 0));
+        CHL_CUDA(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, 0));
+        CHL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &nb, unit ? batch_kernel<true, true> : batch_kernel<false, true>, kWarpsPerBlock * 32, 0));
+        nb = std::max(nb, 1);
+        const size_t per_warp = ((size_t)smem_sm / nb - (size_t)reserved) / kWarpsPerBlock;
+        const size_t fixed0 = batch_smem_per_warp(0) + 16;
+        size_t cap = per_warp > fixed0 ? ((per_warp - fixed0) / 8) & ~(size_t)3 : 32;
+        b.auto_stage = (uint32_t)std::min<size_t>(2048, std::max<size_t>(32, cap));
+    }
+
     // Schedule defaults from graph statistics (measured on RMAT scale 18 and
     // 512/1024-square grids): heavy-tailed degree distributions start with
     // 1024 roots and double, so the hubs commit before the bulk of the trees
@@ -2239,6 +2394,14 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
                                          : (unit ? 0 : kHeapSmem * 8) + kStage * 12;
         size_t rcap = std::min<uint32_t>(std::max<uint32_t>(max_list, 32), 2048);
         const size_t smem_cap = std::min<size_t>((size_t)max_smem, 96 * 1024);
+        if (use_batch) {
+            // The batch kernel stages a prefix of the root label and reads the
+            // rest from global memory, so the staging capacity trades against
+            // occupancy: by default the largest capacity that keeps the
+            // register-limited number of blocks resident per SM.
+            uint32_t cap = opts.root_stage ? opts.root_stage : b.auto_stage;
+            rcap = std::min<size_t>(rcap, std::max<uint32_t>(cap, 32));
+        }
         if (kWarpsPerBlock * (rcap * 8 + fixed) > smem_cap)
             rcap = (smem_cap / kWarpsPerBlock - fixed) / 8;
         b.rcap = (uint32_t)rcap;
@@ -2280,6 +2443,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             for (int s2 = 0; s2 < 2; ++s2) ta.win[s2] = b.dg->win[s2];
             ta.ws_front = b.ws_front;
             ta.scan_back = opts.scan_order == 1 ? 1 : 0;
+            ta.chunk_sched = opts.prune_sched == 2 ? 1 : 0;
             ta.smem_block = (uint32_t)smem;
             ta.r_big = r0;
             if (use_batch) {
