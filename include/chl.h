@@ -175,8 +175,12 @@ typedef struct chl_build_opts {
                              tree (batched settle), 0 = auto: the most that
                              keeps the register-limited occupancy           */
     int32_t prune_sched;  /* batched settle prune tests: 0 auto, 1 a lane
-                             group per vertex, 2 (vertex, chunk) items      */
-    uint32_t reserved[2];
+                             group per vertex, 2 (vertex, 32-entry chunk)
+                             items, 3 (vertex, 64-entry chunk) items        */
+    int32_t root_probe;   /* batched settle root-label lookups: 0 auto,
+                             1 sorted staging + binary search, 2 hash table
+                             in shared memory                               */
+    uint32_t reserved[1];
 } chl_build_opts;
 
 /* Fill opts with the defaults (hybrid, sf 32, ps 1024, autotune on,

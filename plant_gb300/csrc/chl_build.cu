@@ -87,6 +87,9 @@ struct TreeArgs {
     uint32_t *ws_front;             // per warp slot: queued (unsettled) vertices
     int scan_back;                  // prune tests read label lists from the end
     int chunk_sched;                // batch kernel: prune tests as (vertex, chunk) items
+    uint32_t hash_slots;            // batch kernel: root hash table slots (0: sorted staging)
+    int wide;                       // chunk schedule: 64-entry items instead of 32
+    uint32_t hash_shift;            // 32 - log2(hash_slots)
     uint32_t r_big;                 // roots below r_big: one block per tree
     uint32_t smem_block;            // dynamic shared memory of a block (bytes)
     const uint16_t *win16[2];       // win clamped to 65535 (a valid lower bound)
@@ -545,6 +548,42 @@ struct RootView {
     }
 };
 
+// The root's committed label as an open-addressing hash table in shared
+// memory (linear probing, load <= 1/2), so the up to 8 lookups of a lane are
+// independent instead of a chain of dependent binary-search probes.  Entries
+// beyond the table's half capacity (the highest hubs) stay in the global
+// sorted list and are searched there.  Slot = hub << 32 | dist; ~0 = empty
+// (hub 0xFFFFFFFF never occurs: hubs are ranks < n < 2^32).
+constexpr uint64_t kSlotEmpty = ~0ull;
+
+__device__ __forceinline__ uint32_t slot_of(uint32_t h, uint32_t shift) { return (h * 0x9E3779B1u) >> shift; }
+
+struct RootHash {
+    const uint64_t *tab;
+    uint32_t mask;      // table slots - 1
+    uint32_t Th;        // entries hashed (the first Th of the list)
+    uint32_t hlast;     // hub of entry Th - 1 (0 if Th == 0)
+    const uint2 *g;     // whole list in global memory
+    uint32_t R;
+    // lookup of h; *dist set when found
+    __device__ __forceinline__ bool find_tail(uint32_t h, uint32_t &dist) const {
+        uint32_t lo = Th, hi = R;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(&g[mid].x) < h) lo = mid + 1;
+            else hi = mid;
+        }
+        if (lo < R) {
+            const uint2 e = __ldg(&g[lo]);
+            if (e.x == h) {
+                dist = e.y;
+                return true;
+            }
+        }
+        return false;
+    }
+};
+
 // ------------------------------------------------- CTA-cooperative trees
 //
 // The largest trees of a superstep (its first roots: roots go in rank
@@ -929,6 +968,7 @@ batch_kernel(TreeArgs a) {
     unsigned char *base = smem + wib * batch_smem_per_warp(a.rcap);
     uint64_t *s_ba = (uint64_t *)base;                 // arc begin of batch vertex
     uint32_t *s_rh = (uint32_t *)(s_ba + kBatch);
+    uint64_t *s_tab = (uint64_t *)s_rh;                // root hash table (same space as s_rh, s_rd)
     uint32_t *s_rd = s_rh + a.rcap;
     uint32_t *s_bv = s_rd + a.rcap;                    // batch vertex
     uint32_t *s_bk = s_bv + kBatch;                    // batch key
@@ -988,6 +1028,10 @@ batch_kernel(TreeArgs a) {
         __syncthreads();   // the block leaves the shared layout before warps reuse it
     }
     // ---- warp-per-tree phase
+    if (a.hash_slots) {
+        for (uint32_t k = lane; k < a.hash_slots; k += 32) s_tab[k] = kSlotEmpty;
+        __syncwarp();
+    }
     while (true) {
         uint32_t r = kInf;
         if (pending != kInf) {
@@ -1021,12 +1065,94 @@ batch_kernel(TreeArgs a) {
             root.sd = s_rd;
             root.g = (const uint2 *)(a.l_ent + rb);
             root.R = R;
-            root.Rs = min(R, a.rcap);
+            root.Rs = a.hash_slots ? 0u : min(R, a.rcap);
             for (uint32_t k = lane; k < root.Rs; k += 32) {
                 const uint2 e = a.l_ent[rb + k];
                 s_rh[k] = e.x;
                 s_rd[k] = e.y;
             }
+            RootHash rhash;
+            rhash.tab = s_tab;
+            rhash.mask = a.hash_slots - 1;
+            rhash.g = root.g;
+            rhash.R = R;
+            rhash.Th = 0;
+            rhash.hlast = 0;
+            if (a.hash_slots) {
+                rhash.Th = min(R, a.hash_slots / 2);
+                for (uint32_t k = lane; k < rhash.Th; k += 32) {
+                    const uint2 e = a.l_ent[rb + k];
+                    const uint64_t val = ((uint64_t)e.x << 32) | e.y;
+                    uint32_t sl = slot_of(e.x, a.hash_shift);
+                    while (atomicCAS((unsigned long long *)&s_tab[sl], (unsigned long long)kSlotEmpty,
+                                     (unsigned long long)val) != (unsigned long long)kSlotEmpty)
+                        sl = (sl + 1) & rhash.mask;
+                }
+                if (rhash.Th) rhash.hlast = a.l_ent[rb + rhash.Th - 1].x;
+            }
+            // Prune test of one lane's (up to) 8 consecutive entries of L(u)
+            // (entries [e0, e0 + 8) of which [glb, gle) belong to the list):
+            // does some (h, dd) with the root's (h, dr) give dr + dd <= gdj?
+            auto test8 = [&](const auto &q, uint64_t e0, uint64_t glb, uint64_t gle, uint32_t gdj) -> bool {
+                constexpr int NE = (int)(sizeof(q) / sizeof(uint4)) * 2;   // entries per lane
+                bool hit = false;
+                if (a.hash_slots) {
+                    // independent first probes, then the rare collision chains
+                    uint64_t v[NE];
+                    uint32_t sl[NE];
+#pragma unroll
+                    for (int t = 0; t < NE; ++t) {
+                        const uint64_t e = e0 + t;
+                        const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
+                        v[t] = kSlotEmpty;
+                        sl[t] = 0;
+                        if (e >= glb && e < gle && hh <= rhash.hlast && rhash.Th) {
+                            sl[t] = slot_of(hh, a.hash_shift);
+                            v[t] = s_tab[sl[t]];
+                        }
+                    }
+#pragma unroll
+                    for (int t = 0; t < NE; ++t) {
+                        const uint64_t e = e0 + t;
+                        const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
+                        const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
+                        if (e < glb || e >= gle) continue;
+                        if (rhash.Th && hh <= rhash.hlast) {
+                            uint64_t w = v[t];
+                            uint32_t z = sl[t];
+                            while (w != kSlotEmpty && (uint32_t)(w >> 32) != hh) {
+                                z = (z + 1) & rhash.mask;
+                                w = s_tab[z];
+                            }
+                            if (w != kSlotEmpty && (uint32_t)w + dd <= gdj) hit = true;
+                        } else if (rhash.Th < R) {
+                            uint32_t dr;
+                            if (rhash.find_tail(hh, dr) && dr + dd <= gdj) hit = true;
+                        }
+                    }
+                    return hit;
+                }
+                // sorted list: the lane's 8 hubs ascend, so one binary search,
+                // then short gallops from the previous lower bound
+                uint32_t p = 0;
+                bool first = true;
+#pragma unroll
+                for (int t = 0; t < NE; ++t) {
+                    const uint64_t e = e0 + t;
+                    const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
+                    const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
+                    if (e >= glb && e < gle) {
+                        if (first) {
+                            p = root.lower(hh);
+                            first = false;
+                        } else {
+                            p = root.gallop(p, hh);
+                        }
+                        if (p < R && root.hub(p) == hh && root.dist(p) + dd <= gdj) hit = true;
+                    }
+                }
+                return hit;
+            };
             if (lane == 0) {
                 __stcg(&key[v], 1u);
                 vis[0] = v;
@@ -1087,7 +1213,8 @@ batch_kernel(TreeArgs a) {
                             const uint64_t lb = a.l_off[xu], le = a.l_off[xu + 1];
                             s_ba[j] = lb;
                             s_bl[j] = (uint32_t)(le - lb);
-                            nch = (uint32_t)((le - (lb & ~1ull) + 31) >> 5);
+                            nch = a.wide ? (uint32_t)((le - (lb & ~1ull) + 63) >> 6)
+                                         : (uint32_t)((le - (lb & ~1ull) + 31) >> 5);
                             s_nch[j] = nch;
                         }
                         maxnch = max(maxnch, __reduce_max_sync(kFull, nch));
@@ -1136,31 +1263,28 @@ batch_kernel(TreeArgs a) {
                             const uint64_t gle = glb + s_bl[gj];
                             const uint32_t gdj = s_bk[gj] >> 1;
                             const uint32_t ck = a.scan_back ? s_nch[gj] - 1 - c : c;
-                            const uint64_t e0 = (glb & ~1ull) + 32ull * ck + 8 * sub;
-                            uint4 q[4];
+                            if (a.wide) {
+                                // 64-entry items: 16 entries (8 loads in flight) per lane
+                                const uint64_t e0 = (glb & ~1ull) + 64ull * ck + 16 * sub;
+                                uint4 q[8];
 #pragma unroll
-                            for (int t = 0; t < 4; ++t) {
-                                q[t] = make_uint4(0, 0, 0, 0);
-                                if (e0 + 2 * t < gle) q[t] = *(const uint4 *)(a.l_ent + e0 + 2 * t);
-                            }
-                            uint32_t p = 0;
-                            bool first = true;
-#pragma unroll
-                            for (int t = 0; t < 8; ++t) {
-                                const uint64_t e = e0 + t;
-                                const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
-                                const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
-                                if (e >= glb && e < gle) {
-                                    if (first) {
-                                        p = root.lower(hh);
-                                        first = false;
-                                    } else {
-                                        p = root.gallop(p, hh);
-                                    }
-                                    if (p < R && root.hub(p) == hh && root.dist(p) + dd <= gdj) hit = true;
+                                for (int t = 0; t < 8; ++t) {
+                                    q[t] = make_uint4(0, 0, 0, 0);
+                                    if (e0 + 2 * t < gle) q[t] = *(const uint4 *)(a.l_ent + e0 + 2 * t);
                                 }
+                                hit = test8(q, e0, glb, gle, gdj);
+                                nread += 16;
+                            } else {
+                                const uint64_t e0 = (glb & ~1ull) + 32ull * ck + 8 * sub;
+                                uint4 q[4];
+#pragma unroll
+                                for (int t = 0; t < 4; ++t) {
+                                    q[t] = make_uint4(0, 0, 0, 0);
+                                    if (e0 + 2 * t < gle) q[t] = *(const uint4 *)(a.l_ent + e0 + 2 * t);
+                                }
+                                hit = test8(q, e0, glb, gle, gdj);
+                                nread += 8;
                             }
-                            nread += 8;
                         }
                         const uint32_t hm = __ballot_sync(kFull, hit) & gmask;
                         if (act && hm && sub == 0) s_bp[gj] = 1;
@@ -1219,25 +1343,7 @@ batch_kernel(TreeArgs a) {
                                 q[t] = make_uint4(0, 0, 0, 0);
                                 if (e0 + 2 * t < gle) q[t] = *(const uint4 *)(a.l_ent + e0 + 2 * t);
                             }
-                            // the lane's 8 hubs ascend: one binary search, then
-                            // short gallops from the previous lower bound
-                            uint32_t p = 0;
-                            bool first = true;
-#pragma unroll
-                            for (int t = 0; t < 8; ++t) {
-                                const uint64_t e = e0 + t;
-                                const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
-                                const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
-                                if (e >= glb && e < gle) {
-                                    if (first) {
-                                        p = root.lower(hh);
-                                        first = false;
-                                    } else {
-                                        p = root.gallop(p, hh);
-                                    }
-                                    if (p < R && root.hub(p) == hh && root.dist(p) + dd <= gdj) hit = true;
-                                }
-                            }
+                            hit = test8(q, e0, glb, gle, gdj);
                             nread += 8;
                         }
                         const uint32_t hm = __ballot_sync(kFull, hit) & gmask;
@@ -1422,6 +1528,9 @@ batch_kernel(TreeArgs a) {
             c_vis += t_size;
             const long long tz0 = clock64();
             for (uint32_t k = lane; k < nvis; k += 32) __stcg(&key[vis[k]], kInf);
+            if (a.hash_slots) {
+                for (uint32_t k = lane; k < a.hash_slots; k += 32) s_tab[k] = kSlotEmpty;
+            }
             cyc[6] += clock64() - tz0;
             __syncwarp();
         }
@@ -2402,8 +2511,19 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             uint32_t cap = opts.root_stage ? opts.root_stage : b.auto_stage;
             rcap = std::min<size_t>(rcap, std::max<uint32_t>(cap, 32));
         }
-        if (kWarpsPerBlock * (rcap * 8 + fixed) > smem_cap)
+        uint32_t hash_slots = 0;
+        if (use_batch && opts.root_probe == 2) {
+            // hash table: a power of two at least twice the longest root label
+            uint32_t t = 64;
+            const uint32_t tmax = opts.root_stage ? std::max<uint32_t>(opts.root_stage, 64) : 2048;
+            while (t < 2 * std::max<uint32_t>(max_list, 32) && 2 * t <= tmax) t *= 2;
+            hash_slots = t;
+            rcap = t;
+        }
+        if (kWarpsPerBlock * (rcap * 8 + fixed) > smem_cap) {
             rcap = (smem_cap / kWarpsPerBlock - fixed) / 8;
+            while (hash_slots > rcap) hash_slots /= 2;
+        }
         b.rcap = (uint32_t)rcap;
         const size_t smem = use_settle  ? kWarpsPerBlock * settle_smem_per_warp(b.rcap)
                             : use_batch ? kWarpsPerBlock * batch_smem_per_warp(b.rcap)
@@ -2444,6 +2564,11 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             ta.ws_front = b.ws_front;
             ta.scan_back = opts.scan_order == 1 ? 1 : 0;
             ta.chunk_sched = opts.prune_sched == 2 ? 1 : 0;
+            ta.hash_slots = hash_slots;
+            ta.wide = opts.prune_sched == 3 ? 1 : 0;
+            if (ta.wide) ta.chunk_sched = 1;
+            ta.hash_shift = 32;
+            for (uint32_t t = hash_slots; t > 1; t >>= 1) --ta.hash_shift;
             ta.smem_block = (uint32_t)smem;
             ta.r_big = r0;
             if (use_batch) {

@@ -134,7 +134,11 @@ def test_build_is_deterministic(P):
                {"use_graphs": 0}, {"use_graphs": 0, "mode": 1}, {"use_graphs": 1, "mode": 1, "tree_algo": 3},
                {"root_stage": 32}, {"root_stage": 32, "mode": 1}, {"root_stage": 36, "cta_roots": 5},
                {"root_stage": 4096}, {"prune_sched": 2}, {"prune_sched": 2, "root_stage": 32},
-               {"prune_sched": 2, "scan_order": 1}, {"prune_sched": 2, "mode": 1}, {"prune_sched": 1}):
+               {"prune_sched": 2, "scan_order": 1}, {"prune_sched": 2, "mode": 1}, {"prune_sched": 1},
+               {"root_probe": 2}, {"root_probe": 2, "prune_sched": 2}, {"root_probe": 2, "root_stage": 64},
+               {"root_probe": 2, "mode": 1, "cta_roots": 3}, {"root_probe": 2, "root_stage": 64, "prune_sched": 2},
+               {"prune_sched": 3}, {"prune_sched": 3, "root_probe": 2, "scan_order": 1},
+               {"prune_sched": 3, "root_probe": 2, "root_stage": 64, "mode": 1}):
         b = P.build(g, order, sf=0.2, **kw).export()
         for x, y in zip(a, b):
             assert np.array_equal(x, y), kw
