@@ -164,8 +164,9 @@ typedef struct chl_build_opts {
     int32_t tree_algo;    /* 0 or 2: batched settle (default), 1: binary
                              heap, 3: settle rounds over a logged frontier
                              with staged prune tests                      */
-    int32_t scan_order;   /* prune-test list order: 0 auto, 1 from the end,
-                             2 from the start                              */
+    int32_t scan_order;   /* prune-test list order: 0 auto (from the end on
+                             road-like graphs, from the start on heavy-
+                             tailed ones), 1 from the end, 2 from the start */
     int32_t cta_roots;    /* roots per superstep built by a whole block:
                              0 auto, -1 none, > 0 that many                */
     uint32_t root_limit;  /* > 0: build the trees of ranks < root_limit only
@@ -174,13 +175,15 @@ typedef struct chl_build_opts {
     uint32_t root_stage;  /* root-label entries staged in shared memory per
                              tree (batched settle), 0 = auto: the most that
                              keeps the register-limited occupancy           */
-    int32_t prune_sched;  /* batched settle prune tests: 0 auto, 1 a lane
-                             group per vertex, 2 (vertex, 32-entry chunk)
-                             items, 3 (vertex, 64-entry chunk) items        */
-    int32_t root_probe;   /* batched settle root-label lookups: 0 auto,
-                             1 sorted staging + binary search, 2 hash table
-                             in shared memory                               */
-    uint32_t reserved[1];
+    int32_t prune_sched;  /* batched settle prune tests: 0 auto (= 3), 1 a
+                             lane group per vertex, 2 (vertex, 32-entry
+                             chunk) items, 3 (vertex, 64-entry chunk) items */
+    int32_t root_probe;   /* batched settle root-label lookups: 0 auto
+                             (= 2), 1 sorted staging + binary search, 2 hash
+                             table in shared memory                         */
+    int32_t superstep_extend; /* batched settle: while a superstep's trees
+                             run, idle warps take up to this many times its
+                             nominal roots (0 auto = 4, 1 off)              */
 } chl_build_opts;
 
 /* Fill opts with the defaults (hybrid, sf 32, ps 1024, autotune on,

@@ -55,6 +55,8 @@ struct BuildCtl {
     unsigned int err;               // 1: distance overflow, 2: workspace bound
     unsigned long long max_ratio_num;  // (tree, labels) of the worst root
     unsigned long long max_ratio_den;
+    unsigned long long running;     // trees of the nominal root range in progress
+    unsigned long long close_at;    // first root refused after the extension closed
     unsigned long long cyc[8];      // per-phase SM cycles summed over warps (diagnostics)
     unsigned long long cnt[4];      // frontier entries scanned, rounds, settle calls, arcs relaxed
 };
@@ -70,6 +72,7 @@ struct TreeArgs {
     const uint64_t *l_off;          // committed labels, index lidx(v, side)
     const uint2 *l_ent;
     uint32_t r0, r_end;
+    uint32_t r_hard;                // batch kernel: roots past r_end taken while nominal trees run
     unsigned long long budget;
     int hub_bits;
     uint64_t *out_key;
@@ -584,6 +587,40 @@ struct RootHash {
     }
 };
 
+// Work-conserving supersteps.  A superstep's nominal roots are [r0, r_end);
+// while any nominal tree is still running, idle warps take further roots up
+// to r_hard instead of waiting (a superstep is as long as its largest tree,
+// which one warp builds).  The processed roots stay one contiguous range:
+// the warp that ends the last running nominal tree sets kClosed in the fetch
+// counter with one atomicOr, and every fetch returning a value with kClosed
+// set is refused; close_at records the first refused rank.  Any consecutive
+// root range per superstep gives the same labels: trees prune only against
+// the labels of earlier supersteps.
+constexpr unsigned long long kClosed = 1ull << 62;
+
+__device__ __forceinline__ uint32_t fetch_root(const TreeArgs &a, bool &nominal) {
+    nominal = false;
+    const unsigned long long used = *(volatile unsigned long long *)&a.ctl->nlab;
+    if (used >= a.budget) return kInf;
+    const unsigned long long t = atomicAdd(&a.ctl->next_root, 1ull);
+    if (t & kClosed) return kInf;
+    if (t < a.r_end) {
+        atomicAdd(&a.ctl->running, 1ull);
+        nominal = true;
+        return (uint32_t)t;
+    }
+    return t < a.r_hard ? (uint32_t)t : kInf;
+}
+
+__device__ __forceinline__ void finish_root(const TreeArgs &a, bool nominal) {
+    if (!nominal || a.r_hard <= a.r_end) return;
+    if (atomicAdd(&a.ctl->running, ~0ull) == 1ull &&
+        (*(volatile unsigned long long *)&a.ctl->next_root & ~kClosed) >= a.r_end) {
+        const unsigned long long old = atomicOr(&a.ctl->next_root, kClosed);
+        if (!(old & kClosed)) a.ctl->close_at = old;
+    }
+}
+
 // ------------------------------------------------- CTA-cooperative trees
 //
 // The largest trees of a superstep (its first roots: roots go in rank
@@ -991,6 +1028,7 @@ batch_kernel(TreeArgs a) {
 
     // ---- block-per-tree phase for the superstep's first (largest) roots
     uint32_t pending = kInf;
+    bool pending_nominal = false;
     if (a.r_big > a.r0) {
         CtaShared &sh = *(CtaShared *)smem;
         const size_t s0 = (size_t)blockIdx.x * kWarpsPerBlock;
@@ -1002,19 +1040,19 @@ batch_kernel(TreeArgs a) {
         while (true) {
             __syncthreads();
             if (threadIdx.x == 0) {
-                uint32_t rr = kInf;
-                unsigned long long used = *(volatile unsigned long long *)&a.ctl->nlab;
-                if (used < a.budget) {
-                    unsigned long long t = atomicAdd(&a.ctl->next_root, 1ull);
-                    if (t < a.r_end) rr = (uint32_t)t;
-                }
-                sh.root = rr;
+                bool nom = false;
+                sh.root = fetch_root(a, nom);
+                sh.pad[0] = nom ? 1u : 0u;
             }
             __syncthreads();
             const uint32_t rc = sh.root;
+            const bool rc_nominal = sh.pad[0] != 0;
             if (rc == kInf) break;
             if (rc >= a.r_big) {
-                if (wib == 0) pending = rc;   // warp 0 builds this one alone
+                if (wib == 0) {
+                    pending = rc;   // warp 0 builds this one alone
+                    pending_nominal = rc_nominal;
+                }
                 break;
             }
             uint32_t ts = 0, tl = 0;
@@ -1023,6 +1061,7 @@ batch_kernel(TreeArgs a) {
             if (threadIdx.x == 0) {
                 a.tree_size[rc - a.r0] = ts;
                 a.tree_labels[rc - a.r0] = tl;
+                finish_root(a, rc_nominal);
             }
         }
         __syncthreads();   // the block leaves the shared layout before warps reuse it
@@ -1034,18 +1073,15 @@ batch_kernel(TreeArgs a) {
     }
     while (true) {
         uint32_t r = kInf;
+        bool r_nominal = false;
         if (pending != kInf) {
             r = pending;
+            r_nominal = pending_nominal;
             pending = kInf;
         } else {
-            if (lane == 0) {
-                unsigned long long used = *(volatile unsigned long long *)&a.ctl->nlab;
-                if (used < a.budget) {
-                    unsigned long long t = atomicAdd(&a.ctl->next_root, 1ull);
-                    if (t < a.r_end) r = (uint32_t)t;
-                }
-            }
+            if (lane == 0) r = fetch_root(a, r_nominal);
             r = __shfl_sync(kFull, r, 0);
+            r_nominal = __shfl_sync(kFull, r_nominal ? 1u : 0u, 0) != 0;
         }
         if (r == kInf) break;
         uint32_t t_size = 0, t_lab = 0;
@@ -1537,6 +1573,7 @@ batch_kernel(TreeArgs a) {
         if (lane == 0) {
             a.tree_size[r - a.r0] = t_size;
             a.tree_labels[r - a.r0] = t_lab;
+            finish_root(a, r_nominal);
         }
     }
     if (lane == 0) {
@@ -2454,6 +2491,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     // half of the committed prefix.
     uint32_t auto_first;
     double auto_growth;
+    bool heavy_tail = false;
     {
         uint64_t arcs_out = g->off[1][n];
         uint64_t maxdeg = 0;
@@ -2462,7 +2500,15 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         const bool heavy = maxdeg > 32.0 * std::max(1.0, avgdeg);
         auto_first = heavy ? 1024u : std::max<uint32_t>(64u, b.warps);
         auto_growth = heavy ? 2.0 : 0.5;
+        heavy_tail = heavy;
     }
+    // prune-test defaults of the batched settle (measured on RMAT scale 18
+    // and 512/1024-square grids): 64-entry items, root label hashed in
+    // shared memory, lists read from the end (recent, local hubs first) on
+    // road-like graphs and from the start on heavy-tailed ones
+    const int prune_sched = opts.prune_sched ? opts.prune_sched : 3;
+    const int root_probe = opts.root_probe ? opts.root_probe : 2;
+    const int scan_back = opts.scan_order ? (opts.scan_order == 1 ? 1 : 0) : (heavy_tail ? 0 : 1);
 
     // superstep loop
     const double sf = opts.sf > 0 ? opts.sf : 32.0;
@@ -2512,7 +2558,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             rcap = std::min<size_t>(rcap, std::max<uint32_t>(cap, 32));
         }
         uint32_t hash_slots = 0;
-        if (use_batch && opts.root_probe == 2) {
+        if (use_batch && root_probe == 2) {
             // hash table: a power of two at least twice the longest root label
             uint32_t t = 64;
             const uint32_t tmax = opts.root_stage ? std::max<uint32_t>(opts.root_stage, 64) : 2048;
@@ -2546,6 +2592,13 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             ta.l_ent = b.ent_a;
             ta.r0 = r0;
             ta.r_end = r_end;
+            // work-conserving extension (batch kernel): up to ext x the
+            // nominal size while nominal trees run; none on a rerun
+            uint32_t ext = opts.superstep_extend == 0 ? (heavy_tail ? 1u : 4u)
+                                                      : (uint32_t)std::max(1, opts.superstep_extend);
+            if (!use_batch || rerun) ext = 1;
+            ta.r_hard = (uint32_t)std::min<uint64_t>(n, (uint64_t)r0 + (uint64_t)ext * (r_end - r0));
+            if (opts.root_limit) ta.r_hard = std::min<uint32_t>(ta.r_hard, std::max(opts.root_limit, r_end));
             ta.budget = rerun ? ~0ull : budget;
             ta.hub_bits = b.hub_bits;
             ta.out_key = b.nk0;
@@ -2562,10 +2615,10 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             const int blocks = (int)(b.warps / kWarpsPerBlock);
             for (int s2 = 0; s2 < 2; ++s2) ta.win[s2] = b.dg->win[s2];
             ta.ws_front = b.ws_front;
-            ta.scan_back = opts.scan_order == 1 ? 1 : 0;
-            ta.chunk_sched = opts.prune_sched == 2 ? 1 : 0;
+            ta.scan_back = scan_back;
+            ta.chunk_sched = prune_sched == 2 ? 1 : 0;
             ta.hash_slots = hash_slots;
-            ta.wide = opts.prune_sched == 3 ? 1 : 0;
+            ta.wide = prune_sched == 3 ? 1 : 0;
             if (ta.wide) ta.chunk_sched = 1;
             ta.hash_shift = 32;
             for (uint32_t t = hash_slots; t > 1; t >>= 1) --ta.hash_shift;
@@ -2607,7 +2660,8 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             CHL_CUDA(cudaEventElapsedTime(&ms, ev_a, ev_b));
             tree_ms += ms;
             step_tree_ms = ms;
-            uint32_t r1 = (uint32_t)std::min<unsigned long long>(hc.next_root, r_end);
+            const unsigned long long fetched = (hc.next_root & kClosed) ? hc.close_at : hc.next_root;
+            uint32_t r1 = (uint32_t)std::min<unsigned long long>(fetched, std::max(ta.r_hard, r_end));
             if (hc.err) {
                 set_error(hc.err == 1 ? "a shortest-path distance reaches INT_MAX (the reference asserts dd < infty)"
                                       : "tree workspace bound exceeded");
