@@ -183,7 +183,11 @@ typedef struct chl_build_opts {
                              table in shared memory                         */
     int32_t superstep_extend; /* batched settle: while a superstep's trees
                              run, idle warps take up to this many times its
-                             nominal roots (0 auto = 4, 1 off)              */
+                             nominal roots (0 auto: 4 on road-like graphs,
+                             off on heavy-tailed ones; 1 off)               */
+    int32_t settle_rule;  /* batched settle finality test: 0 auto (= 1),
+                             1 IN criterion, 2 IN and OUT criteria          */
+    uint32_t reserved[4];
 } chl_build_opts;
 
 /* Fill opts with the defaults (hybrid, sf 32, ps 1024, autotune on,

@@ -87,6 +87,8 @@ struct TreeArgs {
     BuildCtl *ctl;
     uint32_t rcap;                  // root label entries staged in smem
     const uint32_t *win[2];         // [f]: shortest arc into v along direction f
+    const uint32_t *wout[2];        // [f]: shortest arc out of v along direction f
+    int out_crit;                   // batch kernel: OUT criterion on
     uint32_t *ws_front;             // per warp slot: queued (unsettled) vertices
     int scan_back;                  // prune tests read label lists from the end
     int chunk_sched;                // batch kernel: prune tests as (vertex, chunk) items
@@ -598,6 +600,11 @@ struct RootHash {
 // the labels of earlier supersteps.
 constexpr unsigned long long kClosed = 1ull << 62;
 
+__device__ __forceinline__ uint32_t sat_add(uint32_t x, uint32_t y) {
+    const uint32_t z = x + y;
+    return z < x ? 0xFFFFFFFFu : z;
+}
+
 __device__ __forceinline__ uint32_t fetch_root(const TreeArgs &a, bool &nominal) {
     nominal = false;
     const unsigned long long used = *(volatile unsigned long long *)&a.ctl->nlab;
@@ -1093,6 +1100,7 @@ batch_kernel(TreeArgs a) {
             const uint2 *garc = a.g_arc[f];
             const uint32_t *ghead = a.g_head[f];
             const uint32_t *win = a.win[f];
+            const uint32_t *wout = a.wout[f];
             const uint32_t ridx = lidx(v, f, a.sides);
             const uint64_t rb = a.l_off[ridx], re = a.l_off[ridx + 1];
             const uint32_t R = (uint32_t)(re - rb);
@@ -1207,7 +1215,16 @@ batch_kernel(TreeArgs a) {
             // a queued vertex lowers dnext, so dnext is the exact minimum of
             // the queue after the round.
             uint32_t dnext = kInf;
+            // OUT criterion (Crauser et al.): v is also final when
+            // d(v) < min over queued u of (d(u) + shortest arc out of u) --
+            // no queued vertex can reach it with d <= d(v), so its distance
+            // and via flag are final.  omin is that minimum over the queue
+            // at the start of the round; it holds only until the first
+            // settle of the round changes the queue (out_ok).
+            uint32_t onext = kInf, omin = 0;
+            bool out_ok = false;
             auto settle = [&]() {
+                out_ok = false;
                 long long tc0 = clock64();
                 if (kPhaseTiming) dcnt[2]++;
                 t_size += nb;
@@ -1258,6 +1275,10 @@ batch_kernel(TreeArgs a) {
                     }
                     __syncwarp();
                     const uint32_t nitems = ntest * maxnch;
+                    // i / ntest as a multiply by ceil(2^32 / ntest): exact for
+                    // i < ntest * maxnch when maxnch * ntest^2 < 2^32
+                    const uint64_t inv = ((1ull << 32) + ntest - 1) / max(ntest, 1u);
+                    const bool mul_div = (uint64_t)maxnch * ntest * ntest < (1ull << 32);
                     uint32_t cursor = 0, nread = 0;
                     while (true) {
                         // the next (up to) 8 live items, in item order
@@ -1267,7 +1288,7 @@ batch_kernel(TreeArgs a) {
                             bool live = false;
                             uint32_t item = 0;
                             if (i < nitems) {
-                                const uint32_t c = i / ntest;
+                                const uint32_t c = mul_div ? (uint32_t)(((uint64_t)i * inv) >> 32) : i / ntest;
                                 const uint32_t j = s_tl[i - c * ntest];
                                 live = s_bp[j] == 0 && c < s_nch[j];
                                 item = (c << 8) | j;
@@ -1426,7 +1447,12 @@ batch_kernel(TreeArgs a) {
                 }
                 long long tc3 = clock64();
                 cyc[3] += tc3 - tc2;
-                uint32_t total = 0;
+                // arcs of the batch flattened over the lanes: the vertices
+                // with arcs are compacted (s_tl[k] = batch index, s_bx[k] =
+                // first flattened arc), so the owner of arc t0 + lane is the
+                // window's first owner plus the vertex starts inside the
+                // window below the lane (one OR-reduction, no search)
+                uint32_t total = 0, ncomp = 0;
                 for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
                     const uint32_t j = j0 + lane;
                     uint32_t deg = 0;
@@ -1442,24 +1468,39 @@ batch_kernel(TreeArgs a) {
                         const uint32_t y = __shfl_up_sync(kFull, incl, o);
                         if (lane >= (uint32_t)o) incl += y;
                     }
-                    if (j < nb) s_bx[j] = total + incl - deg;
+                    const uint32_t nem = __ballot_sync(kFull, deg > 0);
+                    if (deg > 0) {
+                        const uint32_t k = ncomp + __popc(nem & lanemask_lt());
+                        s_tl[k] = j;
+                        s_bx[k] = total + incl - deg;
+                    }
                     total += __shfl_sync(kFull, incl, 31);
+                    ncomp += __popc(nem);
                 }
-                if (lane == 0) s_bx[nb] = total;
+                if (lane == 0) s_bx[ncomp] = total;
                 __syncwarp();
                 c_arcs += total;
+                uint32_t cur = 0;   // compacted owner of arc t0
                 for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+                    if (cur + 1 < ncomp && s_bx[cur + 1] <= t0) ++cur;
+                    uint32_t bit = 0;
+                    {
+                        const uint32_t kk = cur + 1 + lane;
+                        if (kk < ncomp) {
+                            const uint32_t st = s_bx[kk];
+                            if (st < t0 + 32) bit = 1u << (st - t0);
+                        }
+                    }
+                    const uint32_t starts = __reduce_or_sync(kFull, bit);
+                    const uint32_t upto = lane == 31 ? kFull : ((2u << lane) - 1u);
+                    const uint32_t own = cur + (uint32_t)__popc(starts & upto);
+                    cur += (uint32_t)__popc(starts);
                     const uint32_t t = t0 + lane;
                     bool upd = false;
                     uint32_t w = 0, nk = 0, old = kInf;
                     if (t < total) {
-                        uint32_t lo = 0, hi = nb;
-                        while (hi - lo > 1) {
-                            const uint32_t mid = (lo + hi) >> 1;
-                            if (s_bx[mid] <= t) lo = mid;
-                            else hi = mid;
-                        }
-                        const uint64_t e = s_ba[lo] + (t - s_bx[lo]);
+                        const uint32_t lo = s_tl[own];
+                        const uint64_t e = s_ba[lo] + (t - s_bx[own]);
                         uint32_t len;
                         if (UNIT) {
                             w = ghead[e];
@@ -1477,7 +1518,11 @@ batch_kernel(TreeArgs a) {
                             nk = (uint32_t)dd64 * 2u + nv;
                             old = atomicMin(&key[w], nk);
                             upd = nk < old;
-                            if (upd) dnext = min(dnext, nk >> 1);
+                            if (upd) {
+                                dnext = min(dnext, nk >> 1);
+                                if (a.out_crit)
+                                    onext = min(onext, sat_add(nk >> 1, wout[w]));
+                            }
                         } else {
                             a.ctl->err = 1;   // the reference asserts dd < infty
                         }
@@ -1516,6 +1561,8 @@ batch_kernel(TreeArgs a) {
                 const uint32_t nf0 = nf;
                 uint32_t keep = 0;
                 dnext = kInf;
+                onext = kInf;
+                out_ok = a.out_crit != 0;
                 if (kPhaseTiming) {
                     dcnt[0] += nf0;
                     dcnt[1]++;
@@ -1528,7 +1575,8 @@ batch_kernel(TreeArgs a) {
                     const bool valid = i < nf0;
                     const uint32_t x = valid ? front[i] : 0u;
                     const uint32_t kx = valid ? __ldcg(&key[x]) : kInf;
-                    const bool take = valid && (uint64_t)(kx >> 1) < (uint64_t)dmin + win[x];
+                    const bool take = valid && ((uint64_t)(kx >> 1) < (uint64_t)dmin + win[x] ||
+                                                (out_ok && (kx >> 1) < omin));
                     const uint32_t tm = __ballot_sync(kFull, take);
                     if (take) {
                         const uint32_t at = nb + __popc(tm & lanemask_lt());
@@ -1541,6 +1589,8 @@ batch_kernel(TreeArgs a) {
                     if (kp) {
                         front[keep + __popc(km & lanemask_lt())] = x;
                         dnext = min(dnext, kx >> 1);
+                        if (a.out_crit)
+                            onext = min(onext, sat_add(kx >> 1, wout[x]));
                     }
                     keep += __popc(km);
                     __syncwarp();
@@ -1560,6 +1610,7 @@ batch_kernel(TreeArgs a) {
                 }
                 nf = keep + app;
                 dmin = __reduce_min_sync(kFull, dnext);
+                omin = __reduce_min_sync(kFull, onext);
             }
             c_vis += t_size;
             const long long tz0 = clock64();
@@ -2178,6 +2229,7 @@ struct DevGraph {
     uint32_t *head[2] = {nullptr, nullptr};
     uint32_t *win[2] = {nullptr, nullptr};   // shortest arc into v, per direction
     uint16_t *win16[2] = {nullptr, nullptr};
+    uint32_t *wout[2] = {nullptr, nullptr};  // shortest arc out of v, per direction
     void release() {
         // side 1 may alias side 0 (symmetric graphs): free each buffer once
         if (off[1] != off[0]) cudaFree(off[1]);
@@ -2185,6 +2237,8 @@ struct DevGraph {
         if (head[1] != head[0]) cudaFree(head[1]);
         if (win[1] != win[0]) cudaFree(win[1]);
         if (win16[1] != win16[0]) cudaFree(win16[1]);
+        if (wout[1] != wout[0]) cudaFree(wout[1]);
+        cudaFree(wout[0]);
         cudaFree(win16[0]);
         cudaFree(off[0]);
         cudaFree(arc[0]);
@@ -2196,6 +2250,7 @@ struct DevGraph {
             head[s] = nullptr;
             win[s] = nullptr;
             win16[s] = nullptr;
+            wout[s] = nullptr;
         }
     }
 };
@@ -2239,6 +2294,13 @@ int upload_graph(const chl_graph *g, DevGraph &dg, cudaStream_t st) {
         rc = dalloc(&dg.win16[s], (size_t)g->n);
         if (rc) return rc;
         CHL_CUDA(cudaMemcpy(dg.win16[s], w16.data(), (size_t)g->n * 2, cudaMemcpyHostToDevice));
+        std::vector<uint32_t> wo(g->n, 0x7FFFFFFFu);
+        for (uint32_t v = 0; v < g->n; ++v)
+            for (uint64_t i = g->off[src][v]; i < g->off[src][v + 1]; ++i)
+                wo[v] = std::min<uint32_t>(wo[v], (uint32_t)g->len[src][i]);
+        rc = dalloc(&dg.wout[s], (size_t)g->n);
+        if (rc) return rc;
+        CHL_CUDA(cudaMemcpy(dg.wout[s], wo.data(), (size_t)g->n * 4, cudaMemcpyHostToDevice));
     }
     if (nsides == 1) {
         dg.off[1] = dg.off[0];
@@ -2246,6 +2308,7 @@ int upload_graph(const chl_graph *g, DevGraph &dg, cudaStream_t st) {
         dg.head[1] = dg.head[0];
         dg.win[1] = dg.win[0];
         dg.win16[1] = dg.win16[0];
+        dg.wout[1] = dg.wout[0];
     }
     return CHL_OK;
 }
@@ -2509,6 +2572,9 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     const int prune_sched = opts.prune_sched ? opts.prune_sched : 3;
     const int root_probe = opts.root_probe ? opts.root_probe : 2;
     const int scan_back = opts.scan_order ? (opts.scan_order == 1 ? 1 : 0) : (heavy_tail ? 0 : 1);
+    // OUT criterion: measured slower on the 512/1024-square grids and RMAT
+    // scale 18 (the extra loads outweigh the larger batches), so opt-in
+    const int out_crit = opts.settle_rule == 2 ? 1 : 0;
 
     // superstep loop
     const double sf = opts.sf > 0 ? opts.sf : 32.0;
@@ -2614,6 +2680,8 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             ta.rcap = b.rcap;
             const int blocks = (int)(b.warps / kWarpsPerBlock);
             for (int s2 = 0; s2 < 2; ++s2) ta.win[s2] = b.dg->win[s2];
+            for (int s2 = 0; s2 < 2; ++s2) ta.wout[s2] = b.dg->wout[s2];
+            ta.out_crit = out_crit;
             ta.ws_front = b.ws_front;
             ta.scan_back = scan_back;
             ta.chunk_sched = prune_sched == 2 ? 1 : 0;
