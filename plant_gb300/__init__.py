@@ -588,6 +588,12 @@ class RankNet:
         net.set_params(p)
         return net
 
+    @classmethod
+    def pretrained(cls) -> "RankNet":
+        """The 3-layer network trained on hub frequencies of 256 small GPU
+        labelings (``bench.py --rank``), shipped with the package."""
+        return cls.load(os.path.join(_HERE, "ranknet_l3.npy"), layers=3)
+
     def order(self, g: Graph, seed: int = 1) -> np.ndarray:
         o = np.zeros(g.get_n(), np.uint32)
         _check(lib().chl_gnn_order(self._h, g._h, seed, _ptr(o, _U32P)), "gnn order")

@@ -1155,6 +1155,11 @@ batch_kernel(TreeArgs a) {
                             v[t] = s_tab[sl[t]];
                         }
                     }
+                    // resolve the probes in rounds: every pending entry
+                    // checks its slot and loads the next one, so the probes
+                    // of one round are independent; long chains (rare at
+                    // load <= 1/2) finish one by one
+                    uint32_t pend = 0;
 #pragma unroll
                     for (int t = 0; t < NE; ++t) {
                         const uint64_t e = e0 + t;
@@ -1162,17 +1167,44 @@ batch_kernel(TreeArgs a) {
                         const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
                         if (e < glb || e >= gle) continue;
                         if (rhash.Th && hh <= rhash.hlast) {
-                            uint64_t w = v[t];
-                            uint32_t z = sl[t];
-                            while (w != kSlotEmpty && (uint32_t)(w >> 32) != hh) {
-                                z = (z + 1) & rhash.mask;
-                                w = s_tab[z];
-                            }
-                            if (w != kSlotEmpty && (uint32_t)w + dd <= gdj) hit = true;
+                            pend |= 1u << t;
                         } else if (rhash.Th < R) {
                             uint32_t dr;
                             if (rhash.find_tail(hh, dr) && dr + dd <= gdj) hit = true;
                         }
+                    }
+#pragma unroll
+                    for (int round = 0; round < 3; ++round) {
+                        if (!pend) break;
+#pragma unroll
+                        for (int t = 0; t < NE; ++t) {
+                            if (!(pend >> t & 1u)) continue;
+                            const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
+                            const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
+                            const uint64_t w = v[t];
+                            if (w == kSlotEmpty) {
+                                pend &= ~(1u << t);
+                            } else if ((uint32_t)(w >> 32) == hh) {
+                                if ((uint32_t)w + dd <= gdj) hit = true;
+                                pend &= ~(1u << t);
+                            } else {
+                                sl[t] = (sl[t] + 1) & rhash.mask;
+                                v[t] = s_tab[sl[t]];
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int t = 0; t < NE; ++t) {
+                        if (!(pend >> t & 1u)) continue;
+                        const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
+                        const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
+                        uint64_t w = v[t];
+                        uint32_t z = sl[t];
+                        while (w != kSlotEmpty && (uint32_t)(w >> 32) != hh) {
+                            z = (z + 1) & rhash.mask;
+                            w = s_tab[z];
+                        }
+                        if (w != kSlotEmpty && (uint32_t)w + dd <= gdj) hit = true;
                     }
                     return hit;
                 }
@@ -1481,69 +1513,89 @@ batch_kernel(TreeArgs a) {
                 __syncwarp();
                 c_arcs += total;
                 uint32_t cur = 0;   // compacted owner of arc t0
-                for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+                // owner (compacted index) of arc t0 + lane
+                auto owner = [&](uint32_t t0) -> uint32_t {
                     if (cur + 1 < ncomp && s_bx[cur + 1] <= t0) ++cur;
                     uint32_t bit = 0;
-                    {
-                        const uint32_t kk = cur + 1 + lane;
-                        if (kk < ncomp) {
-                            const uint32_t st = s_bx[kk];
-                            if (st < t0 + 32) bit = 1u << (st - t0);
-                        }
+                    const uint32_t kk = cur + 1 + lane;
+                    if (kk < ncomp) {
+                        const uint32_t st = s_bx[kk];
+                        if (st < t0 + 32) bit = 1u << (st - t0);
                     }
                     const uint32_t starts = __reduce_or_sync(kFull, bit);
                     const uint32_t upto = lane == 31 ? kFull : ((2u << lane) - 1u);
                     const uint32_t own = cur + (uint32_t)__popc(starts & upto);
                     cur += (uint32_t)__popc(starts);
-                    const uint32_t t = t0 + lane;
-                    bool upd = false;
-                    uint32_t w = 0, nk = 0, old = kInf;
-                    if (t < total) {
-                        const uint32_t lo = s_tl[own];
-                        const uint64_t e = s_ba[lo] + (t - s_bx[own]);
-                        uint32_t len;
-                        if (UNIT) {
-                            w = ghead[e];
-                            len = 1;
-                        } else {
-                            const uint2 hl = garc[e];
-                            w = hl.x;
-                            len = hl.y;
+                    return own;
+                };
+                // two 32-arc chunks per step: arc loads, rank loads and
+                // atomics of both chunks are issued together
+                for (uint32_t t0 = 0; t0 < total; t0 += 64) {
+                    uint32_t w[2] = {0, 0}, nk[2] = {0, 0}, old[2] = {kInf, kInf}, kxs[2] = {0, 0};
+                    uint32_t len[2] = {0, 0};
+                    bool act[2] = {false, false}, upd[2] = {false, false};
+#pragma unroll
+                    for (int c = 0; c < 2; ++c) {
+                        const uint32_t tc = t0 + 32u * c;
+                        const uint32_t own = tc < total ? owner(tc) : 0u;
+                        const uint32_t t = tc + lane;
+                        if (t < total) {
+                            const uint32_t lo = s_tl[own];
+                            const uint64_t e = s_ba[lo] + (t - s_bx[own]);
+                            if (UNIT) {
+                                w[c] = ghead[e];
+                                len[c] = 1;
+                            } else {
+                                const uint2 hl = garc[e];
+                                w[c] = hl.x;
+                                len[c] = hl.y;
+                            }
+                            kxs[c] = s_bk[lo];
+                            act[c] = true;
                         }
-                        const uint32_t kx = s_bk[lo];
-                        const uint64_t dd64 = (uint64_t)(kx >> 1) + len;
+                    }
+                    uint32_t nv[2] = {1u, 1u};
+                    if (PLANT) {
+#pragma unroll
+                        for (int c = 0; c < 2; ++c)
+                            if (act[c]) nv[c] = ((kxs[c] & 1u) && a.rank[w[c]] >= r) ? 1u : 0u;
+                    }
+#pragma unroll
+                    for (int c = 0; c < 2; ++c) {
+                        if (!act[c]) continue;
+                        const uint64_t dd64 = (uint64_t)(kxs[c] >> 1) + len[c];
                         if (dd64 < 0x7FFFFFFFull) {
-                            uint32_t nv = 1u;
-                            if (PLANT) nv = ((kx & 1u) && a.rank[w] >= r) ? 1u : 0u;
-                            nk = (uint32_t)dd64 * 2u + nv;
-                            old = atomicMin(&key[w], nk);
-                            upd = nk < old;
-                            if (upd) {
-                                dnext = min(dnext, nk >> 1);
-                                if (a.out_crit)
-                                    onext = min(onext, sat_add(nk >> 1, wout[w]));
+                            nk[c] = (uint32_t)dd64 * 2u + nv[c];
+                            old[c] = atomicMin(&key[w[c]], nk[c]);
+                            upd[c] = nk[c] < old[c];
+                            if (upd[c]) {
+                                dnext = min(dnext, nk[c] >> 1);
+                                if (a.out_crit) onext = min(onext, sat_add(nk[c] >> 1, wout[w[c]]));
                             }
                         } else {
                             a.ctl->err = 1;   // the reference asserts dd < infty
                         }
                     }
-                    const bool fresh = upd && old == kInf;
-                    const uint32_t fm = __ballot_sync(kFull, fresh);
-                    if (fresh) {
-                        const uint32_t o = __popc(fm & lanemask_lt());
-                        if (nf + o < a.n && nvis + o < a.n) {
-                            front[nf + o] = w;
-                            vis[nvis + o] = w;
-                        } else {
-                            a.ctl->err = 2;
+#pragma unroll
+                    for (int c = 0; c < 2; ++c) {
+                        const bool fresh = upd[c] && old[c] == kInf;
+                        const uint32_t fm = __ballot_sync(kFull, fresh);
+                        if (fresh) {
+                            const uint32_t o = __popc(fm & lanemask_lt());
+                            if (nf + o < a.n && nvis + o < a.n) {
+                                front[nf + o] = w[c];
+                                vis[nvis + o] = w[c];
+                            } else {
+                                a.ctl->err = 2;
+                            }
                         }
-                    }
-                    nf = min(nf + __popc(fm), a.n);
-                    nvis = min(nvis + __popc(fm), a.n);
-                    if (PLANT) {
-                        int dq = 0;
-                        if (upd) dq = (int)(nk & 1u) - (old == kInf ? 0 : (int)(old & 1u));
-                        ql += __reduce_add_sync(kFull, dq);
+                        nf = min(nf + __popc(fm), a.n);
+                        nvis = min(nvis + __popc(fm), a.n);
+                        if (PLANT) {
+                            int dq = 0;
+                            if (upd[c]) dq = (int)(nk[c] & 1u) - (old[c] == kInf ? 0 : (int)(old[c] & 1u));
+                            ql += __reduce_add_sync(kFull, dq);
+                        }
                     }
                 }
                 __syncwarp();
@@ -1567,15 +1619,11 @@ batch_kernel(TreeArgs a) {
                     dcnt[0] += nf0;
                     dcnt[1]++;
                 }
-                for (uint32_t b0 = 0; b0 < nf0 && !stop; b0 += 32) {
-                    if (nb > (uint32_t)kBatch - 32) settle();
-                    if (stop) break;
-                    const long long ts0 = clock64();
-                    const uint32_t i = b0 + lane;
-                    const bool valid = i < nf0;
-                    const uint32_t x = valid ? front[i] : 0u;
-                    const uint32_t kx = valid ? __ldcg(&key[x]) : kInf;
-                    const bool take = valid && ((uint64_t)(kx >> 1) < (uint64_t)dmin + win[x] ||
+                // two 32-entry chunks per step: their loads are issued
+                // together (both chunks are read before either is
+                // compacted, and compaction only moves entries left)
+                auto classify = [&](bool valid, uint32_t x, uint32_t kx, uint32_t wx) {
+                    const bool take = valid && ((uint64_t)(kx >> 1) < (uint64_t)dmin + wx ||
                                                 (out_ok && (kx >> 1) < omin));
                     const uint32_t tm = __ballot_sync(kFull, take);
                     if (take) {
@@ -1589,10 +1637,25 @@ batch_kernel(TreeArgs a) {
                     if (kp) {
                         front[keep + __popc(km & lanemask_lt())] = x;
                         dnext = min(dnext, kx >> 1);
-                        if (a.out_crit)
-                            onext = min(onext, sat_add(kx >> 1, wout[x]));
+                        if (a.out_crit) onext = min(onext, sat_add(kx >> 1, wout[x]));
                     }
                     keep += __popc(km);
+                };
+                for (uint32_t b0 = 0; b0 < nf0 && !stop; b0 += 64) {
+                    if (nb > (uint32_t)kBatch - 64) settle();
+                    if (stop) break;
+                    const long long ts0 = clock64();
+                    const uint32_t i0 = b0 + lane, i1 = b0 + 32 + lane;
+                    const bool v0 = i0 < nf0, v1 = i1 < nf0;
+                    const uint32_t x0 = v0 ? front[i0] : 0u;
+                    const uint32_t x1 = v1 ? front[i1] : 0u;
+                    const uint32_t k0 = v0 ? __ldcg(&key[x0]) : kInf;
+                    const uint32_t k1 = v1 ? __ldcg(&key[x1]) : kInf;
+                    const uint32_t w0 = v0 ? win[x0] : 0u;
+                    const uint32_t w1 = v1 ? win[x1] : 0u;
+                    __syncwarp();
+                    classify(v0, x0, k0, w0);
+                    classify(v1, x1, k1, w1);
                     __syncwarp();
                     cyc[0] += clock64() - ts0;
                 }

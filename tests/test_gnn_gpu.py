@@ -195,3 +195,15 @@ def test_selection_uses_learned_only_when_no_worse(P):
     pairs = P.generate_query(4096, g.get_n(), seed=7).reshape(-1, 2)
     Lp = P.build(g, deg)
     assert np.array_equal(P.query(c2.labels, pairs), P.query(Lp, pairs))
+
+
+def test_pretrained_network_orders_exactly(P, O):
+    net = P.RankNet.pretrained()
+    g = P.Graph.grid(40, 40, highways=8, hw_steps=8, seed=31)
+    order = net.order(g)
+    n = g.get_n()
+    assert np.array_equal(np.sort(order), np.arange(n, dtype=np.uint32))
+    off, head, ln = g.csr(True)
+    ref, _ = O.gll(O.OGraph.from_csr(n, off, head, ln), order)
+    for a, b in zip(P.build(g, order).export(), ref.export(n)):
+        assert np.array_equal(np.asarray(a), np.asarray(b))

@@ -86,3 +86,11 @@ def test_features_definition():
     assert np.all(raw[:, 2] == 0)
     z = R.standardise(raw)
     assert np.allclose(z[:, 0].mean(), 0, atol=1e-6) and np.allclose(z[:, 2], 0)
+
+
+def test_shipped_parameters_have_the_layout():
+    import os
+    p = np.load(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                             "plant_gb300", "ranknet_l3.npy"))
+    assert p.dtype == np.float32 and p.size == R.param_count(3)
+    assert np.all(np.isfinite(p))
