@@ -177,7 +177,8 @@ typedef struct chl_build_opts {
                              keeps the register-limited occupancy           */
     int32_t prune_sched;  /* batched settle prune tests: 0 auto (= 3), 1 a
                              lane group per vertex, 2 (vertex, 32-entry
-                             chunk) items, 3 (vertex, 64-entry chunk) items */
+                             chunk) items, 3 (vertex, 64-entry chunk) items,
+                             4 (vertex, 16-entry chunk) items, one per lane */
     int32_t root_probe;   /* batched settle root-label lookups: 0 auto
                              (= 2), 1 sorted staging + binary search, 2 hash
                              table in shared memory                         */

@@ -43,6 +43,16 @@ constexpr int kStage = 32;          // label staging entries per warp
 #define CHL_PHASE_TIMING 0              // 1: per-phase clock64 counters (diagnostic builds)
 #endif
 constexpr bool kPhaseTiming = CHL_PHASE_TIMING != 0;
+// batched settle code-shape switches (for A/B measurements)
+#ifndef CHL_PROBE_ROUNDS
+#define CHL_PROBE_ROUNDS 0   // hash probe rounds resolved in lock step (measured slower)
+#endif
+#ifndef CHL_SCAN_CHUNKS
+#define CHL_SCAN_CHUNKS 2    // 32-entry frontier chunks per scan step
+#endif
+#ifndef CHL_RELAX_CHUNKS
+#define CHL_RELAX_CHUNKS 2   // 32-arc chunks per relax step
+#endif
 
 struct BuildCtl {
     unsigned long long next_root;   // root fetch counter (absolute rank)
@@ -89,11 +99,14 @@ struct TreeArgs {
     const uint32_t *win[2];         // [f]: shortest arc into v along direction f
     const uint32_t *wout[2];        // [f]: shortest arc out of v along direction f
     int out_crit;                   // batch kernel: OUT criterion on
+    const uint4 *g_farc[2];         // batch kernel: (head, length, rank[head]) per arc
+    const uint2 *g_fhead[2];        // batch kernel: (head, rank[head]) per arc, unit lengths
     uint32_t *ws_front;             // per warp slot: queued (unsettled) vertices
     int scan_back;                  // prune tests read label lists from the end
     int chunk_sched;                // batch kernel: prune tests as (vertex, chunk) items
     uint32_t hash_slots;            // batch kernel: root hash table slots (0: sorted staging)
     int wide;                       // chunk schedule: 64-entry items instead of 32
+    int lane_items;                 // chunk schedule: one 16-entry item per lane
     uint32_t hash_shift;            // 32 - log2(hash_slots)
     uint32_t r_big;                 // roots below r_big: one block per tree
     uint32_t smem_block;            // dynamic shared memory of a block (bytes)
@@ -473,7 +486,7 @@ tree_kernel(TreeArgs a) {
 constexpr int kBatch = 128;
 
 __host__ __device__ constexpr size_t batch_smem_per_warp(uint32_t rcap) {
-    return ((size_t)8 * kBatch + (size_t)4 * (2 * rcap + 7 * kBatch + 1 + 8) + 15) & ~(size_t)15;
+    return ((size_t)8 * kBatch + (size_t)4 * (2 * rcap + 7 * kBatch + 1 + 32) + 15) & ~(size_t)15;
 }
 
 __device__ __forceinline__ uint32_t bsearch_hub(const uint32_t *rh, int rstride, uint32_t R, uint32_t h) {
@@ -1097,10 +1110,10 @@ batch_kernel(TreeArgs a) {
             const long long tr0 = clock64();
             const int f = (a.sides == 1) ? 1 : sd;
             const uint64_t *goff = a.g_off[f];
-            const uint2 *garc = a.g_arc[f];
-            const uint32_t *ghead = a.g_head[f];
             const uint32_t *win = a.win[f];
             const uint32_t *wout = a.wout[f];
+            const uint4 *farc = a.g_farc[f];
+            const uint2 *fhead = a.g_fhead[f];
             const uint32_t ridx = lidx(v, f, a.sides);
             const uint64_t rb = a.l_off[ridx], re = a.l_off[ridx + 1];
             const uint32_t R = (uint32_t)(re - rb);
@@ -1174,7 +1187,7 @@ batch_kernel(TreeArgs a) {
                         }
                     }
 #pragma unroll
-                    for (int round = 0; round < 3; ++round) {
+                    for (int round = 0; round < CHL_PROBE_ROUNDS; ++round) {
                         if (!pend) break;
 #pragma unroll
                         for (int t = 0; t < NE; ++t) {
@@ -1263,7 +1276,7 @@ batch_kernel(TreeArgs a) {
                 int nv_batch = 0;
                 for (uint32_t j = lane; j < nb; j += 32) {
                     const uint32_t kx = s_bk[j];
-                    const uint32_t rx = a.rank[s_bv[j]];
+                    const uint32_t rx = s_bp[j];   // rank stored by the scan
                     uint32_t skip;
                     if (PLANT) {
                         nv_batch += (int)(kx & 1u);
@@ -1298,8 +1311,9 @@ batch_kernel(TreeArgs a) {
                             const uint64_t lb = a.l_off[xu], le = a.l_off[xu + 1];
                             s_ba[j] = lb;
                             s_bl[j] = (uint32_t)(le - lb);
-                            nch = a.wide ? (uint32_t)((le - (lb & ~1ull) + 63) >> 6)
-                                         : (uint32_t)((le - (lb & ~1ull) + 31) >> 5);
+                            nch = a.lane_items ? (uint32_t)((le - (lb & ~1ull) + 15) >> 4)
+                                  : a.wide     ? (uint32_t)((le - (lb & ~1ull) + 63) >> 6)
+                                               : (uint32_t)((le - (lb & ~1ull) + 31) >> 5);
                             s_nch[j] = nch;
                         }
                         maxnch = max(maxnch, __reduce_max_sync(kFull, nch));
@@ -1312,10 +1326,12 @@ batch_kernel(TreeArgs a) {
                     const uint64_t inv = ((1ull << 32) + ntest - 1) / max(ntest, 1u);
                     const bool mul_div = (uint64_t)maxnch * ntest * ntest < (1ull << 32);
                     uint32_t cursor = 0, nread = 0;
+                    // items per step: one per lane group, or one per lane
+                    const uint32_t G = a.lane_items ? 32u : 8u;
                     while (true) {
-                        // the next (up to) 8 live items, in item order
+                        // the next (up to) G live items, in item order
                         uint32_t got = 0;
-                        while (got < 8 && cursor < nitems) {
+                        while (got < G && cursor < nitems) {
                             const uint32_t i = cursor + lane;
                             bool live = false;
                             uint32_t item = 0;
@@ -1327,7 +1343,7 @@ batch_kernel(TreeArgs a) {
                             }
                             const uint32_t lm = __ballot_sync(kFull, live);
                             const uint32_t nl = (uint32_t)__popc(lm);
-                            const uint32_t take = min(8u - got, nl);
+                            const uint32_t take = min(G - got, nl);
                             const uint32_t rk = __popc(lm & lanemask_lt());
                             if (live && rk < take) s_as[got + rk] = item;
                             if (take < nl) {
@@ -1341,6 +1357,33 @@ batch_kernel(TreeArgs a) {
                         }
                         __syncwarp();
                         if (got == 0) break;
+                        if (a.lane_items) {
+                            // one 16-entry item per lane (8 loads of one
+                            // 128-byte line in flight per lane)
+                            bool hit = false;
+                            uint32_t lj = 0;
+                            if (lane < got) {
+                                const uint32_t item = s_as[lane];
+                                lj = item & 0xFFu;
+                                const uint32_t c = item >> 8;
+                                const uint64_t glb = s_ba[lj];
+                                const uint64_t gle = glb + s_bl[lj];
+                                const uint32_t gdj = s_bk[lj] >> 1;
+                                const uint32_t ck = a.scan_back ? s_nch[lj] - 1 - c : c;
+                                const uint64_t e0 = (glb & ~1ull) + 16ull * ck;
+                                uint4 q[8];
+#pragma unroll
+                                for (int t = 0; t < 8; ++t) {
+                                    q[t] = make_uint4(0, 0, 0, 0);
+                                    if (e0 + 2 * t < gle) q[t] = *(const uint4 *)(a.l_ent + e0 + 2 * t);
+                                }
+                                hit = test8(q, e0, glb, gle, gdj);
+                                nread += 16;
+                            }
+                            if (hit) s_bp[lj] = 1;
+                            __syncwarp();
+                            continue;
+                        }
                         const bool act = g < got;
                         bool hit = false;
                         uint32_t gj = 0;
@@ -1530,12 +1573,23 @@ batch_kernel(TreeArgs a) {
                 };
                 // two 32-arc chunks per step: arc loads, rank loads and
                 // atomics of both chunks are issued together
-                for (uint32_t t0 = 0; t0 < total; t0 += 64) {
-                    uint32_t w[2] = {0, 0}, nk[2] = {0, 0}, old[2] = {kInf, kInf}, kxs[2] = {0, 0};
-                    uint32_t len[2] = {0, 0};
-                    bool act[2] = {false, false}, upd[2] = {false, false};
+                constexpr int RC = CHL_RELAX_CHUNKS;
+                for (uint32_t t0 = 0; t0 < total; t0 += 32 * RC) {
+                    uint32_t w[RC], nk[RC], old[RC], kxs[RC], len[RC], rk[RC];
+                    bool act[RC], upd[RC];
 #pragma unroll
-                    for (int c = 0; c < 2; ++c) {
+                    for (int c = 0; c < RC; ++c) {
+                        w[c] = 0;
+                        nk[c] = 0;
+                        old[c] = kInf;
+                        kxs[c] = 0;
+                        len[c] = 0;
+                        rk[c] = 0;
+                        act[c] = false;
+                        upd[c] = false;
+                    }
+#pragma unroll
+                    for (int c = 0; c < RC; ++c) {
                         const uint32_t tc = t0 + 32u * c;
                         const uint32_t own = tc < total ? owner(tc) : 0u;
                         const uint32_t t = tc + lane;
@@ -1543,25 +1597,26 @@ batch_kernel(TreeArgs a) {
                             const uint32_t lo = s_tl[own];
                             const uint64_t e = s_ba[lo] + (t - s_bx[own]);
                             if (UNIT) {
-                                w[c] = ghead[e];
+                                const uint2 hr = fhead[e];
+                                w[c] = hr.x;
+                                rk[c] = hr.y;
                                 len[c] = 1;
                             } else {
-                                const uint2 hl = garc[e];
+                                const uint4 hl = farc[e];
                                 w[c] = hl.x;
                                 len[c] = hl.y;
+                                rk[c] = hl.z;
                             }
                             kxs[c] = s_bk[lo];
                             act[c] = true;
                         }
                     }
-                    uint32_t nv[2] = {1u, 1u};
-                    if (PLANT) {
+                    uint32_t nv[RC];
 #pragma unroll
-                        for (int c = 0; c < 2; ++c)
-                            if (act[c]) nv[c] = ((kxs[c] & 1u) && a.rank[w[c]] >= r) ? 1u : 0u;
-                    }
+                    for (int c = 0; c < RC; ++c)
+                        nv[c] = (!PLANT || ((kxs[c] & 1u) && rk[c] >= r)) ? 1u : 0u;
 #pragma unroll
-                    for (int c = 0; c < 2; ++c) {
+                    for (int c = 0; c < RC; ++c) {
                         if (!act[c]) continue;
                         const uint64_t dd64 = (uint64_t)(kxs[c] >> 1) + len[c];
                         if (dd64 < 0x7FFFFFFFull) {
@@ -1577,7 +1632,7 @@ batch_kernel(TreeArgs a) {
                         }
                     }
 #pragma unroll
-                    for (int c = 0; c < 2; ++c) {
+                    for (int c = 0; c < RC; ++c) {
                         const bool fresh = upd[c] && old[c] == kInf;
                         const uint32_t fm = __ballot_sync(kFull, fresh);
                         if (fresh) {
@@ -1622,7 +1677,7 @@ batch_kernel(TreeArgs a) {
                 // two 32-entry chunks per step: their loads are issued
                 // together (both chunks are read before either is
                 // compacted, and compaction only moves entries left)
-                auto classify = [&](bool valid, uint32_t x, uint32_t kx, uint32_t wx) {
+                auto classify = [&](bool valid, uint32_t x, uint32_t kx, uint32_t wx, uint32_t rx) {
                     const bool take = valid && ((uint64_t)(kx >> 1) < (uint64_t)dmin + wx ||
                                                 (out_ok && (kx >> 1) < omin));
                     const uint32_t tm = __ballot_sync(kFull, take);
@@ -1630,6 +1685,7 @@ batch_kernel(TreeArgs a) {
                         const uint32_t at = nb + __popc(tm & lanemask_lt());
                         s_bv[at] = x;
                         s_bk[at] = kx;
+                        s_bp[at] = rx;   // rank, turned into the skip flag by settle()
                     }
                     nb += __popc(tm);
                     const bool kp = valid && !take;
@@ -1641,21 +1697,27 @@ batch_kernel(TreeArgs a) {
                     }
                     keep += __popc(km);
                 };
-                for (uint32_t b0 = 0; b0 < nf0 && !stop; b0 += 64) {
-                    if (nb > (uint32_t)kBatch - 64) settle();
+                for (uint32_t b0 = 0; b0 < nf0 && !stop; b0 += 32 * CHL_SCAN_CHUNKS) {
+                    if (nb > (uint32_t)kBatch - 32 * CHL_SCAN_CHUNKS) settle();
                     if (stop) break;
                     const long long ts0 = clock64();
-                    const uint32_t i0 = b0 + lane, i1 = b0 + 32 + lane;
-                    const bool v0 = i0 < nf0, v1 = i1 < nf0;
-                    const uint32_t x0 = v0 ? front[i0] : 0u;
-                    const uint32_t x1 = v1 ? front[i1] : 0u;
-                    const uint32_t k0 = v0 ? __ldcg(&key[x0]) : kInf;
-                    const uint32_t k1 = v1 ? __ldcg(&key[x1]) : kInf;
-                    const uint32_t w0 = v0 ? win[x0] : 0u;
-                    const uint32_t w1 = v1 ? win[x1] : 0u;
+                    bool vv[CHL_SCAN_CHUNKS];
+                    uint32_t xx[CHL_SCAN_CHUNKS], kk[CHL_SCAN_CHUNKS], ww[CHL_SCAN_CHUNKS], rr[CHL_SCAN_CHUNKS];
+#pragma unroll
+                    for (int c = 0; c < CHL_SCAN_CHUNKS; ++c) {
+                        const uint32_t i = b0 + 32 * c + lane;
+                        vv[c] = i < nf0;
+                        xx[c] = vv[c] ? front[i] : 0u;
+                    }
+#pragma unroll
+                    for (int c = 0; c < CHL_SCAN_CHUNKS; ++c) {
+                        kk[c] = vv[c] ? __ldcg(&key[xx[c]]) : kInf;
+                        ww[c] = vv[c] ? win[xx[c]] : 0u;
+                        rr[c] = vv[c] ? __ldg(&a.rank[xx[c]]) : 0u;
+                    }
                     __syncwarp();
-                    classify(v0, x0, k0, w0);
-                    classify(v1, x1, k1, w1);
+#pragma unroll
+                    for (int c = 0; c < CHL_SCAN_CHUNKS; ++c) classify(vv[c], xx[c], kk[c], ww[c], rr[c]);
                     __syncwarp();
                     cyc[0] += clock64() - ts0;
                 }
@@ -2114,6 +2176,22 @@ settle_kernel(TreeArgs a) {
     if (lane == 0) atomicAdd(&a.ctl->label_reads, c_reads);
 }
 
+// Per-build arc arrays carrying the head's rank, so a relaxation reads the
+// head, the length and the rank (PLaNT's via test) with one load.
+__global__ void fat_arcs(uint64_t m, const uint2 *arc, const uint32_t *rank, uint4 *out) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint2 a = arc[e];
+        out[e] = make_uint4(a.x, a.y, rank[a.x], 0u);
+    }
+}
+
+__global__ void fat_heads(uint64_t m, const uint32_t *head, const uint32_t *rank, uint2 *out) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t h = head[e];
+        out[e] = make_uint2(h, rank[h]);
+    }
+}
+
 // ---------------------------------------------------------- commit chain
 
 // Count new labels per label list (sorted keys).
@@ -2422,11 +2500,17 @@ struct Build {
     uint32_t warps = 0;
     uint32_t rcap = 0;
     uint32_t auto_stage = 2048;              // default root-label staging (batch kernel)
+    uint4 *farc[2] = {nullptr, nullptr};     // (head, length, rank[head], 0) per arc
+    uint2 *fhead[2] = {nullptr, nullptr};    // (head, rank[head]) per arc, unit lengths
     cudaGraphExec_t commit_exec = nullptr;   // captured commit chain
     uint64_t graph_launches = 0;
 
     ~Build() {
         if (commit_exec) cudaGraphExecDestroy(commit_exec);
+        if (farc[1] != farc[0]) cudaFree(farc[1]);
+        if (fhead[1] != fhead[0]) cudaFree(fhead[1]);
+        cudaFree(farc[0]);
+        cudaFree(fhead[0]);
         own.release();
         cudaFree(order);
         cudaFree(rank);
@@ -2576,6 +2660,29 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     // roots are requested), 1 tree_kernel (binary heap), 3 settle_kernel
     const bool use_settle = opts.tree_algo == 3 && opts.cta_roots <= 0;
     const bool use_batch = opts.tree_algo == 0 || opts.tree_algo == 2 || (opts.tree_algo == 3 && opts.cta_roots > 0);
+    unsigned long long prep_kernels = 0;
+    if (use_batch) {
+        // arcs with their head's rank for this order
+        const int nsides_g = g->symmetric ? 1 : 2;
+        for (int s = 0; s < nsides_g; ++s) {
+            const int src = g->symmetric ? 1 : s;
+            const uint64_t m = g->off[src][n];
+            const int grid = std::max(1, sms * 8);
+            if (unit) {
+                if ((rc = dalloc(&b.fhead[s], std::max<uint64_t>(m, 1)))) return rc;
+                fat_heads<<<grid, 256, 0, b.st>>>(m, b.dg->head[s], b.rank, b.fhead[s]);
+            } else {
+                if ((rc = dalloc(&b.farc[s], std::max<uint64_t>(m, 1)))) return rc;
+                fat_arcs<<<grid, 256, 0, b.st>>>(m, b.dg->arc[s], b.rank, b.farc[s]);
+            }
+            CHL_CUDA(cudaGetLastError());
+            ++prep_kernels;
+        }
+        if (nsides_g == 1) {
+            b.farc[1] = b.farc[0];
+            b.fhead[1] = b.fhead[0];
+        }
+    }
     const size_t per_slot = (size_t)n * (use_settle ? 24 : use_batch ? 12 : (unit ? 8 : 20));
     uint32_t want = (uint32_t)sms * 48;   // 12 blocks of 4 warps per SM at most
     if (opts.max_warps) want = std::min<uint32_t>(want, opts.max_warps);
@@ -2650,7 +2757,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     uint32_t r0 = 0;
     uint64_t committed = 0;
     uint32_t supersteps = 0, plant_roots = 0;
-    unsigned long long visits = 0, reads = 0, arcs = 0, launches = 0, kernels = 0;
+    unsigned long long visits = 0, reads = 0, arcs = 0, launches = 0, kernels = prep_kernels;
     double tree_ms = 0, sort_ms = 0, commit_ms = 0;
     uint32_t max_list = 0;   // longest committed list
     float step_tree_ms = 0;
@@ -2714,6 +2821,8 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
                 ta.g_off[s] = b.dg->off[s];
                 ta.g_arc[s] = b.dg->arc[s];
                 ta.g_head[s] = b.dg->head[s];
+                ta.g_farc[s] = b.farc[s];
+                ta.g_fhead[s] = b.fhead[s];
             }
             ta.order = b.order;
             ta.rank = b.rank;
@@ -2750,7 +2859,8 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             ta.chunk_sched = prune_sched == 2 ? 1 : 0;
             ta.hash_slots = hash_slots;
             ta.wide = prune_sched == 3 ? 1 : 0;
-            if (ta.wide) ta.chunk_sched = 1;
+            ta.lane_items = prune_sched == 4 ? 1 : 0;
+            if (ta.wide || ta.lane_items) ta.chunk_sched = 1;
             ta.hash_shift = 32;
             for (uint32_t t = hash_slots; t > 1; t >>= 1) --ta.hash_shift;
             ta.smem_block = (uint32_t)smem;
