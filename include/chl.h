@@ -175,7 +175,7 @@ typedef struct chl_build_opts {
     uint32_t root_stage;  /* root-label entries staged in shared memory per
                              tree (batched settle), 0 = auto: the most that
                              keeps the register-limited occupancy           */
-    int32_t prune_sched;  /* batched settle prune tests: 0 auto (= 3), 1 a
+    int32_t prune_sched;  /* batched settle prune tests: 0 auto (= 4), 1 a
                              lane group per vertex, 2 (vertex, 32-entry
                              chunk) items, 3 (vertex, 64-entry chunk) items,
                              4 (vertex, 16-entry chunk) items, one per lane */

@@ -68,7 +68,7 @@ struct BuildCtl {
     unsigned long long running;     // trees of the nominal root range in progress
     unsigned long long close_at;    // first root refused after the extension closed
     unsigned long long cyc[8];      // per-phase SM cycles summed over warps (diagnostics)
-    unsigned long long cnt[4];      // frontier entries scanned, rounds, settle calls, arcs relaxed
+    unsigned long long cnt[4];      // frontier entries scanned, rounds, settle calls, far entries scanned
 };
 
 struct TreeArgs {
@@ -114,6 +114,16 @@ struct TreeArgs {
     uint2 *ws_fq;                   // per warp slot: queue log (vertex, distance)
     uint32_t fq_cap;                // log entries per slot
 };
+
+// Phase-timing clock: with CHL_PHASE_TIMING it is also a compiler memory
+// barrier, so loads and stores are not moved across phase boundaries (a
+// stall is charged to the phase that uses the value); otherwise 0.
+__device__ __forceinline__ long long phase_clock() {
+    if (!kPhaseTiming) return 0;
+    long long t;
+    asm volatile("mov.u64 %0, %%clock64;" : "=l"(t)::"memory");
+    return t;
+}
 
 __device__ __forceinline__ uint32_t lidx(uint32_t v, int side, int sides) {
     return sides == 1 ? v : 2 * v + (uint32_t)side;
@@ -1041,8 +1051,8 @@ batch_kernel(TreeArgs a) {
     uint32_t *front = a.ws_front + (size_t)slot * a.n;
     unsigned long long c_vis = 0, c_reads = 0, c_arcs = 0;
     long long cyc[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // phase cycles (diagnostics)
-    unsigned long long dcnt[4] = {0, 0, 0, 0};      // scanned, rounds, settles, arcs
-    const long long k_start = clock64();
+    unsigned long long dcnt[4] = {0, 0, 0, 0};      // scanned, rounds, settles, far entries
+    const long long k_start = phase_clock();
     const uint32_t g = lane >> 2, sub = lane & 3;
     const uint32_t gmask = 0xFu << (4 * g);
 
@@ -1107,7 +1117,7 @@ batch_kernel(TreeArgs a) {
         uint32_t t_size = 0, t_lab = 0;
         const uint32_t v = a.order[r];
         for (int sd = 0; sd < a.sides; ++sd) {
-            const long long tr0 = clock64();
+            const long long tr0 = phase_clock();
             const int f = (a.sides == 1) ? 1 : sd;
             const uint64_t *goff = a.g_off[f];
             const uint32_t *win = a.win[f];
@@ -1248,7 +1258,7 @@ batch_kernel(TreeArgs a) {
                 front[0] = v;
             }
             __syncwarp();
-            cyc[5] += clock64() - tr0;
+            cyc[5] += phase_clock() - tr0;
             uint32_t nvis = 1, nf = 1;
             int ql = 1;
             uint32_t dmin = 0;          // smallest queued distance (exact, see below)
@@ -1270,7 +1280,7 @@ batch_kernel(TreeArgs a) {
             bool out_ok = false;
             auto settle = [&]() {
                 out_ok = false;
-                long long tc0 = clock64();
+                long long tc0 = phase_clock();
                 if (kPhaseTiming) dcnt[2]++;
                 t_size += nb;
                 int nv_batch = 0;
@@ -1290,7 +1300,7 @@ batch_kernel(TreeArgs a) {
                 }
                 if (PLANT) ql -= __reduce_add_sync(kFull, nv_batch);
                 __syncwarp();
-                long long tc1 = clock64();
+                long long tc1 = phase_clock();
                 cyc[1] += tc1 - tc0;
                 if (R > 0 && a.chunk_sched) {
                     // Prune tests flattened to (vertex, 32-entry chunk) items,
@@ -1491,7 +1501,7 @@ batch_kernel(TreeArgs a) {
                     c_reads += nread;
                     __syncwarp();
                 }
-                long long tc2 = clock64();
+                long long tc2 = phase_clock();
                 cyc[2] += tc2 - tc1;
                 for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
                     const uint32_t j = j0 + lane;
@@ -1520,7 +1530,7 @@ batch_kernel(TreeArgs a) {
                         t_lab += __popc(em);
                     }
                 }
-                long long tc3 = clock64();
+                long long tc3 = phase_clock();
                 cyc[3] += tc3 - tc2;
                 // arcs of the batch flattened over the lanes: the vertices
                 // with arcs are compacted (s_tl[k] = batch index, s_bx[k] =
@@ -1656,7 +1666,7 @@ batch_kernel(TreeArgs a) {
                 __syncwarp();
                 nb = 0;
                 if (PLANT && ql == 0) stop = true;   // plant :95 early exit
-                cyc[4] += clock64() - tc3;
+                cyc[4] += phase_clock() - tc3;
             };
 
             while (nf > 0 && !stop) {
@@ -1681,6 +1691,8 @@ batch_kernel(TreeArgs a) {
                     const bool take = valid && ((uint64_t)(kx >> 1) < (uint64_t)dmin + wx ||
                                                 (out_ok && (kx >> 1) < omin));
                     const uint32_t tm = __ballot_sync(kFull, take);
+                    if (kPhaseTiming)   // queued entries at least 1024 above the minimum
+                        dcnt[3] += __popc(__ballot_sync(kFull, valid && (kx >> 1) >= dmin + 1024u));
                     if (take) {
                         const uint32_t at = nb + __popc(tm & lanemask_lt());
                         s_bv[at] = x;
@@ -1700,7 +1712,7 @@ batch_kernel(TreeArgs a) {
                 for (uint32_t b0 = 0; b0 < nf0 && !stop; b0 += 32 * CHL_SCAN_CHUNKS) {
                     if (nb > (uint32_t)kBatch - 32 * CHL_SCAN_CHUNKS) settle();
                     if (stop) break;
-                    const long long ts0 = clock64();
+                    const long long ts0 = phase_clock();
                     bool vv[CHL_SCAN_CHUNKS];
                     uint32_t xx[CHL_SCAN_CHUNKS], kk[CHL_SCAN_CHUNKS], ww[CHL_SCAN_CHUNKS], rr[CHL_SCAN_CHUNKS];
 #pragma unroll
@@ -1719,7 +1731,7 @@ batch_kernel(TreeArgs a) {
 #pragma unroll
                     for (int c = 0; c < CHL_SCAN_CHUNKS; ++c) classify(vv[c], xx[c], kk[c], ww[c], rr[c]);
                     __syncwarp();
-                    cyc[0] += clock64() - ts0;
+                    cyc[0] += phase_clock() - ts0;
                 }
                 if (nb && !stop) settle();
                 if (stop) break;
@@ -1738,12 +1750,12 @@ batch_kernel(TreeArgs a) {
                 omin = __reduce_min_sync(kFull, onext);
             }
             c_vis += t_size;
-            const long long tz0 = clock64();
+            const long long tz0 = phase_clock();
             for (uint32_t k = lane; k < nvis; k += 32) __stcg(&key[vis[k]], kInf);
             if (a.hash_slots) {
                 for (uint32_t k = lane; k < a.hash_slots; k += 32) s_tab[k] = kSlotEmpty;
             }
-            cyc[6] += clock64() - tz0;
+            cyc[6] += phase_clock() - tz0;
             __syncwarp();
         }
         if (lane == 0) {
@@ -1761,7 +1773,7 @@ batch_kernel(TreeArgs a) {
     if (lane == 0) {
         atomicAdd(&a.ctl->label_reads, c_reads);
         if (kPhaseTiming) {
-            cyc[7] = clock64() - k_start;   // whole residency of the warp
+            cyc[7] = phase_clock() - k_start;   // whole residency of the warp
 #pragma unroll
             for (int i = 0; i < 8; ++i) atomicAdd(&a.ctl->cyc[i], (unsigned long long)cyc[i]);
 #pragma unroll
@@ -2736,10 +2748,10 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         heavy_tail = heavy;
     }
     // prune-test defaults of the batched settle (measured on RMAT scale 18
-    // and 512/1024-square grids): 64-entry items, root label hashed in
+    // and 512/1024-square grids): 16-entry items, one per lane, root label hashed in
     // shared memory, lists read from the end (recent, local hubs first) on
     // road-like graphs and from the start on heavy-tailed ones
-    const int prune_sched = opts.prune_sched ? opts.prune_sched : 3;
+    const int prune_sched = opts.prune_sched ? opts.prune_sched : 4;
     const int root_probe = opts.root_probe ? opts.root_probe : 2;
     const int scan_back = opts.scan_order ? (opts.scan_order == 1 ? 1 : 0) : (heavy_tail ? 0 : 1);
     // OUT criterion: measured slower on the 512/1024-square grids and RMAT
@@ -3051,6 +3063,8 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
                     100 * hc.cyc[4] / tot, 100 * hc.cyc[5] / tot, 100 * hc.cyc[6] / tot, tot);
             fprintf(stderr, "  frontier entries scanned %llu rounds %llu settles %llu (per visit: scanned %.2f)\n",
                     hc.cnt[0], hc.cnt[1], hc.cnt[2], (double)hc.cnt[0] / std::max<unsigned long long>(1, hc.visits));
+            fprintf(stderr, "  scanned entries at least 1024 above the queue minimum: %llu (%.1f%%)\n", hc.cnt[3],
+                    100.0 * hc.cnt[3] / std::max<unsigned long long>(1, hc.cnt[0]));
         }
         if (opts.verbose >= 2)
             fprintf(stderr, "  tree size max %llu mean %.1f\n", tstat[0],
