@@ -73,10 +73,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
         objs.append(o)
         if force or _stale(o, [s] + headers):
             cmd = [nvcc] + ARCH + COMMON + EXTRA + ["-c", s, "-o", o]
-            if src.endswith(".cu"):
-                cmd += ["-Xptxas", "-v"] if verbose else []
-            else:
-                cmd += ["-x", "cu"] if False else []
+            if src.endswith(".cu") and verbose:
+                cmd += ["-Xptxas", "-v"]
             jobs.append(cmd)
     if jobs:
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:

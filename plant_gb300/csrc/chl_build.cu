@@ -48,7 +48,10 @@ constexpr bool kPhaseTiming = CHL_PHASE_TIMING != 0;
 #define CHL_PROBE_ROUNDS 0   // hash probe rounds resolved in lock step (measured slower)
 #endif
 #ifndef CHL_SCAN_CHUNKS
-#define CHL_SCAN_CHUNKS 2    // 32-entry frontier chunks per scan step
+#define CHL_SCAN_CHUNKS 4    // 32-entry frontier chunks per scan step
+#endif
+#ifndef CHL_SMEM_CAP_KB
+#define CHL_SMEM_CAP_KB 112  // dynamic shared memory per block, at most (2 blocks per SM)
 #endif
 #ifndef CHL_RELAX_CHUNKS
 #define CHL_RELAX_CHUNKS 2   // 32-arc chunks per relax step
@@ -493,7 +496,10 @@ tree_kernel(TreeArgs a) {
 //     atomicMin on the packed (distance, via) key.
 // With unit lengths a batch is exactly one BFS level.  Relaxations from a
 // batch cannot improve a batch vertex, so batch order never matters.
-constexpr int kBatch = 128;
+#ifndef CHL_KBATCH
+#define CHL_KBATCH 256
+#endif
+constexpr int kBatch = CHL_KBATCH;   // settled vertices buffered per warp (<= 256: item packing)
 
 __host__ __device__ constexpr size_t batch_smem_per_warp(uint32_t rcap) {
     return ((size_t)8 * kBatch + (size_t)4 * (2 * rcap + 7 * kBatch + 1 + 32) + 15) & ~(size_t)15;
@@ -2796,7 +2802,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
                              : use_batch ? batch_smem_per_warp(0)
                                          : (unit ? 0 : kHeapSmem * 8) + kStage * 12;
         size_t rcap = std::min<uint32_t>(std::max<uint32_t>(max_list, 32), 2048);
-        const size_t smem_cap = std::min<size_t>((size_t)max_smem, 96 * 1024);
+        const size_t smem_cap = std::min<size_t>((size_t)max_smem, CHL_SMEM_CAP_KB * 1024);
         if (use_batch) {
             // The batch kernel stages a prefix of the root label and reads the
             // rest from global memory, so the staging capacity trades against
