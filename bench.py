@@ -63,6 +63,8 @@ def parse():
                     help="grid: 1024x1024 road-like grid (default); rmat: RMAT scale 20, degree order")
     ap.add_argument("--scale", type=int, default=20)
     ap.add_argument("--verbose", type=int, default=0, help="2: per-superstep lines on stderr")
+    ap.add_argument("--max-warps", type=int, default=0,
+                    help="cap on concurrent trees (bounds the per-tree workspace, e.g. for profiler captures)")
     ap.add_argument("--serve", action="store_true",
                     help="also run the open-loop serving test (Poisson arrivals) on the built labels")
     ap.add_argument("--serve-qps", type=float, default=2e8, help="offered pair rate (pairs/s)")
@@ -156,15 +158,25 @@ def profile_traffic():
         return None
 
 
-def make_workload(P, args):
+def make_workload(P, args, cpu_order=False):
+    """The graph (host-side seeded generator) and its order: on the GPU, or
+    with the CPU oracle's identical degree / betweenness order when the
+    reference arm must not touch the GPU engine."""
     if args.workload == "rmat":
         g = P.Graph.rmat(args.scale, 16, 0.57, 0.19, 0.19, seed=1)
-        order = P.Order.degree(g, seed=1)
-        return g, order
-    g = P.Graph.grid(args.side, args.side, del_frac=0.05, diag_frac=0.01, wmin=1, wmax=1000,
-                     highways=args.highways, hw_steps=64, hw_factor=150.0, seed=1)
-    order = P.Order.betweenness(g, args.sources, seed=1)
-    return g, order
+    else:
+        g = P.Graph.grid(args.side, args.side, del_frac=0.05, diag_frac=0.01, wmin=1, wmax=1000,
+                         highways=args.highways, hw_steps=64, hw_factor=150.0, seed=1)
+    if cpu_order:
+        from oracle import oracle as O
+        off, head, ln = g.csr(True)
+        og = O.OGraph.from_csr(g.get_n(), off, head, ln)
+        if args.workload == "rmat":
+            return g, og.degree_order(1)
+        return g, og.betweenness_order(args.sources, 1)
+    if args.workload == "rmat":
+        return g, P.Order.degree(g, seed=1)
+    return g, P.Order.betweenness(g, args.sources, seed=1)
 
 
 def workload_name(args):
@@ -284,8 +296,7 @@ def run_reference(args, ws, rank):
     import plant_gb300 as P
     from oracle import oracle as O
     P.lib()
-    g, order = make_workload(P, args)
-    off, head, ln = g.csr(True)
+    g, order = make_workload(P, args, cpu_order=True)
     og, r, threads, labels, secs = cpu_sample(g, order, args.cpu_seconds)
     vals = []
     for _ in range(args.warmup):
@@ -323,14 +334,14 @@ def run_ours(args, ws, rank):
             dist.barrier()
 
     for _ in range(args.warmup):
-        L = P.build(g, order)
+        L = P.build(g, order, max_warps=args.max_warps)
         del L
     barrier()
     stats = []
     t0 = time.time()
     with Clocks() as ck:
         for _ in range(args.steps):
-            L = P.build(g, order, verbose=args.verbose)
+            L = P.build(g, order, verbose=args.verbose, max_warps=args.max_warps)
             stats.append(L.stats())
     wall = time.time() - t0
     barrier()
@@ -365,7 +376,7 @@ def run_ours(args, ws, rank):
     d2h = 0
     for _ in range(max(1, args.steps)):
         t = time.time()
-        L2 = P.build(g, order)
+        L2 = P.build(g, order, max_warps=args.max_warps)
         o2, h2, d2 = L2.export()
         e2e_s.append(time.time() - t)
         d2h = o2.nbytes + h2.nbytes + d2.nbytes

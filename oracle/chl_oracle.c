@@ -912,69 +912,110 @@ void og_bc_sources(uint32_t n, uint32_t count, uint64_t seed, uint32_t *src) {
  * in-adjacency order; delta[v] sums its out-arc successors in out-adjacency
  * order; bc[v] adds sources in list order.  All in binary64 without fused
  * multiply-add, so a GPU restatement can match it bit for bit. */
-void og_betweenness(const og_graph *g, const uint32_t *src, uint32_t count, double *bc) {
-    const uint32_t n = g->n;
-    int32_t *dist = malloc((size_t)n * sizeof(int32_t));
-    double *sigma = malloc((size_t)n * sizeof(double));
-    double *delta = malloc((size_t)n * sizeof(double));
-    uint32_t *seq = malloc((size_t)n * sizeof(uint32_t));
-    for (uint32_t v = 0; v < n; ++v) bc[v] = 0.0;
+typedef struct {
+    int32_t *dist;
+    double *sigma, *delta;
+    uint32_t *seq;
+    uint32_t ns;
     oh_heap h;
-    oh_init(&h, n);
-    for (uint32_t j = 0; j < count; ++j) {
-        const uint32_t s = src[j];
-        for (uint32_t v = 0; v < n; ++v) dist[v] = INFTY;
-        dist[s] = 0;
-        oh_update(&h, s, 0);
-        uint32_t ns = 0;
-        while (h.size) {
-            uint32_t u = oh_pop(&h);
-            seq[ns++] = u;
-            for (uint64_t e = g->off[1][u]; e < g->off[1][u + 1]; ++e) {
-                int32_t dd = dist[u] + g->len[1][e];
-                uint32_t w = g->head[1][e];
-                if (dd < dist[w]) {
-                    dist[w] = dd;
-                    oh_update(&h, w, dd);
-                }
+} og_bc_ws;
+
+/* Dependencies delta_s[v] of one source s (forward shortest paths). */
+static void bc_one(const og_graph *g, uint32_t s, og_bc_ws *w) {
+    const uint32_t n = g->n;
+    int32_t *dist = w->dist;
+    double *sigma = w->sigma, *delta = w->delta;
+    uint32_t *seq = w->seq;
+    for (uint32_t v = 0; v < n; ++v) dist[v] = INFTY;
+    dist[s] = 0;
+    oh_update(&w->h, s, 0);
+    uint32_t ns = 0;
+    while (w->h.size) {
+        uint32_t u = oh_pop(&w->h);
+        seq[ns++] = u;
+        for (uint64_t e = g->off[1][u]; e < g->off[1][u + 1]; ++e) {
+            int32_t dd = dist[u] + g->len[1][e];
+            uint32_t x = g->head[1][e];
+            if (dd < dist[x]) {
+                dist[x] = dd;
+                oh_update(&w->h, x, dd);
             }
-        }
-        for (uint32_t k = 0; k < ns; ++k) {
-            uint32_t w = seq[k];
-            if (w == s) {
-                sigma[w] = 1.0;
-                continue;
-            }
-            double acc = 0.0;
-            for (uint64_t e = g->off[0][w]; e < g->off[0][w + 1]; ++e) {
-                uint32_t u = g->head[0][e];
-                if (dist[u] != INFTY && dist[u] + g->len[0][e] == dist[w]) acc = acc + sigma[u];
-            }
-            sigma[w] = acc;
-        }
-        for (uint32_t k = ns; k-- > 0;) {
-            uint32_t v = seq[k];
-            double acc = 0.0;
-            for (uint64_t e = g->off[1][v]; e < g->off[1][v + 1]; ++e) {
-                uint32_t w = g->head[1][e];
-                if (dist[w] != INFTY && dist[v] + g->len[1][e] == dist[w]) {
-                    double q = sigma[v] / sigma[w];
-                    double t = 1.0 + delta[w];
-                    acc = acc + q * t;
-                }
-            }
-            delta[v] = acc;
-        }
-        for (uint32_t k = 0; k < ns; ++k) {
-            uint32_t v = seq[k];
-            if (v != s) bc[v] = bc[v] + delta[v];
         }
     }
-    oh_free(&h);
-    free(dist);
-    free(sigma);
-    free(delta);
-    free(seq);
+    for (uint32_t k = 0; k < ns; ++k) {
+        uint32_t x = seq[k];
+        if (x == s) {
+            sigma[x] = 1.0;
+            continue;
+        }
+        double acc = 0.0;
+        for (uint64_t e = g->off[0][x]; e < g->off[0][x + 1]; ++e) {
+            uint32_t u = g->head[0][e];
+            if (dist[u] != INFTY && dist[u] + g->len[0][e] == dist[x]) acc = acc + sigma[u];
+        }
+        sigma[x] = acc;
+    }
+    for (uint32_t k = ns; k-- > 0;) {
+        uint32_t v = seq[k];
+        double acc = 0.0;
+        for (uint64_t e = g->off[1][v]; e < g->off[1][v + 1]; ++e) {
+            uint32_t x = g->head[1][e];
+            if (dist[x] != INFTY && dist[v] + g->len[1][e] == dist[x]) {
+                double q = sigma[v] / sigma[x];
+                double t = 1.0 + delta[x];
+                acc = acc + q * t;
+            }
+        }
+        delta[v] = acc;
+    }
+    w->ns = ns;
+}
+
+/* Brandes dependencies from each source over forward shortest paths, with
+ * a fixed summation order: sigma[w] sums its in-arc predecessors in
+ * in-adjacency order; delta[v] sums its out-arc successors in out-adjacency
+ * order; bc[v] adds sources in list order.  All in binary64 without fused
+ * multiply-add, so a GPU restatement can match it bit for bit.  Sources run
+ * in parallel in groups of `threads`; their dependencies are added to bc in
+ * source order, so the result does not depend on the thread count. */
+void og_betweenness(const og_graph *g, const uint32_t *src, uint32_t count, double *bc) {
+    const uint32_t n = g->n;
+    int threads = omp_get_max_threads();
+    if (threads < 1) threads = 1;
+    if ((uint32_t)threads > count && count > 0) threads = (int)count;
+    og_bc_ws *ws = calloc((size_t)threads, sizeof(og_bc_ws));
+    for (int t = 0; t < threads; ++t) {
+        ws[t].dist = malloc((size_t)n * sizeof(int32_t));
+        ws[t].sigma = malloc((size_t)n * sizeof(double));
+        ws[t].delta = malloc((size_t)n * sizeof(double));
+        ws[t].seq = malloc((size_t)n * sizeof(uint32_t));
+        oh_init(&ws[t].h, n);
+    }
+    for (uint32_t v = 0; v < n; ++v) bc[v] = 0.0;
+    for (uint32_t j0 = 0; j0 < count; j0 += (uint32_t)threads) {
+        const int cnt = (int)((count - j0) < (uint32_t)threads ? (count - j0) : (uint32_t)threads);
+#pragma omp parallel for num_threads(cnt) schedule(static, 1)
+        for (int t = 0; t < cnt; ++t) bc_one(g, src[j0 + (uint32_t)t], &ws[t]);
+        for (int t = 0; t < cnt; ++t) {
+            const uint32_t s = src[j0 + (uint32_t)t];
+            const uint32_t *seq = ws[t].seq;
+            const double *delta = ws[t].delta;
+            const int64_t ns = ws[t].ns;
+#pragma omp parallel for schedule(static)
+            for (int64_t k = 0; k < ns; ++k) {
+                const uint32_t v = seq[k];
+                if (v != s) bc[v] = bc[v] + delta[v];
+            }
+        }
+    }
+    for (int t = 0; t < threads; ++t) {
+        oh_free(&ws[t].h);
+        free(ws[t].dist);
+        free(ws[t].sigma);
+        free(ws[t].delta);
+        free(ws[t].seq);
+    }
+    free(ws);
 }
 
 /* Betweenness order: bc descending, ties by tie_key(seed, v) ascending. */
