@@ -501,8 +501,11 @@ tree_kernel(TreeArgs a) {
 #endif
 constexpr int kBatch = CHL_KBATCH;   // settled vertices buffered per warp (<= 256: item packing)
 
+constexpr int kEmit = 64;   // labels staged per warp before an append
+
 __host__ __device__ constexpr size_t batch_smem_per_warp(uint32_t rcap) {
-    return ((size_t)8 * kBatch + (size_t)4 * (2 * rcap + 7 * kBatch + 1 + 32) + 15) & ~(size_t)15;
+    return ((size_t)8 * kBatch + (size_t)4 * (2 * rcap + 7 * kBatch + 1 + 32) + 8 + (size_t)12 * kEmit + 15) &
+           ~(size_t)15;
 }
 
 __device__ __forceinline__ uint32_t bsearch_hub(const uint32_t *rh, int rstride, uint32_t R, uint32_t h) {
@@ -1050,11 +1053,16 @@ batch_kernel(TreeArgs a) {
     uint32_t *s_tl = s_bx + kBatch + 1;                // batch indices still to test
     uint32_t *s_bl = s_tl + kBatch;                    // label list length (chunk schedule)
     uint32_t *s_nch = s_bl + kBatch;                   // label list chunks (chunk schedule)
-    uint32_t *s_as = s_nch + kBatch;                   // items of the step (8 groups)
+    uint32_t *s_as = s_nch + kBatch;                   // items of the step (up to 32)
+    uint64_t *s_ek = (uint64_t *)(((uintptr_t)(s_as + 32) + 7) & ~(uintptr_t)7);   // staged label keys
+    uint32_t *s_ev = (uint32_t *)(s_ek + kEmit);       // staged label distances
 
     uint32_t *key = a.ws_key + (size_t)slot * a.n;
     uint32_t *vis = a.ws_vis + (size_t)slot * a.n;
-    uint32_t *front = a.ws_front + (size_t)slot * a.n;
+    // queue as two arrays: a round reads `front` and writes the vertices it
+    // keeps, and those its relaxations add, to `fnext`; then they swap
+    uint32_t *front = a.ws_front + (size_t)slot * 2 * a.n;
+    uint32_t *fnext = front + a.n;
     unsigned long long c_vis = 0, c_reads = 0, c_arcs = 0;
     long long cyc[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // phase cycles (diagnostics)
     unsigned long long dcnt[4] = {0, 0, 0, 0};      // scanned, rounds, settles, far entries
@@ -1070,9 +1078,9 @@ batch_kernel(TreeArgs a) {
         const size_t s0 = (size_t)blockIdx.x * kWarpsPerBlock;
         uint32_t *key0 = a.ws_key + s0 * a.n;
         uint32_t *vis0 = a.ws_vis + s0 * a.n;
-        uint32_t *f0 = a.ws_front + s0 * a.n;
-        uint32_t *f1 = a.ws_front + (s0 + 1) * a.n;
-        uint32_t *f2 = a.ws_front + (s0 + 2) * a.n;
+        uint32_t *f0 = a.ws_front + s0 * 2 * a.n;
+        uint32_t *f1 = f0 + a.n;
+        uint32_t *f2 = a.ws_front + (s0 + 1) * 2 * a.n;
         while (true) {
             __syncthreads();
             if (threadIdx.x == 0) {
@@ -1103,6 +1111,29 @@ batch_kernel(TreeArgs a) {
         __syncthreads();   // the block leaves the shared layout before warps reuse it
     }
     // ---- warp-per-tree phase
+    // emitted labels are staged in shared memory and appended to the new
+    // label arrays kEmit at a time (one atomic per flush instead of one
+    // per settle round)
+    uint32_t n_emit = 0;
+    auto flush_labels = [&]() {
+        __syncwarp();
+        if (n_emit) {
+            unsigned long long b = 0;
+            if (lane == 0) b = atomicAdd(&a.ctl->nlab, (unsigned long long)n_emit);
+            b = __shfl_sync(kFull, b, 0);
+            for (uint32_t k = lane; k < n_emit; k += 32) {
+                const unsigned long long p = b + k;
+                if (p < a.out_cap) {
+                    a.out_key[p] = s_ek[k];
+                    a.out_val[p] = s_ev[k];
+                } else {
+                    a.ctl->overflow = 1;
+                }
+            }
+        }
+        n_emit = 0;
+        __syncwarp();
+    };
     if (a.hash_slots) {
         for (uint32_t k = lane; k < a.hash_slots; k += 32) s_tab[k] = kSlotEmpty;
         __syncwarp();
@@ -1265,14 +1296,14 @@ batch_kernel(TreeArgs a) {
             }
             __syncwarp();
             cyc[5] += phase_clock() - tr0;
-            uint32_t nvis = 1, nf = 1;
+            uint32_t nvis = 1, nf = 1, nn = 0;   // queue sizes in front and fnext
             int ql = 1;
             uint32_t dmin = 0;          // smallest queued distance (exact, see below)
             bool stop = false;
             uint32_t nb = 0;            // vertices in the smem batch
 
             // Settle the batch held in smem: prune tests, labels, relaxations.
-            // New vertices are appended at front[nf..]; every key decrease of
+            // New vertices are appended to fnext; every key decrease of
             // a queued vertex lowers dnext, so dnext is the exact minimum of
             // the queue after the round.
             uint32_t dnext = kInf;
@@ -1521,18 +1552,14 @@ batch_kernel(TreeArgs a) {
                     }
                     const uint32_t em = __ballot_sync(kFull, emit);
                     if (em) {
-                        unsigned long long b = 0;
-                        if (lane == 0) b = atomicAdd(&a.ctl->nlab, (unsigned long long)__popc(em));
-                        b = __shfl_sync(kFull, b, 0);
+                        // labels go through the warp's shared staging buffer
+                        if (n_emit + 32 > (uint32_t)kEmit) flush_labels();
                         if (emit) {
-                            const unsigned long long p = b + __popc(em & lanemask_lt());
-                            if (p < a.out_cap) {
-                                a.out_key[p] = ((uint64_t)xu << a.hub_bits) | (uint64_t)(r - a.r0);
-                                a.out_val[p] = dj;
-                            } else {
-                                a.ctl->overflow = 1;
-                            }
+                            const uint32_t at = n_emit + __popc(em & lanemask_lt());
+                            s_ek[at] = ((uint64_t)xu << a.hub_bits) | (uint64_t)(r - a.r0);
+                            s_ev[at] = dj;
                         }
+                        n_emit += __popc(em);
                         t_lab += __popc(em);
                     }
                 }
@@ -1653,14 +1680,14 @@ batch_kernel(TreeArgs a) {
                         const uint32_t fm = __ballot_sync(kFull, fresh);
                         if (fresh) {
                             const uint32_t o = __popc(fm & lanemask_lt());
-                            if (nf + o < a.n && nvis + o < a.n) {
-                                front[nf + o] = w[c];
+                            if (nn + o < a.n && nvis + o < a.n) {
+                                fnext[nn + o] = w[c];
                                 vis[nvis + o] = w[c];
                             } else {
                                 a.ctl->err = 2;
                             }
                         }
-                        nf = min(nf + __popc(fm), a.n);
+                        nn = min(nn + __popc(fm), a.n);
                         nvis = min(nvis + __popc(fm), a.n);
                         if (PLANT) {
                             int dq = 0;
@@ -1678,11 +1705,11 @@ batch_kernel(TreeArgs a) {
             while (nf > 0 && !stop) {
                 // One round: walk the queue once.  Vertices with
                 // d < dmin + win are final and go to the batch (settled
-                // whenever it fills); the rest are compacted in place.
-                // Vertices appended during the round cannot qualify in it
-                // (their d >= dmin + win), so the walk stops at nf0.
+                // whenever it fills); the rest go to fnext, where the
+                // round's relaxations add new vertices (which cannot
+                // qualify in this round: their d >= dmin + win).
                 const uint32_t nf0 = nf;
-                uint32_t keep = 0;
+                nn = 0;
                 dnext = kInf;
                 onext = kInf;
                 out_ok = a.out_crit != 0;
@@ -1690,9 +1717,8 @@ batch_kernel(TreeArgs a) {
                     dcnt[0] += nf0;
                     dcnt[1]++;
                 }
-                // two 32-entry chunks per step: their loads are issued
-                // together (both chunks are read before either is
-                // compacted, and compaction only moves entries left)
+                // several 32-entry chunks per step: their loads are issued
+                // together
                 auto classify = [&](bool valid, uint32_t x, uint32_t kx, uint32_t wx, uint32_t rx) {
                     const bool take = valid && ((uint64_t)(kx >> 1) < (uint64_t)dmin + wx ||
                                                 (out_ok && (kx >> 1) < omin));
@@ -1709,11 +1735,11 @@ batch_kernel(TreeArgs a) {
                     const bool kp = valid && !take;
                     const uint32_t km = __ballot_sync(kFull, kp);
                     if (kp) {
-                        front[keep + __popc(km & lanemask_lt())] = x;
+                        fnext[nn + __popc(km & lanemask_lt())] = x;
                         dnext = min(dnext, kx >> 1);
                         if (a.out_crit) onext = min(onext, sat_add(kx >> 1, wout[x]));
                     }
-                    keep += __popc(km);
+                    nn += __popc(km);
                 };
                 for (uint32_t b0 = 0; b0 < nf0 && !stop; b0 += 32 * CHL_SCAN_CHUNKS) {
                     if (nb > (uint32_t)kBatch - 32 * CHL_SCAN_CHUNKS) settle();
@@ -1741,17 +1767,13 @@ batch_kernel(TreeArgs a) {
                 }
                 if (nb && !stop) settle();
                 if (stop) break;
-                // close the gap between the kept part and the appended part
-                const uint32_t app = nf - nf0;
-                for (uint32_t t0 = 0; t0 < app; t0 += 32) {
-                    const uint32_t t = t0 + lane;
-                    uint32_t x = 0;
-                    if (t < app) x = front[nf0 + t];
-                    __syncwarp();
-                    if (t < app) front[keep + t] = x;
-                    __syncwarp();
+                __syncwarp();
+                {
+                    uint32_t *t = front;
+                    front = fnext;
+                    fnext = t;
                 }
-                nf = keep + app;
+                nf = nn;
                 dmin = __reduce_min_sync(kFull, dnext);
                 omin = __reduce_min_sync(kFull, onext);
             }
@@ -1764,6 +1786,7 @@ batch_kernel(TreeArgs a) {
             cyc[6] += phase_clock() - tz0;
             __syncwarp();
         }
+        flush_labels();
         if (lane == 0) {
             a.tree_size[r - a.r0] = t_size;
             a.tree_labels[r - a.r0] = t_lab;
@@ -2701,7 +2724,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             b.fhead[1] = b.fhead[0];
         }
     }
-    const size_t per_slot = (size_t)n * (use_settle ? 24 : use_batch ? 12 : (unit ? 8 : 20));
+    const size_t per_slot = (size_t)n * (use_settle ? 24 : use_batch ? 16 : (unit ? 8 : 20));
     uint32_t want = (uint32_t)sms * 48;   // 12 blocks of 4 warps per SM at most
     if (opts.max_warps) want = std::min<uint32_t>(want, opts.max_warps);
     const size_t ws_budget = free_b / 3;
@@ -2715,7 +2738,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         b.fq_cap = (uint32_t)std::min<uint64_t>(2ull * n + 64, 0xFFFFFFF0ull);
         if ((rc = dalloc(&b.ws_fq, slots * b.fq_cap))) return rc;
     } else if (use_batch) {
-        if ((rc = dalloc(&b.ws_front, slots * n))) return rc;
+        if ((rc = dalloc(&b.ws_front, slots * 2 * (size_t)n))) return rc;   // front + fnext
     } else if (!unit) {
         if ((rc = dalloc(&b.ws_pos, slots * n)) || (rc = dalloc(&b.ws_heap, slots * n))) return rc;
     }
