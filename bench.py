@@ -149,8 +149,9 @@ def peaks():
 
 
 def profile_traffic():
-    """Per-launch DRAM traffic of the tree kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "tree_kernel_traffic.json")
+    """DRAM bytes per algorithmic byte of the tree kernel, from the committed
+    ncu capture of a smaller grid (scaled to this workload's launches)."""
+    p = os.path.join(ROOT, "profiles", "batch_kernel_traffic_grid512.json")
     try:
         with open(p) as f:
             return json.load(f)
@@ -395,7 +396,10 @@ def run_ours(args, ws, rank):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": (traffic or {}).get("bytes_per_unit_scaled"),
+                     "traffic": (work / max(1, stats[-1]["tree_launches"]) * traffic["dram_per_algorithmic_byte"]
+                                 if traffic else None),
+                     "traffic_note": ("bytes per launch, scaled from " + traffic["workload"] + " (ncu)"
+                                      if traffic else None),
                      "kernel": "batch_kernel", "algorithmic_bytes_per_build": work,
                      "tree_ms_per_build": avg_tree_ms, "tree_launches": stats[-1]["tree_launches"],
                      "ms_per_launch": per_launch_tree},

@@ -5,6 +5,8 @@
 #include <cstdint>
 #include <cstddef>
 #include <string>
+#include <memory>
+#include <utility>
 #include <vector>
 
 #include "../../include/chl.h"
@@ -73,6 +75,28 @@ struct alignas(8) LabelEnt {
     uint32_t dist;
 };
 
+// Allocator whose resize() leaves trivially constructible elements
+// uninitialised (host mirrors of multi-GB device arrays are overwritten at
+// once; zero-filling them first would double the host-side cost).
+template <typename T>
+struct NoInitAlloc : std::allocator<T> {
+    template <typename U>
+    struct rebind {
+        using other = NoInitAlloc<U>;
+    };
+    NoInitAlloc() = default;
+    template <typename U>
+    NoInitAlloc(const NoInitAlloc<U> &) {}
+    template <typename U>
+    void construct(U *p) noexcept {
+        ::new (static_cast<void *>(p)) U;
+    }
+    template <typename U, typename... A>
+    void construct(U *p, A &&...args) {
+        ::new (static_cast<void *>(p)) U(std::forward<A>(args)...);
+    }
+};
+
 // Labels: CSR over label lists, entries (hub, dist) ascending by hub.  A
 // symmetric build stores one list per vertex (index v, both sides equal);
 // otherwise list 2v+side.  Device copy plus a lazily fetched host mirror in
@@ -84,7 +108,7 @@ struct chl_labels {
     mutable LabelEnt *d_ent = nullptr;   // uploaded lazily for imported labels
     uint64_t total = 0;              // entries stored (one side if sym)
     mutable std::vector<uint64_t> h_off;
-    mutable std::vector<LabelEnt> h_ent;
+    mutable std::vector<LabelEnt, NoInitAlloc<LabelEnt>> h_ent;
     mutable bool host_valid = false;
     chl_build_stats stats{};
     uint32_t nl() const { return sym ? n : 2 * n; }

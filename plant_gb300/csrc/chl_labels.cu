@@ -36,16 +36,69 @@ int device_sms() {
     return sms;
 }
 
+// Device -> pageable host copy through two pinned staging buffers: the DMA
+// of one chunk overlaps the (multi-threaded) copy of the previous one out
+// of pinned memory.
+int d2h_staged(void *dst, const void *src, size_t bytes) {
+    constexpr size_t kChunk = 64ull << 20;
+    if (bytes <= kChunk) {
+        CHL_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+        return CHL_OK;
+    }
+    void *pin[2] = {nullptr, nullptr};
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    int rc = CHL_OK;
+    cudaError_t e = cudaHostAlloc(&pin[0], kChunk, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaHostAlloc(&pin[1], kChunk, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+    const size_t chunks = (bytes + kChunk - 1) / kChunk;
+    auto issue = [&](size_t c) {
+        const size_t off = c * kChunk, len = std::min(kChunk, bytes - off);
+        cudaError_t e2 = cudaMemcpyAsync(pin[c & 1], (const char *)src + off, len, cudaMemcpyDeviceToHost, st);
+        if (e2 == cudaSuccess) e2 = cudaEventRecord(ev[c & 1], st);
+        return e2;
+    };
+    if (e == cudaSuccess) e = issue(0);
+    for (size_t c = 0; c < chunks && e == cudaSuccess; ++c) {
+        e = cudaEventSynchronize(ev[c & 1]);
+        if (e != cudaSuccess) break;
+        if (c + 1 < chunks) {
+            e = issue(c + 1);
+            if (e != cudaSuccess) break;
+        }
+        const size_t off = c * kChunk, len = std::min(kChunk, bytes - off);
+        const char *from = (const char *)pin[c & 1];
+        char *to = (char *)dst + off;
+        const int64_t pieces = 16;
+#pragma omp parallel for schedule(static)
+        for (int64_t q = 0; q < pieces; ++q) {
+            const size_t a = len * (size_t)q / pieces, b = len * (size_t)(q + 1) / pieces;
+            std::memcpy(to + a, from + a, b - a);
+        }
+        // the next issue into this buffer happens only after this copy
+    }
+    if (e != cudaSuccess) rc = cuda_status(e, "staged device-to-host copy", __FILE__, __LINE__);
+    if (st) cudaStreamSynchronize(st);
+    for (auto x : ev)
+        if (x) cudaEventDestroy(x);
+    if (st) cudaStreamDestroy(st);
+    for (auto x : pin)
+        if (x) cudaFreeHost(x);
+    return rc;
+}
+
 int labels_fetch_host(const chl_labels *l) {
     if (l->host_valid) return CHL_OK;
     if (!l->d_off) return CHL_ERR_INVALID;
     const uint32_t nl = l->nl();
     l->h_off.resize((size_t)nl + 1);
     l->h_ent.resize(l->total);
-    CHL_CUDA(cudaMemcpy(l->h_off.data(), l->d_off, ((size_t)nl + 1) * 8, cudaMemcpyDeviceToHost));
-    if (l->total)
-        CHL_CUDA(cudaMemcpy(l->h_ent.data(), l->d_ent, l->total * sizeof(LabelEnt),
-                            cudaMemcpyDeviceToHost));
+    int rc = d2h_staged(l->h_off.data(), l->d_off, ((size_t)nl + 1) * 8);
+    if (!rc && l->total) rc = d2h_staged(l->h_ent.data(), l->d_ent, l->total * sizeof(LabelEnt));
+    if (rc) return rc;
     l->host_valid = true;
     return CHL_OK;
 }
@@ -275,17 +328,27 @@ extern "C" int chl_labels_export(const chl_labels *l, uint64_t *off, uint32_t *h
     if (!l || !off) return CHL_ERR_INVALID;
     int rc = labels_fetch_host(l);
     if (rc) return rc;
-    uint64_t p = 0;
+    // offsets of the 2n lists (both sides, even when stored once), then the
+    // entries, copied in parallel over vertices
     off[0] = 0;
     for (uint32_t v = 0; v < l->n; ++v)
         for (int side = 0; side < 2; ++side) {
             const uint32_t x = l->list(v, side);
-            for (uint64_t k = l->h_off[x]; k < l->h_off[x + 1]; ++k, ++p) {
-                if (hubs) hubs[p] = l->h_ent[k].hub;
-                if (dists) dists[p] = (int32_t)l->h_ent[k].dist;
-            }
-            off[2 * v + side + 1] = p;
+            off[2 * v + side + 1] = off[2 * v + side] + (l->h_off[x + 1] - l->h_off[x]);
         }
+    if (hubs || dists) {
+        const int64_t n = l->n;
+#pragma omp parallel for schedule(dynamic, 1024)
+        for (int64_t v = 0; v < n; ++v)
+            for (int side = 0; side < 2; ++side) {
+                const uint32_t x = l->list((uint32_t)v, side);
+                uint64_t p = off[2 * v + side];
+                for (uint64_t k = l->h_off[x]; k < l->h_off[x + 1]; ++k, ++p) {
+                    if (hubs) hubs[p] = l->h_ent[k].hub;
+                    if (dists) dists[p] = (int32_t)l->h_ent[k].dist;
+                }
+            }
+    }
     return CHL_OK;
 }
 
