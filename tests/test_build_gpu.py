@@ -91,6 +91,37 @@ def test_directed_weighted_matches_oracle(P, O, mode, algo, tmp_path):
     assert same_labels(L, ref, n)
 
 
+def test_directed_power_law_matches_oracle(P, O, tmp_path):
+    """Directed, weighted, skewed degrees (2^15 vertices, ~2^18 arcs): two
+    distinct label sides at a size where supersteps, the hash probe and the
+    extension all engage."""
+    rng = np.random.default_rng(11)
+    n, m = 1 << 15, 1 << 18
+    # endpoints: half uniform, half from a Pareto tail over a permutation
+    perm = rng.permutation(n).astype(np.uint32)
+
+    def pick(k):
+        z = perm[np.minimum((rng.pareto(1.2, k) * 40).astype(np.int64), n - 1)]
+        u = rng.integers(0, n, k).astype(np.uint32)
+        return np.where(rng.random(k) < 0.5, z, u).astype(np.uint32)
+
+    src, dst = pick(m), pick(m)
+    keep = src != dst
+    w = rng.integers(1, 100, m).astype(np.int32)
+    g = P.Graph.from_arcs(n, src[keep], dst[keep], w[keep])
+    assert not g.symmetric()
+    p = str(tmp_path / "pl.gr")
+    g.write(p)
+    og = O.OGraph.read_dimacs(p)
+    order = og.degree_order(5)
+    ref, _ = O.gll(og, order)
+    for kw in ({}, {"mode": MODES["gll"]}, {"first_superstep": 100, "growth": 0.5}):
+        L = P.build(g, order, **kw)
+        assert same_labels(L, ref, n), kw
+    pairs = P.generate_query(20000, n, seed=3)
+    assert np.array_equal(P.query(L, pairs), ref.query(pairs))
+
+
 def test_tiny_and_disconnected(P, O):
     # isolated vertices, a 2-cycle and a single arc
     g = P.Graph.from_arcs(5, [0, 1, 3], [1, 0, 4], [2, 2, 7])
