@@ -62,6 +62,13 @@ const char *chl_last_error(void);
  * (shared_memory/graph.hpp:103-153). */
 int chl_graph_load(const char *path, int undirected, chl_graph **out);
 
+/* Replaces hl::Graph::read (shared_memory/graph.hpp:327-335) like
+ * chl_graph_load, with DIMACS files parsed and their arc lists built on the
+ * GPU (the reference's line rules and init_arcs, :168-189 and :103-153).
+ * Files that are not DIMACS by those rules go through the host parsers (METIS,
+ * SNAP, edge list).  *parsed_on_gpu (may be NULL) tells which path ran. */
+int chl_graph_load_gpu(const char *path, int undirected, chl_graph **out,
+                       int *parsed_on_gpu);
 /* Replaces hl::Graph::set_n + add_arc + finalize
  * (shared_memory/graph.hpp:349-353): builds a graph from k arcs
  * (src[i] -> dst[i], length len[i]); when `undirected` is non-zero every arc

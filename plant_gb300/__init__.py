@@ -86,6 +86,7 @@ SIGNATURES = {
     "chl_status_str": (C.c_char_p, [C.c_int]),
     "chl_last_error": (C.c_char_p, []),
     "chl_graph_load": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(_P)]),
+    "chl_graph_load_gpu": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(_P), C.POINTER(C.c_int)]),
     "chl_graph_from_arcs": (C.c_int, [C.c_uint32, C.c_size_t, _U32P, _U32P, _I32P, C.c_int, C.POINTER(_P)]),
     "chl_graph_write_dimacs": (C.c_int, [_P, C.c_char_p]),
     "chl_graph_n": (C.c_uint32, [_P]),
@@ -197,6 +198,16 @@ class Graph:
         h = C.c_void_p()
         _check(lib().chl_graph_load(os.fsencode(path), int(undirected), C.byref(h)), f"read {path}")
         return cls(h)
+
+    @classmethod
+    def read_gpu(cls, path: str, undirected: bool = False):
+        """Graph::read with DIMACS files parsed on the GPU; returns (graph,
+        parsed_on_gpu).  Other formats go through the host parsers."""
+        h = C.c_void_p()
+        used = C.c_int(0)
+        _check(lib().chl_graph_load_gpu(os.fsencode(path), int(undirected), C.byref(h), C.byref(used)),
+               f"read {path}")
+        return cls(h), bool(used.value)
 
     @classmethod
     def from_arcs(cls, n: int, src, dst, length, undirected: bool = False) -> "Graph":

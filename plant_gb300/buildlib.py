@@ -28,6 +28,7 @@ SOURCES = [
     "chl_server.cu",
     "chl_gnn.cu",
     "chl_labelio.cu",
+    "chl_ingest.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

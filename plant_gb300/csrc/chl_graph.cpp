@@ -46,7 +46,7 @@ static inline bool cmp_head(const TmpArc &x, const TmpArc &y) {
     return x.len < y.len;
 }
 
-static void fill_stats(chl_graph *g) {
+void graph_fill_stats(chl_graph *g) {
     int32_t mn = kInfty, mx = 0;
     bool unit = true;
     for (int s = 0; s < 2; ++s) {
@@ -122,7 +122,7 @@ static void init_arcs(chl_graph *g, std::vector<TmpArc> &a) {
     }
     a.clear();
     a.shrink_to_fit();
-    fill_stats(g);
+    graph_fill_stats(g);
 }
 
 // add_tmp_arc (shared_memory/graph.hpp:156-162).  u and v arrive already
@@ -322,7 +322,7 @@ int graph_from_undirected_unique(uint32_t n, std::vector<uint64_t> &uv,
     g->off[0] = g->off[1];
     g->head[0] = g->head[1];
     g->len[0] = g->len[1];
-    fill_stats(g);
+    graph_fill_stats(g);
     *out = g;
     return CHL_OK;
 }

@@ -72,7 +72,7 @@ int main(int argc, char **argv) {
         return 1;
     }
     chl_graph *g = nullptr;
-    if (!graph_path || chl_graph_load(graph_path, 0, &g) != CHL_OK) {
+    if (!graph_path || chl_graph_load_gpu(graph_path, 0, &g, nullptr) != CHL_OK) {
         std::cerr << "Unable to read graph from raw " << (graph_path ? graph_path : "(none)") << std::endl;
         return 1;
     }
