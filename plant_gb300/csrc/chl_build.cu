@@ -53,6 +53,10 @@ constexpr bool kPhaseTiming = CHL_PHASE_TIMING != 0;
 #ifndef CHL_SMEM_CAP_KB
 #define CHL_SMEM_CAP_KB 112  // dynamic shared memory per block, at most (2 blocks per SM)
 #endif
+#ifndef CHL_BATCH_MIN_BLOCKS
+#define CHL_BATCH_MIN_BLOCKS 0   // batched settle launch bound (0: compiler's choice;
+                                 // 1 measured slower: more registers, fewer warps)
+#endif
 #ifndef CHL_RELAX_CHUNKS
 #define CHL_RELAX_CHUNKS 2   // 32-arc chunks per relax step
 #endif
@@ -1036,7 +1040,7 @@ __device__ void cta_tree(const TreeArgs &a, uint32_t r, unsigned char *smem, siz
 }
 
 template <bool UNIT, bool PLANT>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, CHL_BATCH_MIN_BLOCKS)
 batch_kernel(TreeArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
