@@ -366,6 +366,8 @@ def run_ours(args, ws, rank):
     qk = 1 << 22
     q_ms, q_bytes = P.query_bench(L, qk, iters=20, seed=7)
     qps = qk / (q_ms / 1e3)
+    # hot set: every pair one of 1,000 fixed pairs (label lists L2-resident)
+    qh_ms, qh_bytes = P.query_bench(L, qk, iters=20, seed=7, hot=1000)
     # e2e through the C ABI from host buffers
     g.release_device()
     off, head, ln = g.csr(True)
@@ -409,13 +411,29 @@ def run_ours(args, ws, rank):
                   "visits": stats[-1]["visits"], "label_reads": stats[-1]["label_reads"],
                   "wall_s_per_step": wall / args.steps},
         "query": {"pairs": qk, "qps": qps, "ms_per_batch": q_ms, "bytes_per_batch": q_bytes,
-                  "achieved_gbs": q_bytes / (q_ms / 1e3) / 1e9},
+                  "achieved_gbs": q_bytes / (q_ms / 1e3) / 1e9,
+                  "roofline_frac": (q_bytes / (q_ms / 1e3) / 1e9) / peak,
+                  "hot_qps": qk / (qh_ms / 1e3), "hot_set": 1000,
+                  "hot_achieved_gbs": qh_bytes / (qh_ms / 1e3) / 1e9},
     }
     if rank == 0 and not args.no_cpu:
         og, r, threads, lab, secs = cpu_sample(g, order, args.cpu_seconds)
         line["cpu_baseline"] = {"value": lab / secs, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": f"GLL restatement on the first {r} of {n} roots (both sides)",
                                 "seconds": secs}
+        # CPU queries: the batchLocalQuery loop (OpenMP over pairs) on the same labels
+        from oracle import oracle as O
+        o2, h2, d2 = L.export()
+        ol = O.OLabels.from_csr(n, o2, h2, d2)
+        del o2, h2, d2
+        pairs = P.generate_query(1 << 20, n, seed=7)
+        ol.query(pairs[:1024])
+        t = time.time()
+        ol.query(pairs)
+        cq = time.time() - t
+        line["query"]["cpu_qps"] = len(pairs) / cq
+        line["query"]["cpu_cores"] = os.cpu_count()
+        del ol
     if rank == 0 and args.serve:
         line["serving"] = serve_test(P, L, n, args.serve_qps, args.serve_seconds)
     if rank == 0 and args.cpu_full:

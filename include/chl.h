@@ -298,11 +298,12 @@ int chl_query_batch_noalloc(const chl_labels *l, const uint32_t *pairs, size_t k
 int chl_query_batch_device(const chl_labels *l, const uint32_t *d_pairs,
                            size_t k, int32_t *d_out, void *stream);
 /* Device-resident query benchmark (no reference counterpart): k uniform
- * pairs generated on the device, `iters` timed launches of the batch query
- * kernel (CUDA events on its own stream); returns the mean ms per launch
- * and the algorithmic bytes of one launch (8 B per label entry of both
- * lists, plus the 8-byte pair and 4-byte answer). */
-int chl_query_bench(const chl_labels *l, size_t k, uint64_t seed, int iters,
+ * pairs generated on the device (hot > 0: each pair drawn from a fixed set
+ * of `hot` seeded pairs), `iters` timed launches of the batch query kernel
+ * (CUDA events on its own stream); returns the mean ms per launch and the
+ * algorithmic bytes of one launch (8 B per label entry of both lists, plus
+ * the 8-byte pair and 4-byte answer). */
+int chl_query_bench(const chl_labels *l, size_t k, uint64_t seed, int iters, uint32_t hot,
                     double *ms_per_iter, uint64_t *bytes_per_iter);
 /* Replaces hl::generate_query (distributed_memory/query.hpp:43-51) with a
  * seeded generator: k uniform pairs over [0, range). */

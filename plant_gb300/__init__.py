@@ -128,7 +128,7 @@ SIGNATURES = {
     "chl_query_batch": (C.c_int, [_P, _U32P, C.c_size_t, _I32P, _P]),
     "chl_query_batch_noalloc": (C.c_int, [_P, _U32P, C.c_size_t, _I32P, _P]),
     "chl_query_batch_device": (C.c_int, [_P, _P, C.c_size_t, _P, _P]),
-    "chl_query_bench": (C.c_int, [_P, C.c_size_t, C.c_uint64, C.c_int, C.POINTER(C.c_double), _U64P]),
+    "chl_query_bench": (C.c_int, [_P, C.c_size_t, C.c_uint64, C.c_int, C.c_uint32, C.POINTER(C.c_double), _U64P]),
     "chl_query_generate": (C.c_int, [_U32P, C.c_size_t, C.c_uint32, C.c_uint64]),
     "chl_query_load": (C.c_int, [C.c_char_p, C.POINTER(_U32P), C.POINTER(C.c_size_t)]),
     "chl_server_opts_default": (None, [C.POINTER(ServerOpts)]),
@@ -463,11 +463,12 @@ def query(labels: Labeling, pairs) -> np.ndarray:
     return out
 
 
-def query_bench(labels: Labeling, k: int, iters: int = 10, seed: int = 1):
-    """(ms per launch, algorithmic bytes per launch) of k device-resident pairs."""
+def query_bench(labels: Labeling, k: int, iters: int = 10, seed: int = 1, hot: int = 0):
+    """(ms per launch, algorithmic bytes per launch) of k device-resident pairs
+    (uniform, or drawn from `hot` fixed pairs)."""
     ms = C.c_double()
     b = C.c_uint64()
-    _check(lib().chl_query_bench(labels._h, k, seed, iters, C.byref(ms), C.byref(b)), "query bench")
+    _check(lib().chl_query_bench(labels._h, k, seed, iters, hot, C.byref(ms), C.byref(b)), "query bench")
     return ms.value, b.value
 
 

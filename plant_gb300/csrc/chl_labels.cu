@@ -234,10 +234,19 @@ __device__ __forceinline__ uint64_t qmix(uint64_t z) {
 }
 
 // Uniform random pairs generated on the device (query benchmark input).
-__global__ void gen_pairs(uint32_t *pairs, size_t k, uint32_t n, uint64_t seed) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < 2 * k;
-         i += (size_t)gridDim.x * blockDim.x)
-        pairs[i] = (uint32_t)(qmix(seed ^ (i * 0xD1B54A32D192ED03ull)) % n);
+// k seeded uniform pairs; with hot > 0, every pair is one of `hot` fixed
+// seeded pairs (drawn uniformly), as a request stream with a hot set
+__global__ void gen_pairs(uint32_t *pairs, size_t k, uint32_t n, uint64_t seed, uint32_t hot) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < k; q += (size_t)gridDim.x * blockDim.x) {
+        size_t a = 2 * q, b = 2 * q + 1;
+        if (hot) {
+            const size_t j = qmix(seed ^ (q * 0x9E3779B97F4A7C15ull) ^ 0x5A5Aull) % hot;
+            a = 2 * j;
+            b = 2 * j + 1;
+        }
+        pairs[2 * q] = (uint32_t)(qmix(seed ^ (a * 0xD1B54A32D192ED03ull)) % n);
+        pairs[2 * q + 1] = (uint32_t)(qmix(seed ^ (b * 0xD1B54A32D192ED03ull)) % n);
+    }
 }
 
 // Algorithmic bytes of a query batch: 8 (|L(s,1)| + |L(t,0)|) + 8 + 4 per pair.
@@ -392,7 +401,7 @@ extern "C" int chl_query_batch_device(const chl_labels *l, const uint32_t *d_pai
     return query_launch(l, d_pairs, k, d_out, (cudaStream_t)stream);
 }
 
-extern "C" int chl_query_bench(const chl_labels *l, size_t k, uint64_t seed, int iters,
+extern "C" int chl_query_bench(const chl_labels *l, size_t k, uint64_t seed, int iters, uint32_t hot,
                                double *ms_per_iter, uint64_t *bytes_per_iter) {
     if (!l || !ms_per_iter || k == 0 || iters < 1 || l->n == 0) return CHL_ERR_INVALID;
     int rc = labels_ensure_device(l);
@@ -411,7 +420,7 @@ extern "C" int chl_query_bench(const chl_labels *l, size_t k, uint64_t seed, int
     float ms = 0;
     unsigned long long bytes = 0;
     if (e == cudaSuccess) {
-        gen_pairs<<<device_sms() * 8, 256, 0, st>>>(dp, k, l->n, seed);
+        gen_pairs<<<device_sms() * 8, 256, 0, st>>>(dp, k, l->n, seed, hot);
         cudaMemsetAsync(dbytes, 0, 8, st);
         query_bytes<<<device_sms() * 8, 256, 0, st>>>(l->d_off, l->sym ? 1 : 0, dp, k, dbytes);
         rc = query_launch(l, dp, k, dout, st);   // warm-up

@@ -194,6 +194,26 @@ def test_sampled_queries_equal_dijkstra(P, O):
         assert np.array_equal(P.query(L, pairs), d)
 
 
+def test_config1_100k_queries_equal_dijkstra(P, O):
+    """Config 1: 100x100 grid, degree order, 100,000 uniform (s, t) pairs
+    answered by the GPU labels and by plain Dijkstra on the CPU."""
+    g = P.Graph.grid(100, 100, seed=1)
+    order = P.Order.degree(g, seed=1)
+    L = P.build(g, order)
+    n = g.get_n()
+    off, head, ln = g.csr(True)
+    og = O.OGraph.from_csr(n, off, head, ln)
+    pairs = P.generate_query(100000, n, seed=3)
+    got = P.query(L, pairs)
+    exp = np.empty(len(pairs), np.int32)
+    by_src = np.argsort(pairs[:, 0], kind="stable")
+    srcs, first, cnt = np.unique(pairs[by_src, 0], return_index=True, return_counts=True)
+    for s, a, c in zip(srcs, first, cnt):
+        sel = by_src[a:a + c]
+        exp[sel] = og.dijkstra(int(s))[pairs[sel, 1]]
+    assert np.array_equal(got, exp)
+
+
 @pytest.mark.parametrize("mode", list(MODES))
 def test_root_limit_gives_the_label_prefix(P, mode):
     """A build of the roots of rank < R holds exactly the full labeling's
