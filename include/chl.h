@@ -195,7 +195,10 @@ typedef struct chl_build_opts {
                              off on heavy-tailed ones; 1 off)               */
     int32_t settle_rule;  /* batched settle finality test: 0 auto (= 1),
                              1 IN criterion, 2 IN and OUT criteria          */
-    uint32_t reserved[4];
+    int32_t prune_order;  /* label order scanned by prune tests: 0 auto
+                             (a distance-ordered copy with lane items and the
+                             hashed root label), 1 hub order                */
+    uint32_t reserved[3];
 } chl_build_opts;
 
 /* Fill opts with the defaults (hybrid, sf 32, ps 1024, autotune on,

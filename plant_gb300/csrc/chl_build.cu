@@ -106,6 +106,8 @@ struct TreeArgs {
     const uint32_t *win[2];         // [f]: shortest arc into v along direction f
     const uint32_t *wout[2];        // [f]: shortest arc out of v along direction f
     int out_crit;                   // batch kernel: OUT criterion on
+    const uint2 *l_dent;            // batch kernel: committed entries ordered by (distance, hub)
+    int dist_order;                 // batch kernel: prune tests scan l_dent
     const uint4 *g_farc[2];         // batch kernel: (head, length, rank[head]) per arc
     const uint2 *g_fhead[2];        // batch kernel: (head, rank[head]) per arc, unit lengths
     uint32_t *ws_front;             // per warp slot: queued (unsettled) vertices
@@ -1165,6 +1167,9 @@ batch_kernel(TreeArgs a) {
             const uint32_t *wout = a.wout[f];
             const uint4 *farc = a.g_farc[f];
             const uint2 *fhead = a.g_fhead[f];
+            // label entries the prune tests scan: distance-ordered copy or the
+            // hub-ordered lists
+            const uint2 *lscan = a.dist_order ? a.l_dent : a.l_ent;
             const uint32_t ridx = lidx(v, f, a.sides);
             const uint64_t rb = a.l_off[ridx], re = a.l_off[ridx + 1];
             const uint32_t R = (uint32_t)(re - rb);
@@ -1411,7 +1416,7 @@ batch_kernel(TreeArgs a) {
                         if (a.lane_items) {
                             // one 16-entry item per lane (8 loads of one
                             // 128-byte line in flight per lane)
-                            bool hit = false;
+                            bool hit = false, exhausted = false;
                             uint32_t lj = 0;
                             if (lane < got) {
                                 const uint32_t item = s_as[lane];
@@ -1420,18 +1425,29 @@ batch_kernel(TreeArgs a) {
                                 const uint64_t glb = s_ba[lj];
                                 const uint64_t gle = glb + s_bl[lj];
                                 const uint32_t gdj = s_bk[lj] >> 1;
-                                const uint32_t ck = a.scan_back ? s_nch[lj] - 1 - c : c;
+                                const uint32_t ck = (a.scan_back && !a.dist_order) ? s_nch[lj] - 1 - c : c;
                                 const uint64_t e0 = (glb & ~1ull) + 16ull * ck;
                                 uint4 q[8];
 #pragma unroll
                                 for (int t = 0; t < 8; ++t) {
                                     q[t] = make_uint4(0, 0, 0, 0);
-                                    if (e0 + 2 * t < gle) q[t] = *(const uint4 *)(a.l_ent + e0 + 2 * t);
+                                    if (e0 + 2 * t < gle) q[t] = *(const uint4 *)(lscan + e0 + 2 * t);
                                 }
                                 hit = test8(q, e0, glb, gle, gdj);
                                 nread += 16;
+                                if (a.dist_order && !hit) {
+                                    // distance order: once the chunk's last entry is
+                                    // beyond d, no later chunk can hold a witness
+                                    const uint64_t last = min(e0 + 15, gle - 1);
+                                    uint32_t lastd = 0;
+#pragma unroll
+                                    for (int t = 0; t < 16; ++t)
+                                        if ((uint64_t)t == last - e0) lastd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
+                                    if (lastd > gdj) exhausted = true;
+                                }
                             }
                             if (hit) s_bp[lj] = 1;
+                            else if (exhausted) atomicOr(&s_bp[lj], 2u);
                             __syncwarp();
                             continue;
                         }
@@ -1548,7 +1564,7 @@ batch_kernel(TreeArgs a) {
                     const uint32_t j = j0 + lane;
                     bool emit = false;
                     uint32_t xu = 0, dj = 0;
-                    if (j < nb && s_bp[j] == 0) {
+                    if (j < nb && (s_bp[j] & 1u) == 0) {
                         const uint32_t kx = s_bk[j];
                         emit = !PLANT || (kx & 1u);
                         xu = lidx(s_bv[j], 1 - f, a.sides);
@@ -1578,7 +1594,7 @@ batch_kernel(TreeArgs a) {
                 for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
                     const uint32_t j = j0 + lane;
                     uint32_t deg = 0;
-                    if (j < nb && s_bp[j] == 0) {
+                    if (j < nb && (s_bp[j] & 1u) == 0) {
                         const uint32_t x = s_bv[j];
                         const uint64_t ab = goff[x];
                         deg = (uint32_t)(goff[x + 1] - ab);
@@ -2350,6 +2366,63 @@ __global__ void place_new(const uint64_t *keys, const uint32_t *vals,
     }
 }
 
+// ---- distance-ordered copy of the committed labels (prune tests only)
+// Lists in the same CSR offsets, entries ordered by (distance, hub): an
+// entry (h, dd) of L(u) can only witness d(r, u) if dd <= d(r, u), so a
+// prune test stops at the first chunk whose entries all exceed d(r, u).
+
+__device__ __forceinline__ bool ent_less(uint2 a, uint2 b) { return a.y < b.y || (a.y == b.y && a.x < b.x); }
+
+// new labels sorted by (list, hub) -> keys (list << 32 | dist), values hub
+__global__ void dist_keys(const uint64_t *keys, const uint32_t *vals, const unsigned long long *d_n,
+                          unsigned long long cap, int hub_bits, uint32_t r0, uint64_t *k2, uint32_t *v2) {
+    unsigned long long n = *d_n;
+    if (n > cap) n = cap;
+    const uint64_t mask = (1ull << hub_bits) - 1;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint64_t k = keys[i];
+        k2[i] = ((k >> hub_bits) << 32) | vals[i];
+        v2[i] = r0 + (uint32_t)(k & mask);
+    }
+}
+
+// Merge, per list, the committed distance-ordered entries with the new ones
+// (sorted by (list, dist) in k2/v2, the list's run at [pre[x], pre[x+1])).
+// One warp per list; every entry's final slot is its rank in the other run
+// (binary search) plus its own index.  Ties in distance order by hub.
+__global__ void merge_dist_lists(const uint64_t *old_off, const uint2 *old_ent, const uint64_t *new_off,
+                                 const uint64_t *pre, const uint64_t *k2, const uint32_t *v2, uint2 *out,
+                                 uint32_t nl) {
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t x = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); x < nl; x += warps) {
+        const uint64_t ob = old_off[x], oe = old_off[x + 1], nb = new_off[x];
+        const uint64_t pb = pre[x], pe = pre[x + 1];
+        const uint64_t no = oe - ob, nn = pe - pb;
+        for (uint64_t i = lane_id(); i < no; i += 32) {
+            const uint2 e = old_ent[ob + i];
+            uint64_t lo = 0, hi = nn;   // new entries before e
+            while (lo < hi) {
+                const uint64_t mid = (lo + hi) >> 1;
+                const uint2 m = make_uint2(v2[pb + mid], (uint32_t)k2[pb + mid]);
+                if (ent_less(m, e)) lo = mid + 1;
+                else hi = mid;
+            }
+            out[nb + i + lo] = e;
+        }
+        for (uint64_t t = lane_id(); t < nn; t += 32) {
+            const uint2 e = make_uint2(v2[pb + t], (uint32_t)k2[pb + t]);
+            uint64_t lo = 0, hi = no;   // old entries before e
+            while (lo < hi) {
+                const uint64_t mid = (lo + hi) >> 1;
+                if (ent_less(old_ent[ob + mid], e)) lo = mid + 1;
+                else hi = mid;
+            }
+            out[nb + t + lo] = e;
+        }
+    }
+}
+
 // Largest tree/label ratio over the superstep's roots (hybrid switch rule,
 // distributed_memory/akiba.hpp:297-303), kept as an exact fraction.
 __global__ void ratio_max(const uint32_t *tsize, const uint32_t *tlab, const unsigned long long *next_root,
@@ -2526,6 +2599,8 @@ struct Build {
     uint64_t *off_a = nullptr, *off_b = nullptr;
     uint2 *ent_a = nullptr, *ent_b = nullptr;
     uint64_t ent_cap_a = 0, ent_cap_b = 0;
+    uint2 *dent_a = nullptr, *dent_b = nullptr;   // (distance, hub)-ordered copies
+    uint64_t dent_cap_a = 0, dent_cap_b = 0;
     uint64_t *nk0 = nullptr, *nk1 = nullptr;
     uint32_t *nv0 = nullptr, *nv1 = nullptr;
     uint64_t new_cap = 0;
@@ -2563,6 +2638,8 @@ struct Build {
         cudaFree(off_b);
         cudaFree(ent_a);
         cudaFree(ent_b);
+        cudaFree(dent_a);
+        cudaFree(dent_b);
         cudaFree(nk0);
         cudaFree(nk1);
         cudaFree(nv0);
@@ -2689,7 +2766,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     if ((rc = dalloc(&b.off_a, (size_t)b.nl + 1)) || (rc = dalloc(&b.off_b, (size_t)b.nl + 1)))
         return rc;
     CHL_CUDA(cudaMemsetAsync(b.off_a, 0, ((size_t)b.nl + 1) * 8, b.st));
-    if ((rc = ensure_ent(&b.ent_a, &b.ent_cap_a, 1))) return rc;
+    if ((rc = ensure_ent(&b.ent_a, &b.ent_cap_a, 1)) || (rc = ensure_ent(&b.dent_a, &b.dent_cap_a, 1))) return rc;
     if ((rc = dalloc(&b.cnt, (size_t)b.nl + 1)) || (rc = dalloc(&b.pre, (size_t)b.nl + 2))) return rc;
     CHL_CUDA(cudaMemsetAsync(b.cnt, 0, ((size_t)b.nl + 1) * 4, b.st));
     if ((rc = dalloc(&b.tsize, n)) || (rc = dalloc(&b.tlab, n))) return rc;
@@ -2790,6 +2867,9 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     // OUT criterion: measured slower on the 512/1024-square grids and RMAT
     // scale 18 (the extra loads outweigh the larger batches), so opt-in
     const int out_crit = opts.settle_rule == 2 ? 1 : 0;
+    // prune tests over a distance-ordered copy of the labels (lane items and
+    // the hashed root label only; the copy is merged at every commit)
+    const int dist_order = (prune_sched == 4 && root_probe == 2 && opts.prune_order != 1) ? 1 : 0;
 
     // superstep loop
     const double sf = opts.sf > 0 ? opts.sf : 32.0;
@@ -2873,6 +2953,8 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             ta.rank = b.rank;
             ta.l_off = b.off_a;
             ta.l_ent = b.ent_a;
+            ta.l_dent = b.dent_a;
+            ta.dist_order = dist_order;
             ta.r0 = r0;
             ta.r_end = r_end;
             // work-conserving extension (batch kernel): up to ext x the
@@ -2991,6 +3073,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         // array is sized for every new label before the chain (the clean
         // only removes labels).
         if ((rc = ensure_ent(&b.ent_b, &b.ent_cap_b, committed + M))) return rc;
+        if (dist_order && (rc = ensure_ent(&b.dent_b, &b.dent_cap_b, committed + M))) return rc;
         const bool clean_now = !plant_now && M > 0;
         auto chain = [&]() -> int {
             int rc2;
@@ -3029,13 +3112,26 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             copy_old_lists<<<cgrid, 256, 0, b.st>>>(b.off_a, b.ent_a, b.off_b, b.ent_b, b.nl);
             place_new<<<cgrid, 256, 0, b.st>>>(sk, sv, d_count, b.new_cap, b.hub_bits, r0, b.pre, b.off_a,
                                                b.off_b, b.ent_b);
+            if (dist_order) {
+                // the same labels by (list, distance, hub), merged into the
+                // distance-ordered copy (the sort is stable: equal distances
+                // keep hub order)
+                dist_keys<<<cgrid, 256, 0, b.st>>>(sk, sv, d_count, b.new_cap, b.hub_bits, r0, ak, av);
+                int par2 = 0;
+                if ((rc2 = radix_sort_pairs(ak, av, sk, sv, (const uint64_t *)d_count, b.new_cap,
+                                            b.key_bits - b.hub_bits + 32, b.tmp, b.tmp_bytes, b.st, &par2)))
+                    return rc2;
+                merge_dist_lists<<<cgrid, 256, 0, b.st>>>(b.off_a, b.dent_a, b.off_b, b.pre, par2 ? sk : ak,
+                                                          par2 ? sv : av, b.dent_b, b.nl);
+            }
             // longest committed list, for the next superstep's root staging
             CHL_CUDA(cudaMemsetAsync(&b.ctl->max_ratio_den, 0, 8, b.st));
             max_list_len<<<cgrid, 256, 0, b.st>>>(b.off_b, b.nl, &b.ctl->max_ratio_den);
             CHL_CUDA(cudaGetLastError());
             return CHL_OK;
         };
-        kernels += 3 * ((b.key_bits + 7) / 8) + (clean_now ? 9 : 0) + 8;
+        kernels += 3 * ((b.key_bits + 7) / 8) + (clean_now ? 9 : 0) + 8 +
+                   (dist_order ? 2 + 3 * ((b.key_bits - b.hub_bits + 32 + 7) / 8) : 0);
         CHL_CUDA(cudaEventRecord(ev_a, b.st));
         if (opts.use_graphs) {
             CHL_CUDA(cudaStreamBeginCapture(b.st, cudaStreamCaptureModeThreadLocal));
@@ -3071,6 +3167,10 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         std::swap(b.off_a, b.off_b);
         std::swap(b.ent_a, b.ent_b);
         std::swap(b.ent_cap_a, b.ent_cap_b);
+        if (dist_order) {
+            std::swap(b.dent_a, b.dent_b);
+            std::swap(b.dent_cap_a, b.dent_cap_b);
+        }
         CHL_CUDA(cudaMemcpyAsync(&hc, b.ctl, sizeof(hc), cudaMemcpyDeviceToHost, b.st));
         CHL_CUDA(cudaStreamSynchronize(b.st));
         M = hc.nlab;

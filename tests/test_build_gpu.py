@@ -174,7 +174,9 @@ def test_build_is_deterministic(P):
                {"superstep_extend": 16, "mode": 1, "first_superstep": 9},
                {"settle_rule": 2}, {"settle_rule": 2, "mode": 1}, {"settle_rule": 2, "prune_sched": 1},
                {"prune_sched": 4}, {"prune_sched": 4, "mode": 1}, {"prune_sched": 4, "root_stage": 64},
-               {"prune_sched": 4, "scan_order": 2, "root_probe": 1}):
+               {"prune_sched": 4, "scan_order": 2, "root_probe": 1},
+               {"prune_order": 1}, {"prune_order": 1, "mode": 1}, {"prune_order": 0, "mode": 1, "root_stage": 64},
+               {"first_superstep": 1, "growth": 0.01, "superstep_extend": 1}):
         b = P.build(g, order, sf=0.2, **kw).export()
         for x, y in zip(a, b):
             assert np.array_equal(x, y), kw
