@@ -159,7 +159,8 @@ enum chl_build_mode {
 
 typedef struct chl_build_opts {
     int32_t mode;         /* chl_build_mode                                  */
-    double sf;            /* superstep label budget factor (hhl -s), 0 = auto */
+    double sf;            /* superstep label budget factor (hhl -s), 0 = auto
+                             (32 on heavy-tailed graphs, 128 otherwise)   */
     double ps;            /* phase switch ratio tree/label (hhl -ps)          */
     int32_t autotune;     /* 1: pick superstep growth from graph statistics   */
     int32_t use_graphs;   /* 1: capture the per-superstep kernel chain in a
@@ -201,7 +202,7 @@ typedef struct chl_build_opts {
     uint32_t reserved[3];
 } chl_build_opts;
 
-/* Fill opts with the defaults (hybrid, sf 32, ps 1024, autotune on,
+/* Fill opts with the defaults (hybrid, sf auto, ps 1024, autotune on,
  * commit chain captured in a CUDA graph). */
 void chl_build_opts_default(chl_build_opts *opts);
 

@@ -412,7 +412,7 @@ class Labeling:
             self._h = None
 
 
-def build(g: Graph, order, mode: int = MODE_HYBRID, sf: float = 32.0, ps: float = 1024.0,
+def build(g: Graph, order, mode: int = MODE_HYBRID, sf: float = 0.0, ps: float = 1024.0,
           verbose: int = 0, max_warps: int = 0, autotune: int = 1, tree_algo: int = 0,
           first_superstep: int = 0, growth: float = 0.0, scan_order: int = 0,
           cta_roots: int = 0, use_graphs: Optional[int] = None, root_limit: int = 0,

@@ -2872,7 +2872,11 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     const int dist_order = (prune_sched == 4 && root_probe == 2 && opts.prune_order != 1) ? 1 : 0;
 
     // superstep loop
-    const double sf = opts.sf > 0 ? opts.sf : 32.0;
+    // label budget per superstep (the reference's sf * N); auto: 32 on
+    // heavy-tailed graphs, 128 on road-like ones, where larger supersteps
+    // pay off once prune tests stop at the distance cutoff (measured on the
+    // 512/1024-square grids and RMAT scale 20)
+    const double sf = opts.sf > 0 ? opts.sf : (heavy_tail ? 32.0 : 128.0);
     // label_limit = sf * N counts both sides' labels (shared_memory/hhl.cpp:65);
     // a symmetric build stores one side.
     const unsigned long long budget_base =
@@ -3259,7 +3263,7 @@ extern "C" void chl_build_opts_default(chl_build_opts *o) {
     if (!o) return;
     std::memset(o, 0, sizeof(*o));
     o->mode = CHL_MODE_HYBRID;
-    o->sf = 32.0;
+    o->sf = 0.0;
     o->ps = 1024.0;
     o->autotune = 1;
     o->use_graphs = 1;
