@@ -199,7 +199,17 @@ typedef struct chl_build_opts {
     int32_t prune_order;  /* label order scanned by prune tests: 0 auto
                              (a distance-ordered copy with lane items and the
                              hashed root label), 1 hub order                */
-    uint32_t reserved[3];
+    uint32_t label_cap;   /* new-label buffer entries per superstep: 0 auto
+                             (the label budget plus sides * n per tree still
+                             running when it is spent, within a quarter of
+                             free memory).  A superstep that overflows it is
+                             re-run with exactly the room it needed.        */
+    int32_t queue_split;  /* batched settle near/far queue: 0 auto (road-
+                             like graphs: a tree's queue above 1024 vertices
+                             is split, about 256 kept near; heavy-tailed
+                             ones: off), 1 off, q > 1: split above q (about
+                             q / 4 near); off with settle_rule 2            */
+    uint32_t reserved[1];
 } chl_build_opts;
 
 /* Fill opts with the defaults (hybrid, sf auto, ps 1024, autotune on,

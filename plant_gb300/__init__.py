@@ -53,7 +53,8 @@ class BuildOpts(C.Structure):
                 ("cta_roots", C.c_int32), ("root_limit", C.c_uint32), ("root_stage", C.c_uint32),
                 ("prune_sched", C.c_int32), ("root_probe", C.c_int32),
                 ("superstep_extend", C.c_int32), ("settle_rule", C.c_int32),
-                ("prune_order", C.c_int32), ("reserved", C.c_uint32 * 3)]
+                ("prune_order", C.c_int32), ("label_cap", C.c_uint32), ("queue_split", C.c_int32),
+                ("reserved", C.c_uint32 * 1)]
 
 
 class BuildStats(C.Structure):
@@ -417,7 +418,8 @@ def build(g: Graph, order, mode: int = MODE_HYBRID, sf: float = 0.0, ps: float =
           first_superstep: int = 0, growth: float = 0.0, scan_order: int = 0,
           cta_roots: int = 0, use_graphs: Optional[int] = None, root_limit: int = 0,
           root_stage: int = 0, prune_sched: int = 0, root_probe: int = 0,
-          superstep_extend: int = 0, settle_rule: int = 0, prune_order: int = 0) -> Labeling:
+          superstep_extend: int = 0, settle_rule: int = 0, prune_order: int = 0,
+          label_cap: int = 0, queue_split: int = 0) -> Labeling:
     o = _u32(order)
     opts = BuildOpts()
     lib().chl_build_opts_default(C.byref(opts))
@@ -441,6 +443,8 @@ def build(g: Graph, order, mode: int = MODE_HYBRID, sf: float = 0.0, ps: float =
     opts.superstep_extend = superstep_extend
     opts.settle_rule = settle_rule
     opts.prune_order = prune_order
+    opts.label_cap = label_cap
+    opts.queue_split = queue_split
     h = C.c_void_p()
     _check(lib().chl_build(g._h, _ptr(o, _U32P), len(o), C.byref(opts), C.byref(h)), "build")
     return Labeling(h)

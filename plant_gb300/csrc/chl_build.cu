@@ -75,7 +75,7 @@ struct BuildCtl {
     unsigned long long running;     // trees of the nominal root range in progress
     unsigned long long close_at;    // first root refused after the extension closed
     unsigned long long cyc[8];      // per-phase SM cycles summed over warps (diagnostics)
-    unsigned long long cnt[4];      // frontier entries scanned, rounds, settle calls, far entries scanned
+    unsigned long long cnt[4];      // frontier entries scanned, rounds, settle calls, far pile entries read
 };
 
 struct TreeArgs {
@@ -122,6 +122,8 @@ struct TreeArgs {
     const uint16_t *win16[2];       // win clamped to 65535 (a valid lower bound)
     uint2 *ws_fq;                   // per warp slot: queue log (vertex, distance)
     uint32_t fq_cap;                // log entries per slot
+    uint32_t near_on;               // batch kernel: queue size that starts the near/far split (0: never)
+    uint32_t near_target;           // batch kernel: near entries aimed at per refill
 };
 
 // Phase-timing clock: with CHL_PHASE_TIMING it is also a compiler memory
@@ -646,7 +648,9 @@ __device__ __forceinline__ uint32_t sat_add(uint32_t x, uint32_t y) {
 __device__ __forceinline__ uint32_t fetch_root(const TreeArgs &a, bool &nominal) {
     nominal = false;
     const unsigned long long used = *(volatile unsigned long long *)&a.ctl->nlab;
-    if (used >= a.budget) return kInf;
+    // no new tree once the budget is spent, or once the label buffer is full
+    // (the superstep's range is then re-run with a larger buffer)
+    if (used >= a.budget || used >= a.out_cap) return kInf;
     const unsigned long long t = atomicAdd(&a.ctl->next_root, 1ull);
     if (t & kClosed) return kInf;
     if (t < a.r_end) {
@@ -1067,11 +1071,13 @@ batch_kernel(TreeArgs a) {
     uint32_t *vis = a.ws_vis + (size_t)slot * a.n;
     // queue as two arrays: a round reads `front` and writes the vertices it
     // keeps, and those its relaxations add, to `fnext`; then they swap
-    uint32_t *front = a.ws_front + (size_t)slot * 2 * a.n;
+    uint32_t *front = a.ws_front + (size_t)slot * 3 * a.n;
     uint32_t *fnext = front + a.n;
+    // far pile of the near/far queue (see the round loop)
+    uint32_t *pile = fnext + a.n;
     unsigned long long c_vis = 0, c_reads = 0, c_arcs = 0;
     long long cyc[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // phase cycles (diagnostics)
-    unsigned long long dcnt[4] = {0, 0, 0, 0};      // scanned, rounds, settles, far entries
+    unsigned long long dcnt[4] = {0, 0, 0, 0};      // scanned, rounds, settles, far pile entries
     const long long k_start = phase_clock();
     const uint32_t g = lane >> 2, sub = lane & 3;
     const uint32_t gmask = 0xFu << (4 * g);
@@ -1084,9 +1090,9 @@ batch_kernel(TreeArgs a) {
         const size_t s0 = (size_t)blockIdx.x * kWarpsPerBlock;
         uint32_t *key0 = a.ws_key + s0 * a.n;
         uint32_t *vis0 = a.ws_vis + s0 * a.n;
-        uint32_t *f0 = a.ws_front + s0 * 2 * a.n;
+        uint32_t *f0 = a.ws_front + s0 * 3 * a.n;
         uint32_t *f1 = f0 + a.n;
-        uint32_t *f2 = a.ws_front + (s0 + 1) * 2 * a.n;
+        uint32_t *f2 = a.ws_front + (s0 + 1) * 3 * a.n;
         while (true) {
             __syncthreads();
             if (threadIdx.x == 0) {
@@ -1306,6 +1312,14 @@ batch_kernel(TreeArgs a) {
             __syncwarp();
             cyc[5] += phase_clock() - tr0;
             uint32_t nvis = 1, nf = 1, nn = 0;   // queue sizes in front and fnext
+            // Near/far queue.  A large queue is split at a threshold thr:
+            // keys below it are queued in front/fnext and scanned every
+            // round, the rest in the far pile, read only when the near
+            // vertices run out.  thr == kInf: no split (all queued near).
+            uint32_t npile = 0;         // far pile entries (stale ones included)
+            uint32_t thr = kInf;
+            uint32_t pmin = kInf;       // per lane: lower bound of the live far keys
+            uint32_t delta = 0;         // threshold step (0: choose at the next refill)
             int ql = 1;
             uint32_t dmin = 0;          // smallest queued distance (exact, see below)
             bool stop = false;
@@ -1697,18 +1711,35 @@ batch_kernel(TreeArgs a) {
 #pragma unroll
                     for (int c = 0; c < RC; ++c) {
                         const bool fresh = upd[c] && old[c] == kInf;
-                        const uint32_t fm = __ballot_sync(kFull, fresh);
-                        if (fresh) {
+                        // queued near: a new key below thr, or a far vertex
+                        // whose key drops below it (its far entry goes stale)
+                        const uint32_t dk = nk[c] >> 1;
+                        const bool to_near = upd[c] && dk < thr && (old[c] == kInf || (old[c] >> 1) >= thr);
+                        const uint32_t fm = __ballot_sync(kFull, to_near);
+                        if (to_near) {
                             const uint32_t o = __popc(fm & lanemask_lt());
-                            if (nn + o < a.n && nvis + o < a.n) {
-                                fnext[nn + o] = w[c];
-                                vis[nvis + o] = w[c];
-                            } else {
-                                a.ctl->err = 2;
-                            }
+                            if (nn + o < a.n) fnext[nn + o] = w[c];
+                            else a.ctl->err = 2;
                         }
                         nn = min(nn + __popc(fm), a.n);
-                        nvis = min(nvis + __popc(fm), a.n);
+                        const uint32_t vm = thr == kInf ? fm : __ballot_sync(kFull, fresh);
+                        if (fresh) {
+                            const uint32_t o = __popc(vm & lanemask_lt());
+                            if (nvis + o < a.n) vis[nvis + o] = w[c];
+                            else a.ctl->err = 2;
+                        }
+                        nvis = min(nvis + __popc(vm), a.n);
+                        if (thr != kInf) {
+                            if (upd[c] && dk >= thr) pmin = min(pmin, dk);
+                            const bool to_far = fresh && dk >= thr;
+                            const uint32_t pm = __ballot_sync(kFull, to_far);
+                            if (to_far) {
+                                const uint32_t o = __popc(pm & lanemask_lt());
+                                if (npile + o < a.n) pile[npile + o] = w[c];
+                                else a.ctl->err = 2;
+                            }
+                            npile = min(npile + __popc(pm), a.n);
+                        }
                         if (PLANT) {
                             int dq = 0;
                             if (upd[c]) dq = (int)(nk[c] & 1u) - (old[c] == kInf ? 0 : (int)(old[c] & 1u));
@@ -1722,7 +1753,79 @@ batch_kernel(TreeArgs a) {
                 cyc[4] += phase_clock() - tc3;
             };
 
-            while (nf > 0 && !stop) {
+            // Refill the (empty) near queue from the far pile: entries whose
+            // key is below the old threshold are stale (their vertex was
+            // queued near and is settled), entries below the new threshold
+            // thr = (their minimum) + delta move near, the rest stay,
+            // compacted in place.  From the second pass on the minimum is
+            // exact, so a refill takes at most two passes.
+            auto refill = [&]() {
+                const long long tf0 = phase_clock();
+                uint32_t lo = __reduce_min_sync(kFull, pmin);
+                if (delta == 0) {
+                    // first refill of the split: delta for about near_target
+                    // entries, taking the keys as spread evenly over [min, max]
+                    uint32_t mn = kInf, mx = 0;
+                    for (uint32_t i = lane; i < npile; i += 32) {
+                        const uint32_t k = __ldcg(&key[pile[i]]) >> 1;
+                        mn = min(mn, k);
+                        mx = max(mx, k);
+                    }
+                    mn = __reduce_min_sync(kFull, mn);
+                    mx = __reduce_max_sync(kFull, mx);
+                    lo = mn;
+                    uint64_t d = (uint64_t)(mx - min(mn, mx)) * a.near_target / max(npile, 1u);
+                    if (d < 1) d = 1;
+                    if (d > 0x7FFFFFFFull) d = 0x7FFFFFFFull;
+                    delta = (uint32_t)d;
+                    if (kPhaseTiming) dcnt[3] += npile;
+                }
+                for (int pass = 0; pass < 4 && nf == 0 && npile > 0; ++pass) {
+                    const uint32_t t_old = thr;
+                    thr = sat_add(lo, delta);
+                    uint32_t keep = 0, moved = 0, kmin = kInf, nmin = kInf;
+                    if (kPhaseTiming) dcnt[3] += npile;
+                    for (uint32_t b0 = 0; b0 < npile; b0 += 32) {
+                        const uint32_t i = b0 + lane;
+                        const bool valid = i < npile;
+                        const uint32_t x = valid ? pile[i] : 0u;
+                        const uint32_t k = valid ? (__ldcg(&key[x]) >> 1) : kInf;
+                        const bool live = valid && k >= t_old;
+                        const bool nr = live && k < thr;
+                        const bool kp = live && !nr;
+                        const uint32_t nm = __ballot_sync(kFull, nr);
+                        const uint32_t km = __ballot_sync(kFull, kp);
+                        // every lane has read its entry (ballots above), and
+                        // a kept entry moves only to a lower index
+                        if (nr) {
+                            front[moved + __popc(nm & lanemask_lt())] = x;
+                            nmin = min(nmin, k);
+                        }
+                        if (kp) {
+                            pile[keep + __popc(km & lanemask_lt())] = x;
+                            kmin = min(kmin, k);
+                        }
+                        moved += __popc(nm);
+                        keep += __popc(km);
+                    }
+                    __syncwarp();
+                    npile = keep;
+                    nf = moved;
+                    lo = __reduce_min_sync(kFull, kmin);
+                    dmin = __reduce_min_sync(kFull, nmin);   // far keys are >= thr
+                    pmin = lane == 0 ? lo : kInf;
+                    if (moved < a.near_target / 4) delta = delta < 0x40000000u ? 2u * delta : 0x7FFFFFFFu;
+                    else if (moved > 4 * a.near_target) delta = max(delta / 2, 1u);
+                }
+                if (nf == 0 && npile > 0) a.ctl->err = 2;   // not reached: see above
+                cyc[0] += phase_clock() - tf0;
+            };
+
+            while ((nf > 0 || npile > 0) && !stop) {
+                if (nf == 0) {
+                    refill();
+                    if (nf == 0) break;
+                }
                 // One round: walk the queue once.  Vertices with
                 // d < dmin + win are final and go to the batch (settled
                 // whenever it fills); the rest go to fnext, where the
@@ -1743,8 +1846,6 @@ batch_kernel(TreeArgs a) {
                     const bool take = valid && ((uint64_t)(kx >> 1) < (uint64_t)dmin + wx ||
                                                 (out_ok && (kx >> 1) < omin));
                     const uint32_t tm = __ballot_sync(kFull, take);
-                    if (kPhaseTiming)   // queued entries at least 1024 above the minimum
-                        dcnt[3] += __popc(__ballot_sync(kFull, valid && (kx >> 1) >= dmin + 1024u));
                     if (take) {
                         const uint32_t at = nb + __popc(tm & lanemask_lt());
                         s_bv[at] = x;
@@ -1796,6 +1897,17 @@ batch_kernel(TreeArgs a) {
                 nf = nn;
                 dmin = __reduce_min_sync(kFull, dnext);
                 omin = __reduce_min_sync(kFull, onext);
+                if (thr == kInf && nf > a.near_on && a.near_on) {
+                    // the queue grew large: all of it goes to the far pile,
+                    // and the next refill splits it
+                    uint32_t *t = pile;
+                    pile = front;
+                    front = t;
+                    npile = nf;
+                    nf = 0;
+                    thr = 0;
+                    delta = 0;
+                }
             }
             c_vis += t_size;
             const long long tz0 = phase_clock();
@@ -2662,9 +2774,12 @@ struct Build {
     }
 };
 
+// New-label buffers with room for `need` entries (their contents are dead
+// between supersteps).  An overflowed superstep counts every label it tried
+// to append, so its re-run needs exactly that many: no doubling.
 int grow_new(Build &b, uint64_t need) {
     if (need <= b.new_cap) return CHL_OK;
-    uint64_t cap = std::max<uint64_t>(need, b.new_cap * 2);
+    const uint64_t cap = need;
     cudaFree(b.nk0);
     cudaFree(b.nk1);
     cudaFree(b.nv0);
@@ -2771,7 +2886,8 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     CHL_CUDA(cudaMemsetAsync(b.cnt, 0, ((size_t)b.nl + 1) * 4, b.st));
     if ((rc = dalloc(&b.tsize, n)) || (rc = dalloc(&b.tlab, n))) return rc;
     if ((rc = dalloc(&b.ctl, 1))) return rc;
-    if ((rc = grow_new(b, std::max<uint64_t>(4ull * n, 1u << 20)))) return rc;
+    if ((rc = grow_new(b, opts.label_cap ? (uint64_t)opts.label_cap : std::max<uint64_t>(4ull * n, 1u << 20))))
+        return rc;
 
     // workspace: one slot per resident warp
     const int sms = device_sms();
@@ -2805,7 +2921,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             b.fhead[1] = b.fhead[0];
         }
     }
-    const size_t per_slot = (size_t)n * (use_settle ? 24 : use_batch ? 16 : (unit ? 8 : 20));
+    const size_t per_slot = (size_t)n * (use_settle ? 24 : use_batch ? 20 : (unit ? 8 : 20));
     uint32_t want = (uint32_t)sms * 48;   // 12 blocks of 4 warps per SM at most
     if (opts.max_warps) want = std::min<uint32_t>(want, opts.max_warps);
     const size_t ws_budget = free_b / 3;
@@ -2819,7 +2935,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         b.fq_cap = (uint32_t)std::min<uint64_t>(2ull * n + 64, 0xFFFFFFF0ull);
         if ((rc = dalloc(&b.ws_fq, slots * b.fq_cap))) return rc;
     } else if (use_batch) {
-        if ((rc = dalloc(&b.ws_front, slots * 2 * (size_t)n))) return rc;   // front + fnext
+        if ((rc = dalloc(&b.ws_front, slots * 3 * (size_t)n))) return rc;   // front, fnext, far pile
     } else if (!unit) {
         if ((rc = dalloc(&b.ws_pos, slots * n)) || (rc = dalloc(&b.ws_heap, slots * n))) return rc;
     }
@@ -2881,6 +2997,19 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     // a symmetric build stores one side.
     const unsigned long long budget_base =
         (unsigned long long)std::max(1.0, sf * (double)n / (b.sides == 1 ? 2.0 : 1.0));
+    if (opts.label_cap == 0) {
+        // Room for every new label of a superstep: the budget plus what the
+        // trees still running when it is spent can add (at most sides * n
+        // each), so that a superstep does not overflow and run twice.  At
+        // most a quarter of the free memory (36 bytes per entry: two key and
+        // two value arrays for the sort, the clean's flags and prefix);
+        // beyond that an overflow re-runs the superstep's root range.
+        size_t fr = 0, tot = 0;
+        CHL_CUDA(cudaMemGetInfo(&fr, &tot));
+        const uint64_t want = (uint64_t)budget_base + (uint64_t)b.warps * b.sides * n;
+        const uint64_t fit = (uint64_t)(fr / 4 / 36);
+        if ((rc = grow_new(b, std::min(want, fit)))) return rc;
+    }
     bool do_plant = opts.mode != CHL_MODE_GLL;
     bool switch_open = opts.mode == CHL_MODE_HYBRID;
     uint32_t r0 = 0;
@@ -3007,6 +3136,19 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             for (int s2 = 0; s2 < 2; ++s2) ta.win16[s2] = b.dg->win16[s2];
             ta.ws_fq = b.ws_fq;
             ta.fq_cap = b.fq_cap;
+            // near/far queue (batch kernel; the OUT criterion needs the whole
+            // queue every round).  Auto: split above 1024 queued vertices on
+            // road-like graphs, whose queues are long rings of close keys
+            // (1.25x faster builds of the 512/1024-square grids); off on
+            // heavy-tailed ones, whose few-level queues gain nothing (RMAT
+            // scale 20: 4% slower with it)
+            ta.near_on = 0;
+            ta.near_target = 1;
+            const int qs = opts.queue_split ? opts.queue_split : (heavy_tail ? 1 : 1024);
+            if (use_batch && !out_crit && qs > 1) {
+                ta.near_on = (uint32_t)qs;
+                ta.near_target = std::max<uint32_t>(1, ta.near_on / 4);
+            }
             void (*kern)(TreeArgs);
             if (use_settle) {
                 if (unit) kern = plant_now ? settle_kernel<true, true> : settle_kernel<true, false>;
@@ -3200,8 +3342,8 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
                     100 * hc.cyc[4] / tot, 100 * hc.cyc[5] / tot, 100 * hc.cyc[6] / tot, tot);
             fprintf(stderr, "  frontier entries scanned %llu rounds %llu settles %llu (per visit: scanned %.2f)\n",
                     hc.cnt[0], hc.cnt[1], hc.cnt[2], (double)hc.cnt[0] / std::max<unsigned long long>(1, hc.visits));
-            fprintf(stderr, "  scanned entries at least 1024 above the queue minimum: %llu (%.1f%%)\n", hc.cnt[3],
-                    100.0 * hc.cnt[3] / std::max<unsigned long long>(1, hc.cnt[0]));
+            fprintf(stderr, "  far pile entries read by refills: %llu (%.1f%% of the frontier entries scanned)\n",
+                    hc.cnt[3], 100.0 * hc.cnt[3] / std::max<unsigned long long>(1, hc.cnt[0]));
         }
         if (opts.verbose >= 2)
             fprintf(stderr, "  tree size max %llu mean %.1f\n", tstat[0],

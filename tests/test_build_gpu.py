@@ -57,6 +57,24 @@ def test_config1_grid_matches_oracle(P, O, mode, sf, algo):
     assert st["supersteps"] >= 1 and st["labels"] == ref.total()
 
 
+@pytest.mark.parametrize("split", [2, 16, 300])
+@pytest.mark.parametrize("kind", ["grid", "rmat"])
+def test_queue_split_matches_oracle(P, O, split, kind):
+    # trees whose queues are split into near and far piles give the oracle's labels
+    if kind == "grid":
+        g = P.Graph.grid(120, 120, highways=30, seed=6)
+        order = P.Order.degree(g, seed=3)
+    else:
+        g = P.Graph.rmat(12, 8, seed=8)
+        order = P.Order.degree(g, seed=3)
+    off, head, ln = g.csr(True)
+    og = O.OGraph.from_csr(g.get_n(), off, head, ln)
+    ref, _ = O.gll(og, order)
+    for mode in (MODES["hybrid"], MODES["gll"]):
+        L = P.build(g, order, mode=mode, queue_split=split)
+        assert same_labels(L, ref, g.get_n()), (split, mode)
+
+
 @pytest.mark.parametrize("mode", list(MODES))
 @pytest.mark.parametrize("algo", list(ALGOS))
 def test_rmat_unit_lengths_matches_oracle(P, O, mode, algo):
@@ -115,7 +133,8 @@ def test_directed_power_law_matches_oracle(P, O, tmp_path):
     og = O.OGraph.read_dimacs(p)
     order = og.degree_order(5)
     ref, _ = O.gll(og, order)
-    for kw in ({}, {"mode": MODES["gll"]}, {"first_superstep": 100, "growth": 0.5}):
+    for kw in ({"queue_split": 64}, {"mode": MODES["gll"], "queue_split": 16}, {"label_cap": 5000},
+               {}, {"mode": MODES["gll"]}, {"first_superstep": 100, "growth": 0.5}):
         L = P.build(g, order, **kw)
         assert same_labels(L, ref, n), kw
     pairs = P.generate_query(20000, n, seed=3)
@@ -176,7 +195,16 @@ def test_build_is_deterministic(P):
                {"prune_sched": 4}, {"prune_sched": 4, "mode": 1}, {"prune_sched": 4, "root_stage": 64},
                {"prune_sched": 4, "scan_order": 2, "root_probe": 1},
                {"prune_order": 1}, {"prune_order": 1, "mode": 1}, {"prune_order": 0, "mode": 1, "root_stage": 64},
-               {"first_superstep": 1, "growth": 0.01, "superstep_extend": 1}):
+               {"first_superstep": 1, "growth": 0.01, "superstep_extend": 1},
+               # new-label buffers far below a superstep's labels: every
+               # overflowed superstep re-runs its root range
+               {"label_cap": 1000}, {"label_cap": 1000, "mode": 1}, {"label_cap": 4000, "tree_algo": 1},
+               {"label_cap": 3000, "tree_algo": 3}, {"label_cap": 2000, "cta_roots": 1 << 30},
+               # near/far queue split at tiny queue sizes (refills, stale
+               # far entries, threshold doubling and halving), and off
+               {"queue_split": 1}, {"queue_split": 2}, {"queue_split": 8}, {"queue_split": 8, "mode": 1},
+               {"queue_split": 33, "first_superstep": 1, "growth": 0.05}, {"queue_split": 200},
+               {"queue_split": 8, "settle_rule": 2}, {"queue_split": 8, "cta_roots": 5}):
         b = P.build(g, order, sf=0.2, **kw).export()
         for x, y in zip(a, b):
             assert np.array_equal(x, y), kw
