@@ -74,7 +74,8 @@ struct BuildCtl {
     unsigned long long max_ratio_den;
     unsigned long long running;     // trees of the nominal root range in progress
     unsigned long long close_at;    // first root refused after the extension closed
-    unsigned long long cyc[8];      // per-phase SM cycles summed over warps (diagnostics)
+    unsigned long long cyc[10];     // per-phase SM cycles summed over warps (diagnostics; [8]: prune
+                                    // item selection, part of [2]; [9]: selection passes, a count)
     unsigned long long cnt[4];      // frontier entries scanned, rounds, settle calls, far pile entries read
 };
 
@@ -1076,7 +1077,7 @@ batch_kernel(TreeArgs a) {
     // far pile of the near/far queue (see the round loop)
     uint32_t *pile = fnext + a.n;
     unsigned long long c_vis = 0, c_reads = 0, c_arcs = 0;
-    long long cyc[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // phase cycles (diagnostics)
+    long long cyc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};   // phase cycles (diagnostics)
     unsigned long long dcnt[4] = {0, 0, 0, 0};      // scanned, rounds, settles, far pile entries
     const long long k_start = phase_clock();
     const uint32_t g = lane >> 2, sub = lane & 3;
@@ -1209,6 +1210,57 @@ batch_kernel(TreeArgs a) {
                 }
                 if (rhash.Th) rhash.hlast = a.l_ent[rb + rhash.Th - 1].x;
             }
+            // Prune test of one lane's 16 consecutive entries of the
+            // distance-ordered L(u) against the hashed root label (the default
+            // configuration).  vm marks the entries that belong to the list;
+            // an entry beyond d(r, u) witnesses nothing and, the list being
+            // in distance order, marks the list exhausted.
+            auto test16d = [&](const uint4 (&q)[8], uint32_t vm, uint32_t gdj, bool &exhausted) -> bool {
+                bool hit = false;
+                uint64_t v[16];
+                uint32_t sl[16];
+                uint32_t pend = 0;
+#pragma unroll
+                for (int t = 0; t < 16; ++t) {
+                    const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
+                    const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
+                    const bool in = (vm >> t) & 1u;
+                    v[t] = kSlotEmpty;
+                    sl[t] = 0;
+                    if (in && dd > gdj) exhausted = true;
+                    if (in && dd <= gdj && rhash.Th && hh <= rhash.hlast) {
+                        sl[t] = slot_of(hh, a.hash_shift);
+                        v[t] = s_tab[sl[t]];
+                        pend |= 1u << t;
+                    }
+                }
+                if (rhash.Th < R) {
+                    // hubs past the hashed prefix: binary search of the rest
+#pragma unroll
+                    for (int t = 0; t < 16; ++t) {
+                        const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
+                        const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
+                        if (((vm >> t) & 1u) && dd <= gdj && !(rhash.Th && hh <= rhash.hlast)) {
+                            uint32_t dr;
+                            if (rhash.find_tail(hh, dr) && dr + dd <= gdj) hit = true;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int t = 0; t < 16; ++t) {
+                    if (!(pend >> t & 1u)) continue;
+                    const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
+                    const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
+                    uint64_t w = v[t];
+                    uint32_t z = sl[t];
+                    while (w != kSlotEmpty && (uint32_t)(w >> 32) != hh) {
+                        z = (z + 1) & rhash.mask;
+                        w = s_tab[z];
+                    }
+                    if (w != kSlotEmpty && (uint32_t)w + dd <= gdj) hit = true;
+                }
+                return hit;
+            };
             // Prune test of one lane's (up to) 8 consecutive entries of L(u)
             // (entries [e0, e0 + 8) of which [glb, gle) belong to the list):
             // does some (h, dd) with the root's (h, dr) give dr + dd <= gdj?
@@ -1401,7 +1453,9 @@ batch_kernel(TreeArgs a) {
                     while (true) {
                         // the next (up to) G live items, in item order
                         uint32_t got = 0;
+                        const long long tsel = phase_clock();
                         while (got < G && cursor < nitems) {
+                            if (kPhaseTiming) cyc[9]++;
                             const uint32_t i = cursor + lane;
                             bool live = false;
                             uint32_t item = 0;
@@ -1426,6 +1480,7 @@ batch_kernel(TreeArgs a) {
                             got += take;
                         }
                         __syncwarp();
+                        cyc[8] += phase_clock() - tsel;
                         if (got == 0) break;
                         if (a.lane_items) {
                             // one 16-entry item per lane (8 loads of one
@@ -1442,6 +1497,22 @@ batch_kernel(TreeArgs a) {
                                 const uint32_t ck = (a.scan_back && !a.dist_order) ? s_nch[lj] - 1 - c : c;
                                 const uint64_t e0 = (glb & ~1ull) + 16ull * ck;
                                 uint4 q[8];
+                                if (a.dist_order && a.hash_slots) {
+                                    // entries [lo, hi) of the 16 belong to the list:
+                                    // lo is 1 only in chunk 0 of an odd start, and a
+                                    // live item has e0 < gle
+                                    const uint32_t lo = (uint32_t)(glb - min(glb, e0));
+                                    const uint64_t span = gle - e0;
+                                    const uint32_t hi = span < 16 ? (uint32_t)span : 16u;
+                                    const uint32_t vm = ((1u << hi) - 1u) & ~((1u << lo) - 1u);
+#pragma unroll
+                                    for (int t = 0; t < 8; ++t) {
+                                        q[t] = make_uint4(0, 0, 0, 0);
+                                        if ((vm >> (2 * t)) & 3u) q[t] = *(const uint4 *)(lscan + e0 + 2 * t);
+                                    }
+                                    hit = test16d(q, vm, gdj, exhausted);
+                                    nread += 16;
+                                } else {
 #pragma unroll
                                 for (int t = 0; t < 8; ++t) {
                                     q[t] = make_uint4(0, 0, 0, 0);
@@ -1449,7 +1520,8 @@ batch_kernel(TreeArgs a) {
                                 }
                                 hit = test8(q, e0, glb, gle, gdj);
                                 nread += 16;
-                                if (a.dist_order && !hit) {
+                                }
+                                if (a.dist_order && !a.hash_slots && !hit) {
                                     // distance order: once the chunk's last entry is
                                     // beyond d, no later chunk can hold a witness
                                     const uint64_t last = min(e0 + 15, gle - 1);
@@ -1936,7 +2008,7 @@ batch_kernel(TreeArgs a) {
         if (kPhaseTiming) {
             cyc[7] = phase_clock() - k_start;   // whole residency of the warp
 #pragma unroll
-            for (int i = 0; i < 8; ++i) atomicAdd(&a.ctl->cyc[i], (unsigned long long)cyc[i]);
+            for (int i = 0; i < 10; ++i) atomicAdd(&a.ctl->cyc[i], (unsigned long long)cyc[i]);
 #pragma unroll
             for (int i = 0; i < 4; ++i) atomicAdd(&a.ctl->cnt[i], dcnt[i]);
         }
@@ -3340,6 +3412,9 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
                             "stage %.1f%% reset %.1f%% (sum of warp residencies %.3g cycles)\n",
                     100 * hc.cyc[0] / tot, 100 * hc.cyc[1] / tot, 100 * hc.cyc[2] / tot, 100 * hc.cyc[3] / tot,
                     100 * hc.cyc[4] / tot, 100 * hc.cyc[5] / tot, 100 * hc.cyc[6] / tot, tot);
+            fprintf(stderr, "  prune item selection %.1f%% of warp cycles, %llu passes (%.2f per visit)\n",
+                    100 * hc.cyc[8] / tot, hc.cyc[9],
+                    (double)hc.cyc[9] / std::max<unsigned long long>(1, hc.visits));
             fprintf(stderr, "  frontier entries scanned %llu rounds %llu settles %llu (per visit: scanned %.2f)\n",
                     hc.cnt[0], hc.cnt[1], hc.cnt[2], (double)hc.cnt[0] / std::max<unsigned long long>(1, hc.visits));
             fprintf(stderr, "  far pile entries read by refills: %llu (%.1f%% of the frontier entries scanned)\n",
