@@ -160,7 +160,7 @@ enum chl_build_mode {
 typedef struct chl_build_opts {
     int32_t mode;         /* chl_build_mode                                  */
     double sf;            /* superstep label budget factor (hhl -s), 0 = auto
-                             (32 on heavy-tailed graphs, 128 otherwise)   */
+                             (32 on heavy-tailed graphs, 1024 otherwise)  */
     double ps;            /* phase switch ratio tree/label (hhl -ps)          */
     int32_t autotune;     /* 1: pick superstep growth from graph statistics   */
     int32_t use_graphs;   /* 1: capture the per-superstep kernel chain in a

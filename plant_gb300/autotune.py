@@ -29,7 +29,7 @@ DEFAULT_CACHE = os.environ.get(
 
 FIRST = (0, 256, 1024, 4096)      # 0: the built-in choice from graph statistics
 GROWTH = (0.0, 0.5, 1.0, 2.0)     # 0.0: built-in
-SF = (0.0, 32.0, 128.0, 256.0)    # label budget per superstep (x n); 0.0: built-in
+SF = (0.0, 32.0, 128.0, 1024.0)   # label budget per superstep (x n); 0.0: built-in
 CTA = (-1, 64)                    # block-per-tree roots per superstep
 
 

@@ -3061,10 +3061,14 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
 
     // superstep loop
     // label budget per superstep (the reference's sf * N); auto: 32 on
-    // heavy-tailed graphs, 128 on road-like ones, where larger supersteps
-    // pay off once prune tests stop at the distance cutoff (measured on the
-    // 512/1024-square grids and RMAT scale 20)
-    const double sf = opts.sf > 0 ? opts.sf : (heavy_tail ? 32.0 : 128.0);
+    // heavy-tailed graphs, 1024 on road-like ones.  On road-like graphs a
+    // superstep lasts as long as its largest tree, so fewer, larger
+    // supersteps pay off once the near/far queue and the distance cutoff
+    // keep the less-pruned trees cheap; from 1024 on the growth schedule,
+    // not the budget, sets their size (measured on the 512/1024-square
+    // grids: 1024 and unbounded within 1%, 128 1.27x slower; RMAT scale
+    // 20: 16-64 within 3%)
+    const double sf = opts.sf > 0 ? opts.sf : (heavy_tail ? 32.0 : 1024.0);
     // label_limit = sf * N counts both sides' labels (shared_memory/hhl.cpp:65);
     // a symmetric build stores one side.
     const unsigned long long budget_base =

@@ -6,7 +6,7 @@
 //   -o <order>   order file
 //   -l <labels>  write labels (reference text layout)
 //   -s <sf>      superstep label budget sf*N (default: chosen from the
-//                graph, 32 heavy-tailed / 128 road-like; labels are the same)
+//                graph, 32 heavy-tailed / 1024 road-like; labels are the same)
 //   -p <threads> accepted for compatibility (the GPU decides its own)
 //   -paraPLL     accepted, ignored (as in the reference)
 //   -ps <ratio>  PLaNT -> pruned phase switch ratio (default 1024)
