@@ -2801,7 +2801,8 @@ struct Build {
     void *tmp = nullptr;
     size_t tmp_bytes = 0;
     cudaStream_t st = nullptr;
-    uint32_t warps = 0;
+    uint32_t warps = 0;   // warps the schedule is sized for
+    uint32_t slots = 0;   // warp slots launched (workspace slots)
     uint32_t rcap = 0;
     uint32_t auto_stage = 2048;              // default root-label staging (batch kernel)
     uint4 *farc[2] = {nullptr, nullptr};     // (head, length, rank[head], 0) per arc
@@ -3000,7 +3001,20 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     uint32_t fit = (uint32_t)std::max<size_t>(1, ws_budget / std::max<size_t>(per_slot, 1));
     b.warps = std::max<uint32_t>(kWarpsPerBlock, std::min(want, fit));
     b.warps = (b.warps / kWarpsPerBlock) * kWarpsPerBlock;
-    const size_t slots = b.warps;
+    if (use_batch) {
+        // Only the blocks resident from the start build trees: a block
+        // leaves when no root is left for the superstep, and every refusal
+        // of a root is final for it.  The grid and the workspace cover
+        // those alone (b.warps still sets the first superstep's size).
+        int nbo = 0;
+        CHL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &nbo, unit ? batch_kernel<true, true> : batch_kernel<false, true>, kWarpsPerBlock * 32, 0));
+        const uint32_t resident = (uint32_t)std::max(nbo, 1) * (uint32_t)sms * kWarpsPerBlock;
+        b.slots = std::min(b.warps, resident);
+    } else {
+        b.slots = b.warps;
+    }
+    const size_t slots = b.slots;
     if ((rc = dalloc(&b.ws_key, slots * n)) || (rc = dalloc(&b.ws_vis, slots * n))) return rc;
     CHL_CUDA(cudaMemsetAsync(b.ws_key, 0xFF, slots * n * 4, b.st));
     if (use_settle) {
@@ -3082,7 +3096,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         // beyond that an overflow re-runs the superstep's root range.
         size_t fr = 0, tot = 0;
         CHL_CUDA(cudaMemGetInfo(&fr, &tot));
-        const uint64_t want = (uint64_t)budget_base + (uint64_t)b.warps * b.sides * n;
+        const uint64_t want = (uint64_t)budget_base + (uint64_t)b.slots * b.sides * n;
         const uint64_t fit = (uint64_t)(fr / 4 / 36);
         if ((rc = grow_new(b, std::min(want, fit)))) return rc;
     }
@@ -3186,7 +3200,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             ta.ws_heap = b.ws_heap;
             ta.ctl = b.ctl;
             ta.rcap = b.rcap;
-            const int blocks = (int)(b.warps / kWarpsPerBlock);
+            const int blocks = (int)(b.slots / kWarpsPerBlock);
             for (int s2 = 0; s2 < 2; ++s2) ta.win[s2] = b.dg->win[s2];
             for (int s2 = 0; s2 < 2; ++s2) ta.wout[s2] = b.dg->wout[s2];
             ta.out_crit = out_crit;
