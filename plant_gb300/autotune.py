@@ -1,14 +1,15 @@
 """Schedule autotuner for the label build.
 
-The build's speed depends on four schedule knobs: the roots in the first
-superstep, the superstep growth factor, the label budget per superstep, and
-how many of a superstep's first roots are built by a whole block instead of
-one warp.  The labels never depend on them (canonical labels are unique for
+The build's speed depends on five schedule knobs: the roots in the first
+superstep, the superstep growth factor, the label budget per superstep, how
+many of a superstep's first roots are built by a whole block instead of one
+warp, and the queue size at which a tree's queue is split into near and far
+parts.  The labels never depend on them (canonical labels are unique for
 an order), and the labels of the hubs of rank < R are final once the roots
 below R are processed, so every candidate is timed on the same exact work: a
-prefix build of the roots of rank < R (``root_limit``).  The search is coordinate descent over the four
-knobs; the winner is cached in a JSON file keyed by graph statistics, so
-graphs of the same kind skip the search.
+prefix build of the roots of rank < R (``root_limit``).  The search is
+coordinate descent over the five knobs; the winner is cached in a JSON file
+keyed by graph statistics, so graphs of the same kind skip the search.
 
 No reference counterpart: the reference's superstep size is the fixed label
 budget ``-s`` (shared_memory/hhl.cpp:65).
@@ -31,6 +32,7 @@ FIRST = (0, 256, 1024, 4096)      # 0: the built-in choice from graph statistics
 GROWTH = (0.0, 0.5, 1.0, 2.0)     # 0.0: built-in
 SF = (0.0, 32.0, 128.0, 1024.0)   # label budget per superstep (x n); 0.0: built-in
 CTA = (-1, 64)                    # block-per-tree roots per superstep
+QSPLIT = (0, 1, 512, 4096)        # near/far queue split size; 0: built-in, 1: off
 
 
 def graph_key(g: Graph) -> str:
@@ -62,7 +64,8 @@ def _store(path, data):
 
 def tune(g: Graph, order, fraction: float = 0.02, min_roots: int = 4096, repeats: int = 1,
          cache: str | None = DEFAULT_CACHE, force: bool = False, log=None, **build_kw) -> dict:
-    """Best (first_superstep, growth, sf, cta_roots) for g; cached by graph_key."""
+    """Best (first_superstep, growth, sf, cta_roots, queue_split) for g;
+    cached by graph_key."""
     key = graph_key(g)
     data = _load(cache) if cache else {}
     if not force and key in data:
@@ -84,9 +87,10 @@ def tune(g: Graph, order, fraction: float = 0.02, min_roots: int = 4096, repeats
                 log(f"autotune {key} {cfg}: {best:.1f} ms for roots < {R}")
         return timings[k]
 
-    cfg = {"first_superstep": 0, "growth": 0.0, "sf": 0.0, "cta_roots": -1}
+    cfg = {"first_superstep": 0, "growth": 0.0, "sf": 0.0, "cta_roots": -1, "queue_split": 0}
     t0 = time.perf_counter()
-    for knob, values in (("first_superstep", FIRST), ("growth", GROWTH), ("sf", SF), ("cta_roots", CTA)):
+    for knob, values in (("first_superstep", FIRST), ("growth", GROWTH), ("sf", SF), ("cta_roots", CTA),
+                         ("queue_split", QSPLIT)):
         best_v = min(values, key=lambda v: cost({**cfg, knob: v}))
         cfg[knob] = best_v
     result = {"config": cfg, "prefix_roots": R, "prefix_ms": cost(cfg),

@@ -1513,23 +1513,15 @@ batch_kernel(TreeArgs a) {
                                     hit = test16d(q, vm, gdj, exhausted);
                                     nread += 16;
                                 } else {
+                                    // hub-ordered lists (the distance-ordered copy
+                                    // exists only with the hashed root label)
 #pragma unroll
-                                for (int t = 0; t < 8; ++t) {
-                                    q[t] = make_uint4(0, 0, 0, 0);
-                                    if (e0 + 2 * t < gle) q[t] = *(const uint4 *)(lscan + e0 + 2 * t);
-                                }
-                                hit = test8(q, e0, glb, gle, gdj);
-                                nread += 16;
-                                }
-                                if (a.dist_order && !a.hash_slots && !hit) {
-                                    // distance order: once the chunk's last entry is
-                                    // beyond d, no later chunk can hold a witness
-                                    const uint64_t last = min(e0 + 15, gle - 1);
-                                    uint32_t lastd = 0;
-#pragma unroll
-                                    for (int t = 0; t < 16; ++t)
-                                        if ((uint64_t)t == last - e0) lastd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
-                                    if (lastd > gdj) exhausted = true;
+                                    for (int t = 0; t < 8; ++t) {
+                                        q[t] = make_uint4(0, 0, 0, 0);
+                                        if (e0 + 2 * t < gle) q[t] = *(const uint4 *)(lscan + e0 + 2 * t);
+                                    }
+                                    hit = test8(q, e0, glb, gle, gdj);
+                                    nread += 16;
                                 }
                             }
                             if (hit) s_bp[lj] = 1;

@@ -33,3 +33,32 @@ def test_status_strings(P):
     L = P.lib()
     for s in range(7):
         assert L.chl_status_str(s)
+
+
+def test_struct_layouts_match_header(P, tmp_path):
+    """The ctypes mirrors of the option and statistics structs have the C
+    header's size and field offsets (a mismatch would pass garbage options)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    pairs = [("chl_build_opts", P.BuildOpts), ("chl_build_stats", P.BuildStats),
+             ("chl_server_opts", P.ServerOpts)]
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "chl.h"', "int main(void) {"]
+    for cname, py in pairs:
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in pairs:
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
