@@ -20,9 +20,15 @@
 //    higher-ranked vertices and emit a superset that the clean kernel
 //    filters with the reference's clean_cover rule.
 //  * New labels are sorted by (vertex, side, hub) with a stable radix sort
-//    and merged into the committed CSR (double-buffered) in one pass.
-//  * Weighted graphs use an indexed binary heap whose top kHeapSmem slots
-//    live in shared memory; unit-length graphs use a FIFO (BFS order).
+//    and merged into the committed CSR (double-buffered) in one pass; a
+//    second copy of every list, ordered by (distance, hub), is merged too.
+//  * The default tree kernel (batch_kernel) settles vertices in batches by
+//    the IN criterion from a near/far queue and prunes with one 16-entry
+//    item of the distance-ordered lists per lane against a shared-memory
+//    hash of the root's label.  The variants kept for comparison:
+//    tree_kernel (an indexed binary heap whose top kHeapSmem slots live in
+//    shared memory; a FIFO for unit lengths), settle_kernel (logged
+//    frontier) and cta_tree (a whole block per tree).
 #include "chl_dev.cuh"
 
 #include <algorithm>
@@ -498,9 +504,14 @@ tree_kernel(TreeArgs a) {
 // predecessor p on a shortest path then has d(p) <= d(v) - win(v) < dmin and
 // is already settled (the IN criterion of Crauser et al.).  All qualifying
 // vertices are settled together:
-//   * the queue is an unordered frontier array scanned by the whole warp;
-//   * prune tests run in 8-lane groups, 4 vertices at a time, each lane
-//     reading 4 consecutive label entries (256 contiguous bytes per group);
+//   * the queue is an unordered array scanned by the whole warp; a long
+//     queue is split at a distance threshold into a near part, scanned
+//     every round, and a far pile, read only when the near part runs out;
+//   * prune tests are flattened to (vertex, 16-entry chunk) items taken
+//     chunk-major, one per lane (default; 32- and 64-entry items in lane
+//     groups, and one lane group per vertex, are options); with the
+//     distance-ordered lists a vertex's remaining items are dropped once a
+//     chunk passes d(r, u);
 //   * the arcs of the batch are flattened over the lanes and relaxed with
 //     atomicMin on the packed (distance, via) key.
 // With unit lengths a batch is exactly one BFS level.  Relaxations from a
