@@ -1,7 +1,12 @@
-// GPU ingestion of DIMACS graph files.
+// GPU ingestion of DIMACS and SNAP graph files.
 //
-// Follows hl::Graph::read_dimacs (shared_memory/graph.hpp:168-189) line by
-// line and hl::Graph::init_arcs (:103-153) for the arc lists, on the device:
+// Follows hl::Graph::read_dimacs (shared_memory/graph.hpp:168-189) or
+// read_snap (:262-282) line by line and hl::Graph::init_arcs (:103-153) for
+// the arc lists, on the device.  hl::Graph::read (:327-335) tries DIMACS,
+// METIS, SNAP and edge lists in turn; a file whose first non-white-space
+// byte is '#' fails DIMACS (its first line starts with neither 'p', 'a' nor
+// 'c') and METIS (which accepts only digits, white space and '%' comments)
+// at once, so it is parsed as SNAP; any other file as DIMACS.
 //  * the file is copied to HBM; newline positions are found per 4 KB block
 //    (count, exclusive scan, ordered write), so every line is known;
 //  * one thread parses one line with the rules of the reference's fgets +
@@ -9,6 +14,10 @@
 //    a newline, is accepted only as a comment ('c'); `p sp n m` at most once;
 //    `a u v w` with three integers (optional sign, leading white space); any
 //    other first character rejects the file as DIMACS;
+//  * SNAP: '#' lines are comments, and one of them may be the
+//    `# Nodes: n Edges: m` header (matched on the first 511 bytes fgets
+//    returns); any other line needs fewer than 511 characters and two
+//    integers `u v` (length 1); no arc may precede the header;
 //  * every arc (u, v, w) becomes the two records of add_tmp_arc (:156-162),
 //    checked against n;
 //  * init_arcs: sort by (u, reverse first, forward last, head, length) and
@@ -16,9 +25,9 @@
 //    length) and OR the direction flags of equal records; sort by the first
 //    key again; the forward and reverse CSRs are the records in that order.
 // Sorts are LSD passes of the project's stable radix sort (length first).
-// A file the line rules reject as DIMACS, or one this parser does not handle
-// exactly (NUL bytes, numbers of more than 18 digits), is read by the host
-// parsers instead, which also try METIS, SNAP and edge lists.
+// A file the line rules reject, or one this parser does not handle exactly
+// (NUL bytes, numbers of more than 18 digits), is read by the host parsers
+// instead, which also try METIS and edge lists and report the errors.
 #include "chl_dev.cuh"
 
 #include <algorithm>
@@ -40,8 +49,12 @@ namespace {
 constexpr uint32_t kBlockBytes = 4096;
 constexpr int kLineMax = 511;   // fgets buffer of 512 bytes
 
+// line formats parsed on the device
+constexpr int kFmtDimacs = 0;
+constexpr int kFmtSnap = 1;
+
 // flags in the status word
-constexpr unsigned kFailDimacs = 1u;    // not a DIMACS file by the reference's rules
+constexpr unsigned kFailFormat = 1u;    // not a file of the format by the reference's rules
 constexpr unsigned kUnsupported = 2u;   // defer to the host parser
 
 struct ParseOut {
@@ -124,8 +137,26 @@ __device__ __forceinline__ void skip_space(const char *&p, const char *e) {
     while (p < e && is_space(*p)) ++p;
 }
 
+// a literal of the sscanf format: must match the next characters exactly
+__device__ __forceinline__ bool match_lit(const char *&p, const char *e, const char *lit) {
+    for (; *lit; ++lit, ++p)
+        if (p >= e || *p != *lit) return false;
+    return true;
+}
+
+// sscanf(line, "# Nodes: %lld Edges: %lld") == 2, with p just after the '#'
+// (a blank of the format matches any run of white space, none included)
+__device__ __forceinline__ bool snap_header(const char *p, const char *e, long long &n, long long &m, bool &unsup) {
+    skip_space(p, e);
+    if (!match_lit(p, e, "Nodes:") || !scan_ll(p, e, n, unsup)) return false;
+    skip_space(p, e);
+    return match_lit(p, e, "Edges:") && scan_ll(p, e, m, unsup);
+}
+
+// One line per thread.  DIMACS: `p` fills the header fields; SNAP: the
+// `# Nodes:` line does.  Arcs go to unordered slots (init_arcs sorts them).
 __global__ void parse_lines(const char *buf, uint64_t S, const uint64_t *nl, uint64_t nnl, uint64_t lines,
-                            ParseOut *po, int64_t *au, int64_t *av, int64_t *aw) {
+                            int fmt, ParseOut *po, int64_t *au, int64_t *av, int64_t *aw) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < lines; k += stride) {
         const uint64_t start = k == 0 ? 0 : nl[k - 1] + 1;
@@ -140,9 +171,45 @@ __global__ void parse_lines(const char *buf, uint64_t S, const uint64_t *nl, uin
                 break;
             }
         const char c0 = len ? p[0] : '\n';
+        if (fmt == kFmtSnap) {
+            bool unsup = false;
+            if (c0 == '#') {
+                // fgets hands sscanf the first 511 bytes; the rest is skipped
+                long long n = 0, m = 0;
+                const char *qe = p + (len < (uint64_t)kLineMax ? len : (uint64_t)kLineMax);
+                if (snap_header(p + 1, qe, n, m, unsup)) {
+                    atomicAdd(&po->p_count, 1u);
+                    po->p_line = k;   // meaningful only when p_count == 1
+                    po->n = n;
+                    po->m = m;
+                }
+                if (unsup) atomicOr(&po->status, kUnsupported);
+                continue;
+            }
+            // a line fgets returns in pieces is rejected (the last line may
+            // lack its newline)
+            if (len >= (uint64_t)kLineMax) {
+                atomicOr(&po->status, kFailFormat);
+                continue;
+            }
+            const char *q = p;
+            long long u = 0, v = 0;
+            const bool ok = scan_ll(q, e, u, unsup) && scan_ll(q, e, v, unsup);
+            if (unsup) atomicOr(&po->status, kUnsupported);
+            if (!ok) {
+                atomicOr(&po->status, kFailFormat);
+                continue;
+            }
+            const unsigned long long slot = atomicAdd(&po->arcs, 1ull);
+            atomicMin(&po->first_a, (unsigned long long)k);
+            au[slot] = u;
+            av[slot] = v;
+            aw[slot] = 1;
+            continue;
+        }
         if (len >= (uint64_t)kLineMax || !has_nl) {
             // read in pieces by fgets: acceptable only as a comment
-            if (c0 != 'c') atomicOr(&po->status, kFailDimacs);
+            if (c0 != 'c') atomicOr(&po->status, kFailFormat);
             continue;
         }
         if (c0 == 'c') continue;
@@ -159,7 +226,7 @@ __global__ void parse_lines(const char *buf, uint64_t S, const uint64_t *nl, uin
             }
             if (unsup) atomicOr(&po->status, kUnsupported);
             if (!ok) {
-                atomicOr(&po->status, kFailDimacs);
+                atomicOr(&po->status, kFailFormat);
                 continue;
             }
             atomicAdd(&po->p_count, 1u);
@@ -174,7 +241,7 @@ __global__ void parse_lines(const char *buf, uint64_t S, const uint64_t *nl, uin
             const bool ok = scan_ll(q, e, u, unsup) && scan_ll(q, e, v, unsup) && scan_ll(q, e, w, unsup);
             if (unsup) atomicOr(&po->status, kUnsupported);
             if (!ok) {
-                atomicOr(&po->status, kFailDimacs);
+                atomicOr(&po->status, kFailFormat);
                 continue;
             }
             const unsigned long long slot = atomicAdd(&po->arcs, 1ull);
@@ -184,19 +251,20 @@ __global__ void parse_lines(const char *buf, uint64_t S, const uint64_t *nl, uin
             aw[slot] = w;
             continue;
         }
-        atomicOr(&po->status, kFailDimacs);
+        atomicOr(&po->status, kFailFormat);
     }
 }
 
-// add_tmp_arc: bounds check of the 32-bit vertex values against n, then the
-// two records (u, v, w, fwd, und) and (v, u, w, und, rev)
+// add_tmp_arc: bounds check of the 32-bit vertex values (ids minus `base`:
+// 1 for DIMACS, 0 for SNAP) against n, then the two records
+// (u, v, w, fwd, und) and (v, u, w, und, rev)
 __global__ void make_records(uint64_t arcs, const int64_t *au, const int64_t *av, const int64_t *aw, long long n,
-                             int undirected, uint32_t *ru, uint32_t *rh, int32_t *rl, uint32_t *rf,
+                             int base, int undirected, uint32_t *ru, uint32_t *rh, int32_t *rl, uint32_t *rf,
                              unsigned *status) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < arcs; i += stride) {
-        const uint32_t u = (uint32_t)(au[i] - 1), v = (uint32_t)(av[i] - 1);
-        if ((long long)u >= n || (long long)v >= n) atomicOr(status, kFailDimacs);
+        const uint32_t u = (uint32_t)(au[i] - base), v = (uint32_t)(av[i] - base);
+        if ((long long)u >= n || (long long)v >= n) atomicOr(status, kFailFormat);
         const int32_t w = (int32_t)aw[i];
         // flags: bit 0 forward, bit 1 reverse
         ru[2 * i] = u;
@@ -377,9 +445,9 @@ int read_file(const char *path, std::vector<char> &buf) {
     return CHL_OK;
 }
 
-// 1: the file is DIMACS by the reference's rules and the graph was built;
-// 0: defer to the host parsers; < 0: -status of an error
-int ingest_dimacs(const std::vector<char> &file, bool undirected, chl_graph *g) {
+// 1: the file is of format fmt by the reference's rules and the graph was
+// built; 0: defer to the host parsers; < 0: -status of an error
+int ingest_text(const std::vector<char> &file, int fmt, bool undirected, chl_graph *g) {
     const uint64_t S = file.size();
     Pool pool;
     int rc;
@@ -412,14 +480,14 @@ int ingest_dimacs(const std::vector<char> &file, bool undirected, chl_graph *g) 
     int64_t *au, *av, *aw;
     if ((rc = pool.get(&au, lines)) || (rc = pool.get(&av, lines)) || (rc = pool.get(&aw, lines))) return -rc;
     if (lines) {
-        parse_lines<<<device_sms() * 8, 256>>>(d_buf, S, d_nl, nnl, lines, d_po, au, av, aw);
+        parse_lines<<<device_sms() * 8, 256>>>(d_buf, S, d_nl, nnl, lines, fmt, d_po, au, av, aw);
         CHL_CUDA_NEG(cudaGetLastError());
     }
     CHL_CUDA_NEG(cudaMemcpy(&h, d_po, sizeof(h), cudaMemcpyDeviceToHost));
     if (h.status & kUnsupported) return 0;
-    if (h.status & kFailDimacs) return 0;
-    if (h.p_count > 1) return 0;                       // a second `p` line
-    long long n = h.p_count ? h.n : 0;                 // arcs before `p` see n = 0
+    if (h.status & kFailFormat) return 0;
+    if (h.p_count > 1) return 0;                       // a second header
+    long long n = h.p_count ? h.n : 0;                 // arcs before the header see n = 0
     if (h.arcs && (h.p_count == 0 || h.first_a < h.p_line)) return 0;
     if (n < 0) return 0;   // the host decides (every arc fails the bounds check)
     if (n >= (1ll << 30)) {
@@ -435,10 +503,12 @@ int ingest_dimacs(const std::vector<char> &file, bool undirected, chl_graph *g) 
         return -rc;
     const int grid = device_sms() * 8;
     CHL_CUDA_NEG(cudaMemset(d_status, 0, 4));
-    if (arcs) make_records<<<grid, 256>>>(arcs, au, av, aw, n, undirected ? 1 : 0, ru, rh, rl, rf, d_status);
+    if (arcs)
+        make_records<<<grid, 256>>>(arcs, au, av, aw, n, fmt == kFmtDimacs ? 1 : 0, undirected ? 1 : 0, ru, rh,
+                                    rl, rf, d_status);
     unsigned st = 0;
     CHL_CUDA_NEG(cudaMemcpy(&st, d_status, 4, cudaMemcpyDeviceToHost));
-    if (st) return 0;   // an arc endpoint outside [0, n): not DIMACS (the host tries the others)
+    if (st) return 0;   // an arc endpoint outside [0, n): not this format (the host tries the others)
     g->n = (uint32_t)n;
     g->m = arcs * (undirected ? 2 : 1);
     // init_arcs
@@ -528,7 +598,14 @@ extern "C" int chl_graph_load_gpu(const char *path, int undirected, chl_graph **
     if (rc) return rc;
     chl_graph *g = new (std::nothrow) chl_graph();
     if (!g) return CHL_ERR_OOM;
-    const int r = ingest_dimacs(file, undirected != 0, g);
+    // the first byte that is not white space (C isspace) picks the format
+    int fmt = kFmtDimacs;
+    for (char c : file) {
+        if (c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r') continue;
+        if (c == '#') fmt = kFmtSnap;
+        break;
+    }
+    const int r = ingest_text(file, fmt, undirected != 0, g);
     if (r == 1) {
         if (parsed_on_gpu) *parsed_on_gpu = 1;
         *out = g;

@@ -1,4 +1,4 @@
-"""GPU DIMACS ingestion against the host parsers (which follow the
+"""GPU DIMACS and SNAP ingestion against the host parsers (which follow the
 reference's Graph::read and are pinned to it by test_graph_io.py).
 
 Every file must give the same outcome both ways: the same CSRs in both
@@ -43,7 +43,8 @@ def same(P, path, undirected=False, expect_gpu=None):
     return a
 
 
-GOLDEN_GR = sorted(glob.glob(os.path.join(GOLDEN, "**", "*.gr"), recursive=True))
+GOLDEN_GR = sorted(p for ext in ("gr", "txt", "graph")
+                   for p in glob.glob(os.path.join(GOLDEN, "**", "*." + ext), recursive=True))
 
 
 @pytest.mark.parametrize("path", GOLDEN_GR, ids=[os.path.basename(p) for p in GOLDEN_GR])
@@ -105,3 +106,52 @@ def test_random_files_and_large_grid(P, tmp_path):
     g.write(p)
     r = same(P, p, False, expect_gpu=True)
     assert r[0] == "ok" and r[1][0] == g.get_n()
+
+
+def test_snap_quirks(P, tmp_path):
+    # files whose first non-blank byte is '#' are parsed on the GPU as SNAP;
+    # the ones the reference's SNAP rules reject go to the host parsers,
+    # which report the error
+    hdr = "# Nodes: 4 Edges: 3\n"
+    cases = {
+        "plain": (hdr + "0 1\n1 2\n2 3\n", True),
+        "tabs_crlf_junk": ("# Nodes:\t4   Edges: 3\r\n0\t1\r\n1 2 junk\r\n2 3\r\n", True),
+        "comments_no_final_newline": ("# title\n#Nodes:3 Edges:2\n# more\n0 1\n1 2", True),
+        "dups_and_loops": (hdr + "0 1\n1 0\n0 1\n2 2\n3 0\n", True),
+        "signs": (hdr + "+0 +2\n", True),
+        "truncated_ids": (hdr + "4294967297 2\n", True),
+        "long_comment": ("# " + "x" * 700 + "\n" + hdr + "0 2\n", True),
+        "long_header_line": ("# Nodes: 4 Edges: 1" + " " * 600 + "\n0 2\n", True),
+        "hash_only": ("#\n", True),
+        "no_header": ("# hello\n0 1\n", False),
+        "two_headers": (hdr + hdr + "0 1\n", False),
+        "header_after_arc": ("# x\n0 1\n" + hdr, False),
+        "out_of_range": (hdr + "0 5\n", False),
+        "negative": (hdr + "-1 2\n", False),
+        "one_number": (hdr + "0\n", False),
+        "empty_line": (hdr + "\n0 2\n", False),
+        "long_data_line": (hdr + "0 " + " " * 600 + "2\n", False),
+        "leading_blank_line": ("  \n" + hdr + "0 2\n", False),
+        "nul_byte": (("# Nodes: 4 Edges: 1\n0 1\x00\n").encode(), False),
+        "huge_number": (hdr + "0 1234567890123456789012\n", False),
+    }
+    for name, (text, on_gpu) in cases.items():
+        p = write(tmp_path, name + ".txt", text)
+        for und in (False, True):
+            same(P, p, und, expect_gpu=on_gpu)
+
+
+def test_random_snap_files(P, tmp_path):
+    rng = np.random.default_rng(5)
+    for t in range(6):
+        n = int(rng.integers(2, 400))
+        k = int(rng.integers(1, 4000))
+        u = rng.integers(0, n, k)
+        v = rng.integers(0, n, k)
+        lines = ["# Directed graph (each unordered pair of nodes is saved once)",
+                 f"# Nodes: {n} Edges: {k}", "# FromNodeId\tToNodeId"]
+        lines += [f"{a}\t{b}" for a, b in zip(u, v)]
+        p = write(tmp_path, f"s{t}.txt", "\n".join(lines) + ("\n" if t % 2 else ""))
+        for und in (False, True):
+            r = same(P, p, und, expect_gpu=True)
+            assert r[0] == "ok" and r[1][0] == n
