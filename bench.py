@@ -65,6 +65,9 @@ def parse():
     ap.add_argument("--verbose", type=int, default=0, help="2: per-superstep lines on stderr")
     ap.add_argument("--max-warps", type=int, default=0,
                     help="cap on concurrent trees (bounds the per-tree workspace, e.g. for profiler captures)")
+    ap.add_argument("--ingest", action="store_true",
+                    help="graph ingestion: host parsers against the GPU path on DIMACS and SNAP files "
+                         "of the grid workload")
     ap.add_argument("--serve", action="store_true",
                     help="also run the open-loop serving test (Poisson arrivals) on the built labels")
     ap.add_argument("--serve-qps", type=float, default=2e8, help="offered pair rate (pairs/s)")
@@ -524,10 +527,62 @@ def run_rank(args):
     print(json.dumps(out), flush=True)
 
 
+def run_ingest(args):
+    """Graph ingestion: the grid workload written as a DIMACS and as a SNAP
+    file, each read twice by the host parsers (chl_graph_load) and twice by
+    the GPU path (chl_graph_load_gpu) in one process; the CSRs of the two
+    paths are compared."""
+    import shutil
+    import tempfile
+    import plant_gb300 as P
+    g = P.Graph.grid(args.side, args.side, highways=args.highways, seed=1)
+    d = tempfile.mkdtemp(prefix="chl_ingest_")
+    try:
+        files = {"dimacs": os.path.join(d, "g.gr"), "snap": os.path.join(d, "g.txt")}
+        g.write(files["dimacs"])
+        off, head, _ = g.csr(True)
+        src = np.repeat(np.arange(g.get_n(), dtype=np.int64), np.diff(off.astype(np.int64)))
+        with open(files["snap"], "w") as f:
+            f.write(f"# Nodes: {g.get_n()} Edges: {len(head)}\n# FromNodeId\tToNodeId\n")
+            np.savetxt(f, np.stack([src, head.astype(np.int64)], 1), fmt="%d\t%d")
+        tiny = os.path.join(d, "t.gr")
+        with open(tiny, "w") as f:
+            f.write("p sp 2 1\na 1 2 1\n")
+        P.Graph.read_gpu(tiny)   # CUDA context set-up outside the timings
+        out = {"metric": "graph ingestion time (file to CSR)", "unit": "s", "higher_is_better": False,
+               "data": "synthetic (seeded generator)",
+               "config": {"workload": f"grid{args.side}x{args.side}+hw{args.highways}",
+                          "vertices": g.get_n(), "arcs": int(len(head))}}
+        for fmt, path in files.items():
+            res = {"bytes": os.path.getsize(path)}
+            got = {}
+            for way in ("host", "gpu"):
+                ts = []
+                for _ in range(2):
+                    t0 = time.perf_counter()
+                    if way == "host":
+                        got[way] = P.Graph.read(path)
+                    else:
+                        got[way], used = P.Graph.read_gpu(path)
+                        res["parsed_on_gpu"] = bool(used)
+                    ts.append(round(time.perf_counter() - t0, 4))
+                res[way + "_s"] = ts
+            res["identical"] = all(np.array_equal(a, b) for fwd in (True, False)
+                                   for a, b in zip(got["host"].csr(fwd), got["gpu"].csr(fwd)))
+            res["speedup_second_read"] = round(res["host_s"][1] / max(res["gpu_s"][1], 1e-9), 1)
+            out[fmt] = res
+        print(json.dumps(out), flush=True)
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
 def main():
     args = parse()
     if args.rank:
         run_rank(args)
+        return
+    if args.ingest:
+        run_ingest(args)
         return
     global METRIC
     if args.workload == "rmat":
