@@ -208,10 +208,12 @@ def cpu_sample(g, order, seconds, threads=None):
     off, head, ln = g.csr(True)
     og = O.OGraph.from_csr(g.get_n(), off, head, ln)
     threads = threads or os.cpu_count() or 1
+    # grow R until one sample takes at least 2/3 of the target (the first
+    # roots cost the most, so time grows slower than R)
     r = 32
     labels, secs = O.gll_sample(og, order, r, threads)
-    while secs < seconds / 4 and r < len(order):
-        r = min(len(order), int(r * max(2.0, min(8.0, seconds / max(secs, 1e-3) / 2))))
+    while secs < seconds * 2 / 3 and r < len(order):
+        r = min(len(order), int(r * max(1.5, min(8.0, seconds / max(secs, 1e-3)))))
         labels, secs = O.gll_sample(og, order, r, threads)
     return og, r, threads, labels, secs
 
@@ -301,7 +303,10 @@ def run_reference(args, ws, rank):
     from oracle import oracle as O
     P.lib()
     g, order = make_workload(P, args, cpu_order=True)
-    og, r, threads, labels, secs = cpu_sample(g, order, args.cpu_seconds)
+    # one step's sample sized so that the W + K steps take about two minutes
+    # (at most --cpu-seconds each)
+    target = max(2.0, min(args.cpu_seconds, 120.0 / max(1, args.steps + args.warmup)))
+    og, r, threads, labels, secs = cpu_sample(g, order, target)
     vals = []
     for _ in range(args.warmup):
         O.gll_sample(og, order, r, threads)
