@@ -164,8 +164,24 @@ static bool read_dimacs(FILE *file, bool undirected, chl_graph *g,
     return true;
 }
 
-static bool read_metis(FILE *file, bool undirected, chl_graph *g,
-                       std::vector<TmpArc> &tmp, long long &n) {
+// character sources of the METIS reader: the file, or a buffer (whose end
+// reads as EOF)
+struct FileChars {
+    FILE *f;
+    int get() { return fgetc(f); }
+};
+struct BufChars {
+    const char *p, *e;
+    bool hit_end;
+    int get() {
+        if (p < e) return (int)(unsigned char)*p++;
+        hit_end = true;
+        return EOF;
+    }
+};
+
+template <class Chars>
+static bool metis_parse(Chars &src, bool undirected, chl_graph *g, std::vector<TmpArc> &tmp, long long &n) {
     int c, i = 0, fmt = 0, ncon = 0, skip = 0;
     long long elem = 0;
     uint32_t v = 0, head = 0xFFFFFFFFu;
@@ -175,9 +191,9 @@ static bool read_metis(FILE *file, bool undirected, chl_graph *g,
     bool inelem = false;
     (void)ncon;
     do {
-        c = fgetc(file);
+        c = src.get();
         if (newline && c == '%') {
-            while (c != '\n' && c != EOF) c = fgetc(file);
+            while (c != '\n' && c != EOF) c = src.get();
         } else if (c != EOF && isdigit(c)) {
             inelem = true;
             elem = elem * 10 + c - '0';
@@ -228,6 +244,24 @@ static bool read_metis(FILE *file, bool undirected, chl_graph *g,
         }
     } while (c != EOF);
     return true;
+}
+
+static bool read_metis(FILE *file, bool undirected, chl_graph *g,
+                       std::vector<TmpArc> &tmp, long long &n) {
+    FileChars src{file};
+    return metis_parse(src, undirected, g, tmp, n);
+}
+
+// true when the METIS reader returns false before it has read past
+// buf[0, len): it reads characters in order and never revisits a verdict, so
+// it rejects any file that starts with these bytes at the same character
+// (false: no verdict from this prefix)
+bool metis_rejects_prefix(const char *buf, size_t len) {
+    chl_graph g;
+    std::vector<TmpArc> tmp;
+    long long n = 0;
+    BufChars src{buf, buf + len, false};
+    return !metis_parse(src, false, &g, tmp, n) && !src.hit_end;
 }
 
 static bool read_snap(FILE *file, bool undirected, chl_graph *g,

@@ -1,12 +1,17 @@
-// GPU ingestion of DIMACS and SNAP graph files.
+// GPU ingestion of DIMACS, SNAP and edge-list graph files.
 //
-// Follows hl::Graph::read_dimacs (shared_memory/graph.hpp:168-189) or
-// read_snap (:262-282) line by line and hl::Graph::init_arcs (:103-153) for
-// the arc lists, on the device.  hl::Graph::read (:327-335) tries DIMACS,
-// METIS, SNAP and edge lists in turn; a file whose first non-white-space
-// byte is '#' fails DIMACS (its first line starts with neither 'p', 'a' nor
-// 'c') and METIS (which accepts only digits, white space and '%' comments)
-// at once, so it is parsed as SNAP; any other file as DIMACS.
+// Follows hl::Graph::read_dimacs (shared_memory/graph.hpp:168-189),
+// read_snap (:262-282) or read_edgelist (:284-308) line by line and
+// hl::Graph::init_arcs (:103-153) for the arc lists, on the device.
+// hl::Graph::read (:327-335) tries DIMACS, METIS, SNAP and edge lists in
+// turn, so the host picks the reader the reference would end up with:
+//  * first non-white-space byte '#': DIMACS fails on the first line (it
+//    starts with neither 'p', 'a' nor 'c') and METIS at the '#' (it accepts
+//    only digits, white space and '%' comments): SNAP;
+//  * first byte 'p', 'a' or 'c', or an empty file: DIMACS;
+//  * otherwise DIMACS and SNAP fail on the first line (a SNAP arc before the
+//    header sees n = 0), and when the host's METIS reader rejects a prefix
+//    of the file (metis_rejects_prefix), edge list; else the host parsers.
 //  * the file is copied to HBM; newline positions are found per 4 KB block
 //    (count, exclusive scan, ordered write), so every line is known;
 //  * one thread parses one line with the rules of the reference's fgets +
@@ -18,6 +23,9 @@
 //    `# Nodes: n Edges: m` header (matched on the first 511 bytes fgets
 //    returns); any other line needs fewer than 511 characters and two
 //    integers `u v` (length 1); no arc may precede the header;
+//  * edge list: every line needs fewer than 511 characters and three
+//    integers `u v w`; n is the number of distinct ids, and the ids, cut to
+//    32 bits, must be below it;
 //  * every arc (u, v, w) becomes the two records of add_tmp_arc (:156-162),
 //    checked against n;
 //  * init_arcs: sort by (u, reverse first, forward last, head, length) and
@@ -52,6 +60,7 @@ constexpr int kLineMax = 511;   // fgets buffer of 512 bytes
 // line formats parsed on the device
 constexpr int kFmtDimacs = 0;
 constexpr int kFmtSnap = 1;
+constexpr int kFmtEdgelist = 2;
 
 // flags in the status word
 constexpr unsigned kFailFormat = 1u;    // not a file of the format by the reference's rules
@@ -207,6 +216,28 @@ __global__ void parse_lines(const char *buf, uint64_t S, const uint64_t *nl, uin
             aw[slot] = 1;
             continue;
         }
+        if (fmt == kFmtEdgelist) {
+            // a line fgets returns in pieces is rejected (the last line may
+            // lack its newline); `sscanf(buf, "%lld %lld %lld") == 3`
+            bool unsup = false;
+            if (len >= (uint64_t)kLineMax) {
+                atomicOr(&po->status, kFailFormat);
+                continue;
+            }
+            const char *q = p;
+            long long u = 0, v = 0, w = 0;
+            const bool ok = scan_ll(q, e, u, unsup) && scan_ll(q, e, v, unsup) && scan_ll(q, e, w, unsup);
+            if (unsup) atomicOr(&po->status, kUnsupported);
+            if (!ok) {
+                atomicOr(&po->status, kFailFormat);
+                continue;
+            }
+            const unsigned long long slot = atomicAdd(&po->arcs, 1ull);
+            au[slot] = u;
+            av[slot] = v;
+            aw[slot] = w;
+            continue;
+        }
         if (len >= (uint64_t)kLineMax || !has_nl) {
             // read in pieces by fgets: acceptable only as a comment
             if (c0 != 'c') atomicOr(&po->status, kFailFormat);
@@ -252,6 +283,28 @@ __global__ void parse_lines(const char *buf, uint64_t S, const uint64_t *nl, uin
             continue;
         }
         atomicOr(&po->status, kFailFormat);
+    }
+}
+
+// edge-list ids as order-preserving unsigned keys (sign bit flipped)
+__global__ void id_keys(uint64_t arcs, const int64_t *au, const int64_t *av, uint64_t *key, uint32_t *val) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < arcs; i += stride) {
+        key[2 * i] = (uint64_t)au[i] ^ (1ull << 63);
+        key[2 * i + 1] = (uint64_t)av[i] ^ (1ull << 63);
+        val[2 * i] = 0;
+        val[2 * i + 1] = 0;
+    }
+}
+
+// number of distinct values of a sorted key array
+__global__ void count_distinct(uint64_t cnt, const uint64_t *key, unsigned long long *out) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t b = blockIdx.x * (uint64_t)blockDim.x; b < cnt; b += stride) {
+        const uint64_t i = b + threadIdx.x;
+        const bool first = i < cnt && (i == 0 || key[i] != key[i - 1]);
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, first);
+        if ((threadIdx.x & 31) == 0 && m) atomicAdd(out, (unsigned long long)__popc(m));
     }
 }
 
@@ -486,9 +539,33 @@ int ingest_text(const std::vector<char> &file, int fmt, bool undirected, chl_gra
     CHL_CUDA_NEG(cudaMemcpy(&h, d_po, sizeof(h), cudaMemcpyDeviceToHost));
     if (h.status & kUnsupported) return 0;
     if (h.status & kFailFormat) return 0;
-    if (h.p_count > 1) return 0;                       // a second header
-    long long n = h.p_count ? h.n : 0;                 // arcs before the header see n = 0
-    if (h.arcs && (h.p_count == 0 || h.first_a < h.p_line)) return 0;
+    long long n = 0;
+    if (fmt == kFmtEdgelist) {
+        // n = the number of distinct ids
+        if (h.arcs) {
+            const uint64_t c2 = 2 * h.arcs;
+            uint64_t *ka, *kb, *d_c2;
+            uint32_t *va, *vb;
+            unsigned long long *d_dist;
+            if ((rc = pool.get(&ka, c2)) || (rc = pool.get(&kb, c2)) || (rc = pool.get(&va, c2)) ||
+                (rc = pool.get(&vb, c2)) || (rc = pool.get(&d_c2, 1)) || (rc = pool.get(&d_dist, 1)))
+                return -rc;
+            CHL_CUDA_NEG(cudaMemcpy(d_c2, &c2, 8, cudaMemcpyHostToDevice));
+            CHL_CUDA_NEG(cudaMemset(d_dist, 0, 8));
+            id_keys<<<device_sms() * 8, 256>>>(h.arcs, au, av, ka, va);
+            CHL_CUDA_NEG(cudaGetLastError());
+            if ((rc = sort_kv(ka, va, kb, vb, d_c2, c2, 64, tmp, tmp_bytes))) return -rc;
+            count_distinct<<<device_sms() * 8, 256>>>(c2, ka, d_dist);
+            CHL_CUDA_NEG(cudaGetLastError());
+            unsigned long long nd = 0;
+            CHL_CUDA_NEG(cudaMemcpy(&nd, d_dist, 8, cudaMemcpyDeviceToHost));
+            n = (long long)nd;
+        }
+    } else {
+        if (h.p_count > 1) return 0;                   // a second header
+        n = h.p_count ? h.n : 0;                       // arcs before the header see n = 0
+        if (h.arcs && (h.p_count == 0 || h.first_a < h.p_line)) return 0;
+    }
     if (n < 0) return 0;   // the host decides (every arc fails the bounds check)
     if (n >= (1ll << 30)) {
         set_error("graph has too many vertices (the arc head field is 30 bits)");
@@ -598,14 +675,18 @@ extern "C" int chl_graph_load_gpu(const char *path, int undirected, chl_graph **
     if (rc) return rc;
     chl_graph *g = new (std::nothrow) chl_graph();
     if (!g) return CHL_ERR_OOM;
-    // the first byte that is not white space (C isspace) picks the format
-    int fmt = kFmtDimacs;
+    // the reader the reference would end up with (see the top of this file)
+    int fmt = -1;
+    char first = 0;
     for (char c : file) {
         if (c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r') continue;
-        if (c == '#') fmt = kFmtSnap;
+        first = c;
         break;
     }
-    const int r = ingest_text(file, fmt, undirected != 0, g);
+    if (first == '#') fmt = kFmtSnap;
+    else if (file.empty() || file[0] == 'p' || file[0] == 'a' || file[0] == 'c') fmt = kFmtDimacs;
+    else if (metis_rejects_prefix(file.data(), std::min<size_t>(file.size(), (size_t)1 << 16))) fmt = kFmtEdgelist;
+    const int r = fmt < 0 ? 0 : ingest_text(file, fmt, undirected != 0, g);
     if (r == 1) {
         if (parsed_on_gpu) *parsed_on_gpu = 1;
         *out = g;

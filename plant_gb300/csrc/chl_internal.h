@@ -126,6 +126,8 @@ int labels_from_host(uint32_t n, const uint64_t *off2, const uint32_t *hub,
                      const int32_t *dist, chl_labels **out);
 // min/max length, unit-length and symmetry flags of a graph's host CSR
 void graph_fill_stats(chl_graph *g);
+// METIS reader verdict on the complete lines of a file prefix (chl_graph.cpp)
+bool metis_rejects_prefix(const char *buf, size_t len);
 // hl::Labeling::write's text, formatted on the device (labels in HBM)
 int write_labels_text_device(const chl_labels *l, const char *path);
 // free the device copy of a graph (no-op without one)

@@ -1,5 +1,5 @@
-"""GPU DIMACS and SNAP ingestion against the host parsers (which follow the
-reference's Graph::read and are pinned to it by test_graph_io.py).
+"""GPU DIMACS, SNAP and edge-list ingestion against the host parsers (which
+follow the reference's Graph::read and are pinned to it by test_graph_io.py).
 
 Every file must give the same outcome both ways: the same CSRs in both
 directions, the same n, m and symmetry, or the same error.  Files the
@@ -81,7 +81,7 @@ def test_quirks(P, tmp_path):
         "bad_token": ("p sp 2 1\na 1 x 1\n", False),
         "nul_byte": (b"p sp 2 1\na 1 2 1\x00\n", False),
         "huge_number": ("p sp 2 1\na 1 2 1234567890123456789012\n", False),
-        "edgelist_like": ("0 1 5\n1 2 3\n", False),
+        "edgelist_like": ("0 1 5\n1 2 3\n", True),   # an edge list: read on the GPU as one
     }
     for name, (text, on_gpu) in cases.items():
         p = write(tmp_path, name + ".gr", text)
@@ -152,6 +152,53 @@ def test_random_snap_files(P, tmp_path):
                  f"# Nodes: {n} Edges: {k}", "# FromNodeId\tToNodeId"]
         lines += [f"{a}\t{b}" for a, b in zip(u, v)]
         p = write(tmp_path, f"s{t}.txt", "\n".join(lines) + ("\n" if t % 2 else ""))
+        for und in (False, True):
+            r = same(P, p, und, expect_gpu=True)
+            assert r[0] == "ok" and r[1][0] == n
+
+
+def test_edgelist_quirks(P, tmp_path):
+    # a file DIMACS and SNAP reject on its first line is an edge list when the
+    # host's METIS reader rejects a prefix of it; METIS files stay on the host
+    cases = {
+        "plain": ("0 1 5\n1 2 3\n2 0 4\n", True),
+        "unit_weights": ("0 1 1\n1 2 1\n2 0 1\n", True),
+        "no_final_newline": ("0 1 5\n1 0 2", True),
+        "crlf_tabs": ("0\t1\t5\r\n1 0 2\r\n", True),
+        "trailing_comment": ("0 1 5 % comment\n", True),
+        "ids_past_32_bits": ("4294967296 1 5\n1 4294967296 2\n", True),
+        "leading_space": (" 0 1 5\n1 0 2\n", True),
+        "loops_and_dups": ("0 0 3\n0 1 5\n0 1 2\n1 0 7\n", True),
+        "weight_10": ("0 1 10\n1 0 11\n", True),
+        "negative_weight": ("0 1 -4\n1 0 2\n", True),
+        "metis_empty": ("0 5 1\n", False),
+        "metis_two_numbers": ("0 1\n", False),
+        "metis_graph": ("3 2\n2\n1 3\n2\n", False),
+        "negative_id": ("-1 0 3\n0 1 2\n", False),
+        "blank_line": ("0 1 5\n\n1 0 2\n", False),
+        "long_line": ("0 1 " + " " * 600 + "5\n", False),
+        "sparse_ids": ("0 1 5\n1 7 3\n", False),
+        "nul_byte": (b"0 1 5\x00\n1 0 2\n", False),
+        "huge_number": ("0 1 5\n1 0 1234567890123456789012\n", False),
+    }
+    for name, (text, on_gpu) in cases.items():
+        p = write(tmp_path, name + ".txt", text)
+        for und in (False, True):
+            same(P, p, und, expect_gpu=on_gpu)
+
+
+def test_random_edgelist_files(P, tmp_path):
+    rng = np.random.default_rng(9)
+    for t in range(6):
+        n = int(rng.integers(2, 500))
+        k = int(rng.integers(n, 5000))
+        ids = np.concatenate([np.arange(n), rng.integers(0, n, 2 * k - n)])
+        rng.shuffle(ids)
+        u, v = ids[:k], ids[k:]
+        w = rng.integers(-3 if t % 3 == 0 else 1, 100, k)
+        w[0] = int(rng.integers(2, 10))   # a first line METIS rejects (format code w)
+        lines = [f"{a} {b} {c}" for a, b, c in zip(u, v, w)]
+        p = write(tmp_path, f"e{t}.txt", "\n".join(lines) + ("\n" if t % 2 else ""))
         for und in (False, True):
             r = same(P, p, und, expect_gpu=True)
             assert r[0] == "ok" and r[1][0] == n
