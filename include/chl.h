@@ -63,11 +63,11 @@ const char *chl_last_error(void);
 int chl_graph_load(const char *path, int undirected, chl_graph **out);
 
 /* Replaces hl::Graph::read (shared_memory/graph.hpp:327-335) like
- * chl_graph_load, with DIMACS and SNAP files parsed and their arc lists built
- * on the GPU (the reference's line rules and init_arcs, :168-189, :262-282
- * and :103-153; a file whose first non-blank byte is '#' is SNAP).  Files
- * those rules reject, and METIS and edge-list files, go through the host
- * parsers.  *parsed_on_gpu (may be NULL) tells which path ran. */
+ * chl_graph_load, with DIMACS, SNAP and edge-list files parsed and their arc
+ * lists built on the GPU (the reference's line rules and init_arcs, :168-189,
+ * :262-282, :284-308 and :103-153; the host picks the reader the reference
+ * would end up with).  Files those rules reject, and METIS files, go through
+ * the host parsers.  *parsed_on_gpu (may be NULL) tells which path ran. */
 int chl_graph_load_gpu(const char *path, int undirected, chl_graph **out,
                        int *parsed_on_gpu);
 /* Replaces hl::Graph::set_n + add_arc + finalize
