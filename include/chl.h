@@ -77,6 +77,12 @@ int chl_graph_load_gpu(const char *path, int undirected, chl_graph **out,
 int chl_graph_from_arcs(uint32_t n, size_t k, const uint32_t *src,
                         const uint32_t *dst, const int32_t *len,
                         int undirected, chl_graph **out);
+/* The same from an out-arc CSR: the arcs of v are head[off[v] .. off[v+1])
+ * with lengths len[...]; off has n + 1 non-decreasing entries from 0.  The
+ * arc lists are the ones chl_graph_from_arcs builds from those arcs (the
+ * init_arcs merge, shared_memory/graph.hpp:103-153). */
+int chl_graph_from_csr(uint32_t n, const uint64_t *off, const uint32_t *head,
+                       const int32_t *len, int undirected, chl_graph **out);
 
 /* Replaces hl::Graph::write (shared_memory/graph.hpp:338-343) for the
  * forward arcs; used to hand generated graphs to other tools. */

@@ -89,6 +89,7 @@ SIGNATURES = {
     "chl_graph_load": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(_P)]),
     "chl_graph_load_gpu": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(_P), C.POINTER(C.c_int)]),
     "chl_graph_from_arcs": (C.c_int, [C.c_uint32, C.c_size_t, _U32P, _U32P, _I32P, C.c_int, C.POINTER(_P)]),
+    "chl_graph_from_csr": (C.c_int, [C.c_uint32, _U64P, _U32P, _I32P, C.c_int, C.POINTER(_P)]),
     "chl_graph_write_dimacs": (C.c_int, [_P, C.c_char_p]),
     "chl_graph_n": (C.c_uint32, [_P]),
     "chl_graph_m": (C.c_uint64, [_P]),
@@ -217,6 +218,22 @@ class Graph:
         h = C.c_void_p()
         _check(lib().chl_graph_from_arcs(n, len(s), _ptr(s, _U32P), _ptr(d, _U32P), _ptr(w, _I32P),
                                          int(undirected), C.byref(h)), "graph from arcs")
+        return cls(h)
+
+    @classmethod
+    def from_csr(cls, n: int, off, head, length, undirected: bool = False) -> "Graph":
+        """Graph from an out-arc CSR (off[n+1], head, length), merged like
+        from_arcs."""
+        o = np.ascontiguousarray(off, dtype=np.uint64)
+        if len(o) != n + 1:
+            raise CHLError(CHL_ERR_INVALID, "graph from csr", "off must have n + 1 entries")
+        hd = _u32(head)
+        w = np.ascontiguousarray(length, dtype=np.int32)
+        if len(hd) < int(o[-1]) or len(w) < int(o[-1]):
+            raise CHLError(CHL_ERR_INVALID, "graph from csr", "head/length shorter than off[n]")
+        h = C.c_void_p()
+        _check(lib().chl_graph_from_csr(n, _ptr(o, _U64P), _ptr(hd, _U32P), _ptr(w, _I32P), int(undirected),
+                                        C.byref(h)), "graph from csr")
         return cls(h)
 
     @classmethod

@@ -425,6 +425,31 @@ extern "C" int chl_graph_from_arcs(uint32_t n, size_t k, const uint32_t *src,
     return CHL_OK;
 }
 
+extern "C" int chl_graph_from_csr(uint32_t n, const uint64_t *off, const uint32_t *head,
+                                  const int32_t *len, int undirected, chl_graph **out) {
+    if (!out || !off) return CHL_ERR_INVALID;
+    if (off[0] != 0) {
+        set_error("CSR offsets must start at 0");
+        return CHL_ERR_INVALID;
+    }
+    for (uint32_t v = 0; v < n; ++v)
+        if (off[v + 1] < off[v]) {
+            set_error("CSR offsets must not decrease");
+            return CHL_ERR_INVALID;
+        }
+    const uint64_t k = off[n];
+    if (k && (!head || !len)) return CHL_ERR_INVALID;
+    std::vector<uint32_t> src;
+    try {
+        src.resize(k);
+    } catch (...) {
+        return CHL_ERR_OOM;
+    }
+    for (uint32_t v = 0; v < n; ++v)
+        for (uint64_t e = off[v]; e < off[v + 1]; ++e) src[e] = v;
+    return chl_graph_from_arcs(n, k, src.data(), head, len, undirected, out);
+}
+
 extern "C" int chl_graph_write_dimacs(const chl_graph *g, const char *path) {
     if (!g || !path) return CHL_ERR_INVALID;
     FILE *f = fopen(path, "w");

@@ -66,3 +66,36 @@ def test_oracle_reads_same_adjacency(P, O, tmp_path):
         off, head, ln = og.csr(side)
         off2, head2, ln2 = g.csr(bool(side))
         assert np.array_equal(off, off2) and np.array_equal(head, head2) and np.array_equal(ln, ln2)
+
+
+def test_graph_from_csr_matches_from_arcs(P):
+    """chl_graph_from_csr gives the arc lists chl_graph_from_arcs builds from
+    the same arcs (duplicates, loops and both directions merged alike)."""
+    import numpy as np
+    rng = np.random.default_rng(4)
+    for t in range(4):
+        n = int(rng.integers(1, 200))
+        deg = rng.integers(0, 6, n)
+        off = np.concatenate([[0], np.cumsum(deg)]).astype(np.uint64)
+        k = int(off[-1])
+        head = rng.integers(0, n, k).astype(np.uint32)
+        length = rng.integers(1, 9, k).astype(np.int32)
+        src = np.repeat(np.arange(n, dtype=np.uint32), deg)
+        for und in (False, True):
+            a = P.Graph.from_csr(n, off, head, length, und)
+            b = P.Graph.from_arcs(n, src, head, length, und)
+            assert a.get_n() == b.get_n() and a.get_m() == b.get_m()
+            for fwd in (True, False):
+                for x, y in zip(a.csr(fwd), b.csr(fwd)):
+                    assert np.array_equal(x, y)
+
+
+def test_graph_from_csr_rejects_bad_input(P):
+    import numpy as np
+    import pytest
+    with pytest.raises(P.CHLError):
+        P.Graph.from_csr(2, np.array([0, 2, 1], np.uint64), [1, 0], [1, 1])   # decreasing offsets
+    with pytest.raises(P.CHLError):
+        P.Graph.from_csr(2, np.array([0, 1, 2], np.uint64), [1, 5], [1, 1])   # head out of range
+    with pytest.raises(P.CHLError):
+        P.Graph.from_csr(2, np.array([0, 1], np.uint64), [1], [1])           # off too short
