@@ -14,9 +14,14 @@ label build (all roots, canonical labels) with the graph resident in HBM.
   e2e    : labels/s through the C ABI from host buffers: graph + order
            upload, build, and the labels read back to host memory, timed on
            the host around each step
-  roofline: tree kernel, algorithmic bytes (sequential-PLL work of the
-           labelled vertices: 8 B per relaxed arc + 8 B per label entry the
-           prune test reads + 8 B per label written) / tree-kernel time
+  roofline: tree kernel, algorithmic bytes / tree-kernel time.  The bytes
+           are sequential PLL's (roots one at a time in rank order, each
+           tree pruned with the complete labels of higher-ranked hubs):
+           8 B per entry of every settled vertex's label list, per out-arc
+           of every settled vertex and per label written, counted once per
+           workload by oracle/pll_trace.py into profiles/pll_trace_*.json;
+           without such a file, the closed form over the labelled vertices
+           (a lower bound) stands in
   cpu_baseline: the CPU restatement of the reference GLL (OpenMP, all host
            cores) on a bounded sample: the first R roots of the same build
 
@@ -162,6 +167,18 @@ def profile_traffic():
         return None
 
 
+def profile_trace(args):
+    """Sequential PLL work counts of this workload (oracle/pll_trace.py), or
+    None when no trace is committed for it."""
+    p = os.path.join(ROOT, "profiles", "pll_trace_" + workload_slug(args) + ".json")
+    try:
+        with open(p) as f:
+            t = json.load(f)
+    except Exception:
+        return None
+    return t if t.get("workload") == workload_name(args) else None
+
+
 def make_workload(P, args, cpu_order=False):
     """The graph (host-side seeded generator) and its order: on the GPU, or
     with the CPU oracle's identical degree / betweenness order when the
@@ -181,6 +198,13 @@ def make_workload(P, args, cpu_order=False):
     if args.workload == "rmat":
         return g, P.Order.degree(g, seed=1)
     return g, P.Order.betweenness(g, args.sources, seed=1)
+
+
+def workload_slug(args):
+    """File-name form of the workload (profiles/pll_trace_<slug>.json)."""
+    if args.workload == "rmat":
+        return f"rmat{args.scale}"
+    return f"grid{args.side}_hw{args.highways}_bc{args.sources}"
 
 
 def workload_name(args):
@@ -364,7 +388,12 @@ def run_ours(args, ws, rank):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms_step = float(t.item())
     value = ws * labels / (ms_step / 1e3)
-    work = build_work_bytes(L, g)
+    # algorithmic bytes of a build: the sequential PLL trace of this workload
+    # when one is committed, else the closed form over the labelled vertices
+    # (a lower bound: pruned visits left out)
+    labelled = build_work_bytes(L, g)
+    trace = profile_trace(args)
+    work = float(trace["algorithmic_bytes"]) if trace else labelled
     avg_tree_ms = float(np.mean(tree_ms))
     per_launch_tree = avg_tree_ms / max(1, stats[-1]["tree_launches"])
     peak, peak_kind = peaks()
@@ -406,11 +435,15 @@ def run_ours(args, ws, rank):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": (work / max(1, stats[-1]["tree_launches"]) * traffic["dram_per_algorithmic_byte"]
-                                 if traffic else None),
+                     "traffic": (work / max(1, stats[-1]["tree_launches"])
+                                 * traffic["dram_per_trace_byte" if trace else "dram_per_labelled_byte"]
+                                 if traffic and ("dram_per_trace_byte" in traffic or not trace) else None),
                      "traffic_note": ("bytes per launch, scaled from " + traffic["workload"] + " (ncu)"
                                       if traffic else None),
                      "kernel": "batch_kernel", "algorithmic_bytes_per_build": work,
+                     "work_model": ("sequential PLL trace, profiles/pll_trace_" + workload_slug(args) + ".json"
+                                    if trace else "labelled vertices only (closed form, lower bound)"),
+                     "labelled_bytes_per_build": labelled,
                      "tree_ms_per_build": avg_tree_ms, "tree_launches": stats[-1]["tree_launches"],
                      "ms_per_launch": per_launch_tree},
         "build": {"build_s": ms_step / 1e3, "avg_label": stats[-1]["avg_label"], "labels": labels,

@@ -653,6 +653,79 @@ ol_labels *og_gll(const og_graph *g, const uint32_t *order, uint32_t N, int thre
 
 /* Time the GLL restatement on the first `roots` roots only (a bounded sample
  * of a build for baselines); returns labels produced, *secs the time. */
+/* Sequential PLL trace: the work model of the build roofline.  Roots in
+ * rank order, one at a time, both sides as iteration_gll does them
+ * (shared_memory/akiba.hpp:65-125), every label committed at once, so each
+ * tree prunes with the complete labels of all higher-ranked hubs.  Counts
+ * what this sequential algorithm reads and writes:
+ *   out[0] settled vertices (popped with rank >= i)
+ *   out[1] label entries scanned by prune tests (up to the first witness)
+ *   out[2] arcs relaxed (out-arcs of the unpruned vertices)
+ *   out[3] labels written
+ *   out[4] algorithmic bytes = 8 * (out[1] + out[2] + out[3])
+ *   out[5] whole lists of the settled vertices (sum of |L_<i(u, !f)|)
+ *   out[6] out-arcs of the settled vertices
+ *   out[7] the build roofline's bytes: 8 * (out[5] + out[6] + out[3])
+ * The labels are the canonical labels (the same as og_gll's). */
+void og_pll_trace(const og_graph *g, const uint32_t *order, uint32_t N, uint64_t *out) {
+    ol_labels *L = ol_new(N);
+    uint32_t *rev = malloc((size_t)N * sizeof(uint32_t));
+    for (uint32_t i = 0; i < N; ++i) rev[order[i]] = i;
+    o_akiba ak;
+    ak_init(&ak, g->n);
+    uint64_t settled = 0, reads = 0, arcs = 0, labels = 0, lists = 0, outdeg = 0;
+    for (uint32_t i = 0; i < N; ++i) {
+        const uint32_t v = order[i];
+        for (int forward = 0; forward < 2; ++forward) {
+            const int s = forward ? 1 : 0;
+            ak_clear(&ak);
+            ak_update(&ak, v, 0);
+            {
+                const ol_list *x = &L->l[2 * (size_t)v + forward];
+                for (uint32_t k = 0; k < x->n; ++k) ak_update_tmp(&ak, x->h[k], x->d[k]);
+            }
+            while (ak.q.size) {
+                const uint32_t u = oh_pop(&ak.q);
+                const int32_t d = ak.distance[u];
+                if (rev[u] < i) continue;
+                ++settled;
+                ol_list *x = &L->l[2 * (size_t)u + !forward];
+                lists += x->n;
+                outdeg += g->off[s][u + 1] - g->off[s][u];
+                int pruned = 0;
+                for (uint32_t k = 0; k < x->n; ++k) {
+                    ++reads;
+                    const uint32_t hub = x->h[k];
+                    if (ak.label_tmp[hub] != INFTY && ak.label_tmp[hub] + x->d[k] <= d) {
+                        pruned = 1;
+                        break;
+                    }
+                }
+                if (pruned) continue;
+                ol_push(x, i, d);
+                ++labels;
+                for (uint64_t e = g->off[s][u]; e < g->off[s][u + 1]; ++e) {
+                    ++arcs;
+                    const int32_t dd = d + g->len[s][e];
+                    const uint32_t w = g->head[s][e];
+                    if (dd < ak.distance[w]) ak_update(&ak, w, dd);
+                }
+            }
+        }
+    }
+    out[0] = settled;
+    out[1] = reads;
+    out[2] = arcs;
+    out[3] = labels;
+    out[4] = 8 * (reads + arcs + labels);
+    out[5] = lists;
+    out[6] = outdeg;
+    out[7] = 8 * (lists + outdeg + labels);
+    ak_free(&ak);
+    free(rev);
+    ol_free(L);
+}
+
 uint64_t og_gll_sample(const og_graph *g, const uint32_t *order, uint32_t N, int threads,
                        uint32_t roots, double *secs) {
     ol_labels *glob = ol_new(N), *loc = ol_new(N);

@@ -42,6 +42,7 @@ _SIG = {
     "og_dijkstra": (None, [_P, C.c_uint32, C.c_int, _I32P]),
     "og_gll": (_P, [_P, _U32P, C.c_uint32, C.c_int, C.c_uint64, _F64P]),
     "og_gll_sample": (C.c_uint64, [_P, _U32P, C.c_uint32, C.c_int, C.c_uint32, _F64P]),
+    "og_pll_trace": (None, [_P, _U32P, C.c_uint32, _U64P]),
     "og_plant_all": (_P, [_P, _U32P, C.c_uint32, _U32P, _U32P]),
     "og_canonical_check": (C.c_uint64, [_P, _U32P, _P]),
     "og_degree_order": (None, [_P, C.c_uint64, _U32P]),
@@ -203,6 +204,20 @@ def gll_sample(g: OGraph, order, roots, threads=None):
     labels = lib().og_gll_sample(g.h, o.ctypes.data_as(_U32P), len(o), threads or os.cpu_count() or 1,
                                  roots, C.byref(secs))
     return labels, secs.value
+
+
+def pll_trace(g: OGraph, order) -> dict:
+    """Sequential PLL work counts (og_pll_trace): settled vertices, label
+    entries scanned by prune tests (to the first witness), arcs relaxed,
+    labels written, and the build roofline's algorithmic bytes: 8 B per
+    entry of every settled vertex's list, per out-arc of every settled
+    vertex and per label written.  Single-threaded."""
+    o = _u32(order)
+    out = (C.c_uint64 * 8)()
+    lib().og_pll_trace(g.h, o.ctypes.data_as(_U32P), len(o), out)
+    return {"settled": out[0], "label_reads": out[1], "arcs": out[2], "labels": out[3],
+            "scanned_bytes": out[4], "list_entries": out[5], "settled_out_arcs": out[6],
+            "algorithmic_bytes": out[7]}
 
 
 def plant_all(g: OGraph, order):

@@ -106,3 +106,20 @@ def test_oracle_matches_live_reference_config1(P, O, tmp_path):
     out = str(tmp_path / "orc.labels")
     L.write(out)
     assert filecmp.cmp(out, ref, shallow=False)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_pll_trace_builds_the_canonical_labels(O, case):
+    """The sequential PLL behind the build roofline's work counts produces
+    the reference's labels (the same count as the GLL restatement), and its
+    counters are consistent."""
+    c = label_case(case)
+    g = O.OGraph.read_dimacs(c["gr"])
+    order = np.loadtxt(c["order"], dtype=np.uint32)[1:]
+    ref, _ = O.gll(g, order, threads=2)
+    tr = O.pll_trace(g, order)
+    assert tr["labels"] == ref.total()
+    assert tr["label_reads"] <= tr["list_entries"] and tr["arcs"] <= tr["settled_out_arcs"]
+    assert tr["settled"] >= tr["labels"]
+    assert tr["algorithmic_bytes"] == 8 * (tr["list_entries"] + tr["settled_out_arcs"] + tr["labels"])
+    assert tr["scanned_bytes"] == 8 * (tr["label_reads"] + tr["arcs"] + tr["labels"])
