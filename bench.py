@@ -444,6 +444,7 @@ def run_ours(args, ws, rank):
                      "work_model": ("sequential PLL trace, profiles/pll_trace_" + workload_slug(args) + ".json"
                                     if trace else "labelled vertices only (closed form, lower bound)"),
                      "labelled_bytes_per_build": labelled,
+                     "pll_scanned_bytes_per_build": (float(trace["scanned_bytes"]) if trace else None),
                      "tree_ms_per_build": avg_tree_ms, "tree_launches": stats[-1]["tree_launches"],
                      "ms_per_launch": per_launch_tree},
         "build": {"build_s": ms_step / 1e3, "avg_label": stats[-1]["avg_label"], "labels": labels,
