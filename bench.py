@@ -88,6 +88,22 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(x, dist):
+    """The largest x over all ranks (every rank gets it); x itself on one."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(ws, labels_per_rank, ms_step):
+    """Whole-job labels/s: every rank builds the whole labeling (replicas),
+    timed by the slowest rank."""
+    return ws * labels_per_rank / (ms_step / 1e3)
+
+
 def dist_info():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -381,13 +397,8 @@ def run_ours(args, ws, rank):
     build_ms = [s["build_ms"] for s in stats]
     tree_ms = [s["tree_ms"] for s in stats]
     labels = stats[-1]["labels"]
-    ms_step = float(np.mean(build_ms))
-    if dist is not None:
-        import torch
-        t = torch.tensor([ms_step], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = ws * labels / (ms_step / 1e3)
+    ms_step = max_over_ranks(float(np.mean(build_ms)), dist)
+    value = job_throughput(ws, labels, ms_step)
     # algorithmic bytes of a build: the sequential PLL trace of this workload
     # when one is committed, else the closed form over the labelled vertices
     # (a lower bound: pruned visits left out)
