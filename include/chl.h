@@ -176,47 +176,23 @@ typedef struct chl_build_opts {
     uint32_t first_superstep; /* roots in the first superstep, 0 = auto       */
     double growth;        /* superstep growth factor, 0 = auto                */
     uint32_t max_warps;   /* cap on concurrent trees, 0 = auto                */
-    int32_t tree_algo;    /* 0 or 2: batched settle (default), 1: binary
-                             heap, 3: settle rounds over a logged frontier
-                             with staged prune tests                      */
-    int32_t scan_order;   /* prune-test list order: 0 auto (from the end on
-                             road-like graphs, from the start on heavy-
-                             tailed ones), 1 from the end, 2 from the start */
-    int32_t cta_roots;    /* roots per superstep built by a whole block:
-                             0 auto, -1 none, > 0 that many                */
     uint32_t root_limit;  /* > 0: build the trees of ranks < root_limit only
                              (the labels of those hubs, which are final;
                              used to time schedules on a prefix)            */
-    uint32_t root_stage;  /* root-label entries staged in shared memory per
-                             tree (batched settle), 0 = auto: the most that
-                             keeps the register-limited occupancy           */
-    int32_t prune_sched;  /* batched settle prune tests: 0 auto (= 4), 1 a
-                             lane group per vertex, 2 (vertex, 32-entry
-                             chunk) items, 3 (vertex, 64-entry chunk) items,
-                             4 (vertex, 16-entry chunk) items, one per lane */
-    int32_t root_probe;   /* batched settle root-label lookups: 0 auto
-                             (= 2), 1 sorted staging + binary search, 2 hash
-                             table in shared memory                         */
-    int32_t superstep_extend; /* batched settle: while a superstep's trees
-                             run, idle warps take up to this many times its
-                             nominal roots (0 auto: 4 on road-like graphs,
-                             off on heavy-tailed ones; 1 off)               */
-    int32_t settle_rule;  /* batched settle finality test: 0 auto (= 1),
-                             1 IN criterion, 2 IN and OUT criteria          */
-    int32_t prune_order;  /* label order scanned by prune tests: 0 auto
-                             (a distance-ordered copy with lane items and the
-                             hashed root label), 1 hub order                */
+    int32_t superstep_extend; /* while a superstep's trees run, idle warps
+                             take up to this many times its nominal roots
+                             (0 auto: 4 on road-like graphs, off on heavy-
+                             tailed ones; 1 off)                            */
     uint32_t label_cap;   /* new-label buffer entries per superstep: 0 auto
                              (the label budget plus sides * n per tree still
                              running when it is spent, within a quarter of
                              free memory).  A superstep that overflows it is
                              re-run with exactly the room it needed.        */
-    int32_t queue_split;  /* batched settle near/far queue: 0 auto (road-
-                             like graphs: a tree's queue above 1024 vertices
-                             is split, about 256 kept near; heavy-tailed
-                             ones: off), 1 off, q > 1: split above q (about
-                             q / 4 near); off with settle_rule 2            */
-    uint32_t reserved[1];
+    int32_t queue_split;  /* near/far queue: 0 auto (road-like graphs: a
+                             tree's queue above 1024 vertices is split, about
+                             256 kept near; heavy-tailed ones: off), 1 off,
+                             q > 1: split above q (about q / 4 near)        */
+    uint32_t reserved[3];
 } chl_build_opts;
 
 /* Fill opts with the defaults (hybrid, sf auto, ps 1024, autotune on,
@@ -287,6 +263,17 @@ int chl_labels_import(uint32_t n, const uint64_t *off, const uint32_t *hubs,
  * whose hub is rank(v).  Training target of the learned ranking. */
 int chl_labels_hub_freq(const chl_labels *l, const uint32_t *order,
                         uint32_t *freq);
+/* Label digest (no counterpart in the reference): a position-dependent
+ * 64-bit fingerprint, computed on the device, of the content that
+ * hl::Labeling::write (shared_memory/labeling.hpp:167-183) puts in a label
+ * file -- n, then every list 2v + side with its size and (hub, dist) entries
+ * in order.  Each item adds one SplitMix64-mixed term modulo 2^64:
+ *   M(n + C_N) + sum_i M(B_i ^ size_i) + sum_ij M(B_i ^ M(j + C_E) ^ (hub << 32 | dist)),
+ *   B_i = M(i + C_L), C_N = 0x243F6A8885A308D3, C_L = 0x13198A2E03707344,
+ *   C_E = 0xA4093822299F31D0, M(z) = the SplitMix64 finaliser.
+ * Lets a caller compare a build with a reference labeling without writing
+ * its many-GB text file. */
+int chl_labels_digest(const chl_labels *l, uint64_t *digest);
 void chl_labels_free(chl_labels *l);
 
 /* ------------------------------------------------------------------ query */

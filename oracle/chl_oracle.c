@@ -18,6 +18,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "chl_digest.h"
+
 #define INFTY INT_MAX
 
 /* ------------------------------------------------------------- graph */
@@ -266,6 +268,26 @@ ol_labels *ol_import(uint32_t n, const uint64_t *off, const uint32_t *hub, const
     for (size_t x = 0; x < 2 * (size_t)n; ++x)
         for (uint64_t k = off[x]; k < off[x + 1]; ++k) ol_push(&L->l[x], hub[k], dist[k]);
     return L;
+}
+
+/* Digest (chl_digest.h) of the content Labeling::write would emit
+ * (shared_memory/labeling.hpp:167-183): n, then every list 2v + side. */
+uint64_t ol_digest(const ol_labels *L) {
+    uint64_t dg = chd_head(L->n);
+    for (size_t x = 0; x < 2 * (size_t)L->n; ++x) {
+        const uint64_t base = chd_list_base(x);
+        dg += chd_list_term(base, L->l[x].n);
+        for (uint32_t k = 0; k < L->l[x].n; ++k) dg += chd_entry_term(base, k, L->l[x].h[k], (uint32_t)L->l[x].d[k]);
+    }
+    return dg;
+}
+
+/* Digest of an order (rank -> vertex), as written by Order::write
+ * (shared_memory/ordering.hpp:37-49). */
+uint64_t og_order_digest(const uint32_t *order, uint32_t n) {
+    uint64_t dg = chd_head(n);
+    for (uint32_t i = 0; i < n; ++i) dg += chd_order_term(i, order[i]);
+    return dg;
 }
 
 /* Labeling::write (shared_memory/labeling.hpp:167-183) */

@@ -16,7 +16,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
-REF_SRC = os.environ.get("CHL_REFERENCE", "/root/reference")
+# the reference checkout: $CHL_REFERENCE, else a directory named `reference`
+# beside this repository (absent on hosts that only run the prebuilt tests)
+REF_SRC = os.environ.get("CHL_REFERENCE") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 _P = C.c_void_p
 _U32P = C.POINTER(C.c_uint32)
@@ -49,6 +51,8 @@ _SIG = {
     "og_bc_sources": (None, [C.c_uint32, C.c_uint32, C.c_uint64, _U32P]),
     "og_betweenness": (None, [_P, _U32P, C.c_uint32, _F64P]),
     "og_betweenness_order": (None, [_P, C.c_uint32, C.c_uint64, _U32P]),
+    "ol_digest": (C.c_uint64, [_P]),
+    "og_order_digest": (C.c_uint64, [_U32P, C.c_uint32]),
 }
 
 _lib = None
@@ -172,6 +176,10 @@ class OLabels:
         lib().ol_export(self.h, off.ctypes.data_as(_U64P), hub.ctypes.data_as(_U32P), dist.ctypes.data_as(_I32P))
         return off, hub[:t], dist[:t]
 
+    def digest(self):
+        """Label digest (oracle/chl_digest.h) of these labels."""
+        return int(lib().ol_digest(self.h))
+
     def write(self, path):
         if lib().ol_write(self.h, os.fsencode(path)):
             raise IOError(path)
@@ -187,6 +195,12 @@ class OLabels:
         if getattr(self, "h", None) and _lib is not None:
             _lib.ol_free(self.h)
             self.h = None
+
+
+def order_digest(order) -> int:
+    """Order digest (oracle/chl_digest.h)."""
+    o = _u32(order)
+    return int(lib().og_order_digest(o.ctypes.data_as(_U32P), len(o)))
 
 
 def gll(g: OGraph, order, threads=None, sf=32):

@@ -49,12 +49,9 @@ class BuildOpts(C.Structure):
     _fields_ = [("mode", C.c_int32), ("sf", C.c_double), ("ps", C.c_double),
                 ("autotune", C.c_int32), ("use_graphs", C.c_int32), ("verbose", C.c_int32),
                 ("first_superstep", C.c_uint32), ("growth", C.c_double),
-                ("max_warps", C.c_uint32), ("tree_algo", C.c_int32), ("scan_order", C.c_int32),
-                ("cta_roots", C.c_int32), ("root_limit", C.c_uint32), ("root_stage", C.c_uint32),
-                ("prune_sched", C.c_int32), ("root_probe", C.c_int32),
-                ("superstep_extend", C.c_int32), ("settle_rule", C.c_int32),
-                ("prune_order", C.c_int32), ("label_cap", C.c_uint32), ("queue_split", C.c_int32),
-                ("reserved", C.c_uint32 * 1)]
+                ("max_warps", C.c_uint32), ("root_limit", C.c_uint32),
+                ("superstep_extend", C.c_int32), ("label_cap", C.c_uint32), ("queue_split", C.c_int32),
+                ("reserved", C.c_uint32 * 3)]
 
 
 class BuildStats(C.Structure):
@@ -124,6 +121,7 @@ SIGNATURES = {
     "chl_labels_export": (C.c_int, [_P, _U64P, _U32P, _I32P]),
     "chl_labels_import": (C.c_int, [C.c_uint32, _U64P, _U32P, _I32P, C.POINTER(_P)]),
     "chl_labels_hub_freq": (C.c_int, [_P, _U32P, _U32P]),
+    "chl_labels_digest": (C.c_int, [_P, _U64P]),
     "chl_labels_save": (C.c_int, [_P, C.c_char_p]),
     "chl_labels_load": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
     "chl_labels_free": (None, [_P]),
@@ -414,6 +412,13 @@ class Labeling:
         _check(lib().chl_build_get_stats(self._h, C.byref(s)), "stats")
         return s.as_dict()
 
+    def digest(self) -> int:
+        """64-bit fingerprint of the label file's content, computed on the
+        device (chl_labels_digest)."""
+        d = C.c_uint64()
+        _check(lib().chl_labels_digest(self._h, C.byref(d)), "label digest")
+        return int(d.value)
+
     def hub_freq(self, order) -> np.ndarray:
         o = _u32(order)
         f = np.zeros(self.n(), np.uint32)
@@ -431,12 +436,10 @@ class Labeling:
 
 
 def build(g: Graph, order, mode: int = MODE_HYBRID, sf: float = 0.0, ps: float = 1024.0,
-          verbose: int = 0, max_warps: int = 0, autotune: int = 1, tree_algo: int = 0,
-          first_superstep: int = 0, growth: float = 0.0, scan_order: int = 0,
-          cta_roots: int = 0, use_graphs: Optional[int] = None, root_limit: int = 0,
-          root_stage: int = 0, prune_sched: int = 0, root_probe: int = 0,
-          superstep_extend: int = 0, settle_rule: int = 0, prune_order: int = 0,
-          label_cap: int = 0, queue_split: int = 0) -> Labeling:
+          verbose: int = 0, max_warps: int = 0, autotune: int = 1,
+          first_superstep: int = 0, growth: float = 0.0,
+          use_graphs: Optional[int] = None, root_limit: int = 0,
+          superstep_extend: int = 0, label_cap: int = 0, queue_split: int = 0) -> Labeling:
     o = _u32(order)
     opts = BuildOpts()
     lib().chl_build_opts_default(C.byref(opts))
@@ -446,20 +449,12 @@ def build(g: Graph, order, mode: int = MODE_HYBRID, sf: float = 0.0, ps: float =
     opts.verbose = verbose
     opts.max_warps = max_warps
     opts.autotune = autotune
-    opts.tree_algo = tree_algo
     opts.first_superstep = first_superstep
     opts.growth = growth
-    opts.scan_order = scan_order
-    opts.cta_roots = cta_roots
     if use_graphs is not None:
         opts.use_graphs = use_graphs
     opts.root_limit = root_limit
-    opts.root_stage = root_stage
-    opts.prune_sched = prune_sched
-    opts.root_probe = root_probe
     opts.superstep_extend = superstep_extend
-    opts.settle_rule = settle_rule
-    opts.prune_order = prune_order
     opts.label_cap = label_cap
     opts.queue_split = queue_split
     h = C.c_void_p()

@@ -1,14 +1,12 @@
 """Schedule autotuner for the label build.
 
-The build's speed depends on five schedule knobs: the roots in the first
-superstep, the superstep growth factor, the label budget per superstep, how
-many of a superstep's first roots are built by a whole block instead of one
-warp, and the queue size at which a tree's queue is split into near and far
-parts.  The labels never depend on them (canonical labels are unique for
-an order), and the labels of the hubs of rank < R are final once the roots
-below R are processed, so every candidate is timed on the same exact work: a
-prefix build of the roots of rank < R (``root_limit``).  The search is
-coordinate descent over the five knobs; the winner is cached in a JSON file
+The build's speed depends on four schedule knobs: the roots in the first
+superstep, the superstep growth factor, the label budget per superstep, and
+the queue size at which a tree's queue is split into near and far parts.
+The labels never depend on them (canonical labels are unique for an order),
+and the labels of the hubs of rank < R are final once the roots below R are
+processed, so every candidate is timed on the same exact work: a prefix build of the roots of rank < R (``root_limit``).  The search is
+coordinate descent over the four knobs; the winner is cached in a JSON file
 keyed by graph statistics, so graphs of the same kind skip the search.
 
 No reference counterpart: the reference's superstep size is the fixed label
@@ -31,7 +29,6 @@ DEFAULT_CACHE = os.environ.get(
 FIRST = (0, 256, 1024, 4096)      # 0: the built-in choice from graph statistics
 GROWTH = (0.0, 0.5, 1.0, 2.0)     # 0.0: built-in
 SF = (0.0, 32.0, 128.0, 1024.0)   # label budget per superstep (x n); 0.0: built-in
-CTA = (-1, 64)                    # block-per-tree roots per superstep
 QSPLIT = (0, 1, 512, 4096)        # near/far queue split size; 0: built-in, 1: off
 
 
@@ -64,7 +61,7 @@ def _store(path, data):
 
 def tune(g: Graph, order, fraction: float = 0.02, min_roots: int = 4096, repeats: int = 1,
          cache: str | None = DEFAULT_CACHE, force: bool = False, log=None, **build_kw) -> dict:
-    """Best (first_superstep, growth, sf, cta_roots, queue_split) for g;
+    """Best (first_superstep, growth, sf, queue_split) for g;
     cached by graph_key."""
     key = graph_key(g)
     data = _load(cache) if cache else {}
@@ -87,10 +84,9 @@ def tune(g: Graph, order, fraction: float = 0.02, min_roots: int = 4096, repeats
                 log(f"autotune {key} {cfg}: {best:.1f} ms for roots < {R}")
         return timings[k]
 
-    cfg = {"first_superstep": 0, "growth": 0.0, "sf": 0.0, "cta_roots": -1, "queue_split": 0}
+    cfg = {"first_superstep": 0, "growth": 0.0, "sf": 0.0, "queue_split": 0}
     t0 = time.perf_counter()
-    for knob, values in (("first_superstep", FIRST), ("growth", GROWTH), ("sf", SF), ("cta_roots", CTA),
-                         ("queue_split", QSPLIT)):
+    for knob, values in (("first_superstep", FIRST), ("growth", GROWTH), ("sf", SF), ("queue_split", QSPLIT)):
         best_v = min(values, key=lambda v: cost({**cfg, knob: v}))
         cfg[knob] = best_v
     result = {"config": cfg, "prefix_roots": R, "prefix_ms": cost(cfg),

@@ -22,13 +22,10 @@
 //  * New labels are sorted by (vertex, side, hub) with a stable radix sort
 //    and merged into the committed CSR (double-buffered) in one pass; a
 //    second copy of every list, ordered by (distance, hub), is merged too.
-//  * The default tree kernel (batch_kernel) settles vertices in batches by
-//    the IN criterion from a near/far queue and prunes with one 16-entry
-//    item of the distance-ordered lists per lane against a shared-memory
-//    hash of the root's label.  The variants kept for comparison:
-//    tree_kernel (an indexed binary heap whose top kHeapSmem slots live in
-//    shared memory; a FIFO for unit lengths), settle_kernel (logged
-//    frontier) and cta_tree (a whole block per tree).
+//  * The tree kernel (batch_kernel) settles vertices in batches by the IN
+//    criterion from a near/far queue and prunes with one 16-entry item of
+//    the distance-ordered lists per lane against a shared-memory hash of the
+//    root's label.
 #include "chl_dev.cuh"
 
 #include <algorithm>
@@ -42,17 +39,12 @@ namespace chl {
 namespace {
 
 constexpr uint32_t kInf = 0xFFFFFFFFu;
-constexpr int kHeapSmem = 256;      // heap slots kept in shared memory per warp
 constexpr int kWarpsPerBlock = 4;
-constexpr int kStage = 32;          // label staging entries per warp
 #ifndef CHL_PHASE_TIMING
 #define CHL_PHASE_TIMING 0              // 1: per-phase clock64 counters (diagnostic builds)
 #endif
 constexpr bool kPhaseTiming = CHL_PHASE_TIMING != 0;
 // batched settle code-shape switches (for A/B measurements)
-#ifndef CHL_PROBE_ROUNDS
-#define CHL_PROBE_ROUNDS 0   // hash probe rounds resolved in lock step (measured slower)
-#endif
 #ifndef CHL_SCAN_CHUNKS
 #define CHL_SCAN_CHUNKS 4    // 32-entry frontier chunks per scan step
 #endif
@@ -89,14 +81,16 @@ struct TreeArgs {
     uint32_t n;
     int sides;                      // 1: symmetric graph, one label side stored
     const uint64_t *g_off[2];       // [f]: arcs traversed by trees of side f
-    const uint2 *g_arc[2];          // (head, length)
-    const uint32_t *g_head[2];      // heads only (unit-length graphs)
+    const uint4 *g_farc[2];         // (head, length, rank[head], 0) per arc
+    const uint2 *g_fhead[2];        // (head, rank[head]) per arc, unit lengths
+    const uint32_t *win[2];         // [f]: shortest arc into v along direction f
     const uint32_t *order;
     const uint32_t *rank;
     const uint64_t *l_off;          // committed labels, index lidx(v, side)
-    const uint2 *l_ent;
+    const uint2 *l_ent;             // entries ordered by hub
+    const uint2 *l_dent;            // the same entries ordered by (distance, hub)
     uint32_t r0, r_end;
-    uint32_t r_hard;                // batch kernel: roots past r_end taken while nominal trees run
+    uint32_t r_hard;                // roots past r_end taken while nominal trees run
     unsigned long long budget;
     int hub_bits;
     uint64_t *out_key;
@@ -106,31 +100,12 @@ struct TreeArgs {
     uint32_t *tree_labels;
     uint32_t *ws_key;               // per warp slot, n entries each
     uint32_t *ws_vis;
-    uint32_t *ws_pos;
-    uint64_t *ws_heap;
+    uint32_t *ws_front;             // per warp slot: queue, next queue, far pile
     BuildCtl *ctl;
-    uint32_t rcap;                  // root label entries staged in smem
-    const uint32_t *win[2];         // [f]: shortest arc into v along direction f
-    const uint32_t *wout[2];        // [f]: shortest arc out of v along direction f
-    int out_crit;                   // batch kernel: OUT criterion on
-    const uint2 *l_dent;            // batch kernel: committed entries ordered by (distance, hub)
-    int dist_order;                 // batch kernel: prune tests scan l_dent
-    const uint4 *g_farc[2];         // batch kernel: (head, length, rank[head]) per arc
-    const uint2 *g_fhead[2];        // batch kernel: (head, rank[head]) per arc, unit lengths
-    uint32_t *ws_front;             // per warp slot: queued (unsettled) vertices
-    int scan_back;                  // prune tests read label lists from the end
-    int chunk_sched;                // batch kernel: prune tests as (vertex, chunk) items
-    uint32_t hash_slots;            // batch kernel: root hash table slots (0: sorted staging)
-    int wide;                       // chunk schedule: 64-entry items instead of 32
-    int lane_items;                 // chunk schedule: one 16-entry item per lane
+    uint32_t hash_slots;            // root hash table slots (a power of two)
     uint32_t hash_shift;            // 32 - log2(hash_slots)
-    uint32_t r_big;                 // roots below r_big: one block per tree
-    uint32_t smem_block;            // dynamic shared memory of a block (bytes)
-    const uint16_t *win16[2];       // win clamped to 65535 (a valid lower bound)
-    uint2 *ws_fq;                   // per warp slot: queue log (vertex, distance)
-    uint32_t fq_cap;                // log entries per slot
-    uint32_t near_on;               // batch kernel: queue size that starts the near/far split (0: never)
-    uint32_t near_target;           // batch kernel: near entries aimed at per refill
+    uint32_t near_on;               // queue size that starts the near/far split (0: never)
+    uint32_t near_target;           // near entries aimed at per refill
 };
 
 // Phase-timing clock: with CHL_PHASE_TIMING it is also a compiler memory
@@ -145,355 +120,6 @@ __device__ __forceinline__ long long phase_clock() {
 
 __device__ __forceinline__ uint32_t lidx(uint32_t v, int side, int sides) {
     return sides == 1 ? v : 2 * v + (uint32_t)side;
-}
-
-// --------------------------------------------------------------- heap
-// Indexed binary min-heap on (key << 32 | vertex).  Slot i lives in shared
-// memory when i < kHeapSmem, else in the warp's global overflow array.
-struct Heap {
-    uint64_t *sh;
-    uint64_t *gh;
-    uint32_t *pos;
-    uint32_t size;
-    uint32_t cap;                   // kHeapSmem + overflow slots
-
-    __device__ __forceinline__ uint64_t *slot(uint32_t i) const {
-        return i < (uint32_t)kHeapSmem ? sh + i : gh + (i - kHeapSmem);
-    }
-    __device__ void sift_up(uint32_t i, uint64_t e) {
-        while (i > 0) {
-            uint32_t p = (i - 1) >> 1;
-            uint64_t pe = *slot(p);
-            if (pe <= e) break;
-            *slot(i) = pe;
-            pos[(uint32_t)pe] = i;
-            i = p;
-        }
-        *slot(i) = e;
-        pos[(uint32_t)e] = i;
-    }
-    __device__ bool push(uint32_t v, uint32_t key) {
-        if (size >= cap) return false;
-        sift_up(size++, ((uint64_t)key << 32) | v);
-        return true;
-    }
-    __device__ void decrease(uint32_t v, uint32_t key) {
-        sift_up(pos[v], ((uint64_t)key << 32) | v);
-    }
-    __device__ uint64_t pop() {
-        uint64_t top = *slot(0);
-        uint32_t n = --size;
-        if (n > 0) {
-            uint64_t e = *slot(n);
-            uint32_t i = 0;
-            while (true) {
-                uint32_t c = 2 * i + 1;
-                if (c >= n) break;
-                uint64_t ce = *slot(c);
-                if (c + 1 < n) {
-                    uint64_t c2 = *slot(c + 1);
-                    if (c2 < ce) {
-                        ce = c2;
-                        ++c;
-                    }
-                }
-                if (e <= ce) break;
-                *slot(i) = ce;
-                pos[(uint32_t)ce] = i;
-                i = c;
-            }
-            *slot(i) = e;
-            pos[(uint32_t)e] = i;
-        }
-        return top;
-    }
-};
-
-// ---------------------------------------------------------- prune test
-// Does some committed hub h give rootlabel[h] + L(u)[h] <= d?  The root
-// label (sorted by hub) is searched by every lane for its own entry of L(u);
-// L(u) is streamed 32 entries per step (coalesced 256-byte reads).  Returns
-// the number of entries read in *nread.
-__device__ __forceinline__ bool prune_test(const uint32_t *rh, const uint32_t *rd,
-                                           int rstride, uint32_t R, const uint2 *lu,
-                                           uint32_t Lu, uint32_t d, uint32_t &nread) {
-    const uint32_t lane = lane_id();
-    for (uint32_t base = 0; base < Lu; base += 32) {
-        uint32_t k = base + lane;
-        bool hit = false;
-        if (k < Lu) {
-            uint2 e = lu[k];
-            uint32_t lo = 0, hi = R;
-            while (lo < hi) {
-                uint32_t mid = (lo + hi) >> 1;
-                if (rh[(size_t)mid * rstride] < e.x) lo = mid + 1;
-                else hi = mid;
-            }
-            if (lo < R && rh[(size_t)lo * rstride] == e.x &&
-                rd[(size_t)lo * rstride] + e.y <= d)
-                hit = true;
-        }
-        if (__any_sync(kFull, hit)) {
-            nread += min(32u, Lu - base) + base;
-            return true;
-        }
-    }
-    nread += Lu;
-    return false;
-}
-
-// ------------------------------------------------------------ tree kernel
-
-template <bool UNIT, bool PLANT>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
-tree_kernel(TreeArgs a) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
-    const uint32_t slot = blockIdx.x * kWarpsPerBlock + wib;
-    const size_t per_warp = (size_t)a.rcap * 8 + (UNIT ? 0 : kHeapSmem * 8) + kStage * 12;
-    unsigned char *base = smem + wib * per_warp;
-    uint32_t *s_rh = (uint32_t *)base;
-    uint32_t *s_rd = s_rh + a.rcap;
-    uint64_t *s_heap = (uint64_t *)(base + (size_t)a.rcap * 8);
-    uint64_t *s_sk = (uint64_t *)(base + (size_t)a.rcap * 8 + (UNIT ? 0 : kHeapSmem * 8));
-    uint32_t *s_sv = (uint32_t *)(s_sk + kStage);
-
-    uint32_t *key = a.ws_key + (size_t)slot * a.n;
-    uint32_t *vis = a.ws_vis + (size_t)slot * a.n;
-    Heap heap;
-    if (!UNIT) {
-        heap.sh = s_heap;
-        heap.gh = a.ws_heap + (size_t)slot * a.n;
-        heap.pos = a.ws_pos + (size_t)slot * a.n;
-        heap.size = 0;
-        heap.cap = a.n + kHeapSmem;
-    }
-    uint32_t nstage = 0;
-    unsigned long long c_vis = 0, c_reads = 0, c_arcs = 0;
-
-    auto flush = [&]() {
-        unsigned long long b = 0;
-        if (lane == 0) b = atomicAdd(&a.ctl->nlab, (unsigned long long)nstage);
-        b = __shfl_sync(kFull, b, 0);
-        __syncwarp();
-        if (lane < nstage) {
-            unsigned long long p = b + lane;
-            if (p < a.out_cap) {
-                a.out_key[p] = s_sk[lane];
-                a.out_val[p] = s_sv[lane];
-            } else {
-                a.ctl->overflow = 1;
-            }
-        }
-        __syncwarp();
-        nstage = 0;
-    };
-
-    while (true) {
-        uint32_t r = kInf;
-        if (lane == 0) {
-            unsigned long long used = *(volatile unsigned long long *)&a.ctl->nlab;
-            if (used < a.budget) {
-                unsigned long long t = atomicAdd(&a.ctl->next_root, 1ull);
-                if (t < a.r_end) r = (uint32_t)t;
-            }
-        }
-        r = __shfl_sync(kFull, r, 0);
-        if (r == kInf) break;
-        uint32_t t_size = 0, t_lab = 0;
-        const uint32_t v = a.order[r];
-        for (int sd = 0; sd < a.sides; ++sd) {
-            // Trees of side f walk arcs of direction f and add (r, d) to
-            // L(u, !f) (Akiba::iteration_gll's `forward`).  The reference
-            // runs side false first, then side true.
-            const int f = (a.sides == 1) ? 1 : sd;
-            const uint64_t *goff = a.g_off[f];
-            const uint2 *garc = a.g_arc[f];
-            const uint32_t *ghead = a.g_head[f];
-            // stage L(v, f)
-            const uint32_t ridx = lidx(v, f, a.sides);
-            const uint64_t rb = a.l_off[ridx], re = a.l_off[ridx + 1];
-            const uint32_t R = (uint32_t)(re - rb);
-            const uint32_t *rh, *rd;
-            int rstride;
-            if (R <= a.rcap) {
-                for (uint32_t k = lane; k < R; k += 32) {
-                    uint2 e = a.l_ent[rb + k];
-                    s_rh[k] = e.x;
-                    s_rd[k] = e.y;
-                }
-                rh = s_rh;
-                rd = s_rd;
-                rstride = 1;
-            } else {
-                rh = (const uint32_t *)(a.l_ent + rb);
-                rd = rh + 1;
-                rstride = 2;
-            }
-            // root: distance 0, not via a higher-ranked vertex
-            if (lane == 0) {
-                key[v] = 1u;
-                vis[0] = v;
-                if (!UNIT) heap.push(v, 1u);
-            }
-            __syncwarp();
-            uint32_t nvis = 1, qh = 0;
-            int ql = 1;   // queued vertices with no higher-ranked ancestor
-            while (true) {
-                uint32_t u, k;
-                if (UNIT) {
-                    if (qh >= nvis) break;
-                    u = vis[qh++];
-                    k = key[u];
-                } else {
-                    uint64_t top = 0;
-                    bool empty = false;
-                    if (lane == 0) {
-                        empty = heap.size == 0;
-                        if (!empty) top = heap.pop();
-                    }
-                    empty = __shfl_sync(kFull, empty, 0);
-                    if (empty) break;
-                    top = __shfl_sync(kFull, top, 0);
-                    u = (uint32_t)top;
-                    k = (uint32_t)(top >> 32);
-                }
-                ++t_size;
-                const uint32_t d = k >> 1;
-                const bool nonvia = k & 1u;
-                if (PLANT) {
-                    if (nonvia) --ql;
-                } else {
-                    if (a.rank[u] < r) continue;   // iteration_gll :92
-                }
-                const uint32_t uidx = lidx(u, 1 - f, a.sides);
-                // Issue the independent loads of this step together: the
-                // label list bounds of u, its arc range, and the first chunk
-                // of arcs with the heads' ranks and keys.  They overlap with
-                // the prune test; if u is pruned they are simply unused.
-                const uint64_t ub = a.l_off[uidx], ue = a.l_off[uidx + 1];
-                const uint64_t ab = goff[u], ae = goff[u + 1];
-                uint32_t pw = 0, plen = 0, prank = 0, pkey = kInf;
-                if (ab + lane < ae) {
-                    if (UNIT) {
-                        pw = ghead[ab + lane];
-                        plen = 1;
-                    } else {
-                        const uint2 hl = garc[ab + lane];
-                        pw = hl.x;
-                        plen = hl.y;
-                    }
-                    if (PLANT) prank = a.rank[pw];
-                    pkey = key[pw];
-                }
-                bool pruned = false;
-                if (PLANT && R > 0 && a.rank[u] < a.r0) {
-                    pruned = true;   // committed vertex: a committed witness always exists
-                } else if (R > 0) {
-                    uint32_t nr = 0;
-                    pruned = prune_test(rh, rd, rstride, R, a.l_ent + ub, (uint32_t)(ue - ub), d, nr);
-                    c_reads += nr;
-                }
-                if (!pruned) {
-                    if (!PLANT || nonvia) {
-                        if (lane == 0) {
-                            s_sk[nstage] = ((uint64_t)uidx << a.hub_bits) | (uint64_t)(r - a.r0);
-                            s_sv[nstage] = d;
-                        }
-                        ++nstage;
-                        ++t_lab;
-                        if (nstage == kStage) flush();
-                    }
-                    c_arcs += ae - ab;
-                    for (uint64_t e0 = ab; e0 < ae; e0 += 32) {
-                        const uint64_t e = e0 + lane;
-                        bool upd = false;
-                        uint32_t w = 0, nk = 0, old = kInf;
-                        if (e < ae) {
-                            uint32_t len, rk, kw;
-                            if (e0 == ab) {
-                                w = pw;
-                                len = plen;
-                                rk = prank;
-                                kw = pkey;
-                            } else {
-                                if (UNIT) {
-                                    w = ghead[e];
-                                    len = 1;
-                                } else {
-                                    const uint2 hl = garc[e];
-                                    w = hl.x;
-                                    len = hl.y;
-                                }
-                                rk = PLANT ? a.rank[w] : 0u;
-                                kw = key[w];
-                            }
-                            const uint64_t dd64 = (uint64_t)d + len;
-                            if (dd64 < 0x7FFFFFFFull) {
-                                const uint32_t dd = (uint32_t)dd64;
-                                uint32_t nv = 1u;
-                                if (PLANT) nv = (nonvia && rk >= r) ? 1u : 0u;
-                                nk = dd * 2u + nv;
-                                old = kw;
-                                upd = nk < old;
-                                if (upd) key[w] = nk;
-                            } else {
-                                a.ctl->err = 1;   // the reference asserts dd < infty
-                            }
-                        }
-                        const bool fresh = upd && old == kInf;
-                        const uint32_t fm = __ballot_sync(kFull, fresh);
-                        if (fresh) {
-                            const uint32_t at = nvis + __popc(fm & lanemask_lt());
-                            if (at < a.n) vis[at] = w;
-                            else a.ctl->err = 2;
-                        }
-                        nvis = min(nvis + __popc(fm), a.n);
-                        if (PLANT) {
-                            int dq = 0;
-                            if (upd) dq = (int)(nk & 1u) - (old == kInf ? 0 : (int)(old & 1u));
-                            ql += __reduce_add_sync(kFull, dq);
-                        }
-                        if (!UNIT) {
-                            uint32_t um = __ballot_sync(kFull, upd);
-                            while (um) {
-                                const int src = __ffs(um) - 1;
-                                um &= um - 1;
-                                const uint32_t w_ = __shfl_sync(kFull, w, src);
-                                const uint32_t nk_ = __shfl_sync(kFull, nk, src);
-                                const uint32_t old_ = __shfl_sync(kFull, old, src);
-                                if (lane == 0) {
-                                    if (old_ == kInf) {
-                                        if (!heap.push(w_, nk_)) a.ctl->err = 2;
-                                    } else {
-                                        heap.decrease(w_, nk_);
-                                    }
-                                }
-                            }
-                        }
-                        __syncwarp();
-                    }
-                }
-                if (PLANT && ql == 0) break;   // plant :95 early exit
-            }
-            // reset the warp's workspace for the next tree
-            c_vis += t_size;
-            for (uint32_t k = lane; k < nvis; k += 32) key[vis[k]] = kInf;
-            if (!UNIT && lane == 0) heap.size = 0;
-            __syncwarp();
-        }
-        if (lane == 0) {
-            a.tree_size[r - a.r0] = t_size;
-            a.tree_labels[r - a.r0] = t_lab;
-        }
-    }
-    if (nstage) flush();
-    // counters (one atomic per warp)
-    if (lane == 0) {
-        atomicAdd(&a.ctl->visits, c_vis);
-        atomicAdd(&a.ctl->arcs, c_arcs);
-    }
-    if (lane == 0) atomicAdd(&a.ctl->label_reads, c_reads);
 }
 
 // ------------------------------------------------------ batch tree kernel
@@ -523,87 +149,11 @@ constexpr int kBatch = CHL_KBATCH;   // settled vertices buffered per warp (<= 2
 
 constexpr int kEmit = 64;   // labels staged per warp before an append
 
-__host__ __device__ constexpr size_t batch_smem_per_warp(uint32_t rcap) {
-    return ((size_t)8 * kBatch + (size_t)4 * (2 * rcap + 7 * kBatch + 1 + 32) + 8 + (size_t)12 * kEmit + 15) &
+__host__ __device__ constexpr size_t batch_smem_per_warp(uint32_t hash_slots) {
+    return ((size_t)8 * kBatch + (size_t)8 * hash_slots + (size_t)4 * (7 * kBatch + 1 + 32) + 8 +
+            (size_t)12 * kEmit + 15) &
            ~(size_t)15;
 }
-
-__device__ __forceinline__ uint32_t bsearch_hub(const uint32_t *rh, int rstride, uint32_t R, uint32_t h) {
-    uint32_t lo = 0, hi = R;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (rh[(size_t)mid * rstride] < h) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
-}
-
-// Lower bound of h in rh[p0..R), knowing rh[p0-1] < h (or p0 == 0):
-// exponential steps, then a binary search inside the last step.
-__device__ __forceinline__ uint32_t gallop_hub(const uint32_t *rh, int rstride, uint32_t R, uint32_t p0,
-                                               uint32_t h) {
-    uint32_t lo = p0, step = 1;
-    while (lo < R && rh[(size_t)lo * rstride] < h) {
-        const uint32_t nxt = lo + step;
-        if (nxt >= R || rh[(size_t)nxt * rstride] >= h) {
-            uint32_t l2 = lo + 1, h2 = nxt < R ? nxt : R;
-            while (l2 < h2) {
-                const uint32_t mid = (l2 + h2) >> 1;
-                if (rh[(size_t)mid * rstride] < h) l2 = mid + 1;
-                else h2 = mid;
-            }
-            return l2;
-        }
-        lo = nxt;
-        step <<= 1;
-    }
-    return lo;
-}
-
-// The root's committed label as seen by the batch kernel's prune tests: the
-// first Rs entries staged in shared memory (hubs, distances), the rest read
-// from the global label array.  Lists are ascending by hub, so a probe of
-// index p < Rs never touches global memory.
-struct RootView {
-    const uint32_t *sh, *sd;   // staged prefix
-    const uint2 *g;            // whole list in global memory
-    uint32_t Rs, R;
-    __device__ __forceinline__ uint32_t hub(uint32_t p) const { return p < Rs ? sh[p] : __ldg(&g[p].x); }
-    __device__ __forceinline__ uint32_t dist(uint32_t p) const { return p < Rs ? sd[p] : __ldg(&g[p].y); }
-    // lower bound of h
-    __device__ __forceinline__ uint32_t lower(uint32_t h) const {
-        uint32_t lo = 0, hi = Rs;
-        if (Rs < R && (Rs == 0 || sh[Rs - 1] < h)) {
-            lo = Rs;
-            hi = R;
-        }
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (hub(mid) < h) lo = mid + 1;
-            else hi = mid;
-        }
-        return lo;
-    }
-    // lower bound of h in [p0, R), knowing hub(p0 - 1) < h (or p0 == 0)
-    __device__ __forceinline__ uint32_t gallop(uint32_t p0, uint32_t h) const {
-        uint32_t lo = p0, step = 1;
-        while (lo < R && hub(lo) < h) {
-            const uint32_t nxt = lo + step;
-            if (nxt >= R || hub(nxt) >= h) {
-                uint32_t l2 = lo + 1, h2 = nxt < R ? nxt : R;
-                while (l2 < h2) {
-                    const uint32_t mid = (l2 + h2) >> 1;
-                    if (hub(mid) < h) l2 = mid + 1;
-                    else h2 = mid;
-                }
-                return l2;
-            }
-            lo = nxt;
-            step <<= 1;
-        }
-        return lo;
-    }
-};
 
 // The root's committed label as an open-addressing hash table in shared
 // memory (linear probing, load <= 1/2), so the up to 8 lookups of a lane are
@@ -682,399 +232,22 @@ __device__ __forceinline__ void finish_root(const TreeArgs &a, bool nominal) {
     }
 }
 
-// ------------------------------------------------- CTA-cooperative trees
-//
-// The largest trees of a superstep (its first roots: roots go in rank
-// order) set its length.  For them the whole block (kWarpsPerBlock warps)
-// works on one tree: one shared root label (kWarpsPerBlock times the
-// capacity of a warp's), frontier scans, prune tests and relaxations split
-// over all threads, the settle list in global memory.  Same rounds and the
-// same IN criterion as the per-warp trees.
-constexpr int kBatchC = 512;
-
-struct CtaShared {
-    uint32_t nf;       // current frontier size
-    uint32_t nnext;    // entries written to the next frontier
-    uint32_t ns;       // settle-list size of the round
-    uint32_t nvis;     // touched vertices
-    int ql;            // queued vertices without a higher-ranked ancestor
-    uint32_t dnext;    // minimum queued distance after the round
-    uint32_t stop;
-    uint32_t total;    // arcs of the current batch
-    uint32_t t_size, t_lab;
-    uint32_t root;
-    uint32_t pad[5];
-};
-
-__host__ __device__ constexpr size_t cta_fixed_bytes() {
-    return sizeof(CtaShared) + (size_t)8 * kBatchC + (size_t)4 * (4 * kBatchC + 4);
-}
-
-template <bool UNIT, bool PLANT>
-__device__ void cta_tree(const TreeArgs &a, uint32_t r, unsigned char *smem, size_t smem_bytes, uint32_t *key,
-                         uint32_t *vis, uint32_t *fa, uint32_t *fb, uint32_t *S, unsigned long long &c_vis,
-                         unsigned long long &c_reads, unsigned long long &c_arcs, uint32_t &t_size_out,
-                         uint32_t &t_lab_out) {
-    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    constexpr uint32_t NT = kWarpsPerBlock * 32;
-    CtaShared &sh = *(CtaShared *)smem;
-    uint64_t *s_ba = (uint64_t *)(smem + sizeof(CtaShared));
-    uint32_t *s_bv = (uint32_t *)(s_ba + kBatchC);
-    uint32_t *s_bk = s_bv + kBatchC;
-    uint32_t *s_bp = s_bk + kBatchC;
-    uint32_t *s_bx = s_bp + kBatchC;                      // kBatchC + 1 (+3 pad)
-    uint32_t *s_rh = s_bx + kBatchC + 4;
-    const uint32_t rcapC = (uint32_t)((smem_bytes - cta_fixed_bytes()) / 8);
-    uint32_t *s_rd = s_rh + rcapC;
-    const uint32_t g = lane >> 2, sub = lane & 3;
-    const uint32_t gmask = 0xFu << (4 * g);
-    const uint32_t v = a.order[r];
-    if (tid == 0) {
-        sh.t_size = 0;
-        sh.t_lab = 0;
-    }
-    for (int sd = 0; sd < a.sides; ++sd) {
-        const int f = (a.sides == 1) ? 1 : sd;
-        const uint64_t *goff = a.g_off[f];
-        const uint2 *garc = a.g_arc[f];
-        const uint32_t *ghead = a.g_head[f];
-        const uint32_t *win = a.win[f];
-        const uint32_t ridx = lidx(v, f, a.sides);
-        const uint64_t rb = a.l_off[ridx], re = a.l_off[ridx + 1];
-        const uint32_t R = (uint32_t)(re - rb);
-        const uint32_t *rh, *rd;
-        int rstride;
-        __syncthreads();
-        if (R <= rcapC) {
-            for (uint32_t k = tid; k < R; k += NT) {
-                const uint2 e = a.l_ent[rb + k];
-                s_rh[k] = e.x;
-                s_rd[k] = e.y;
-            }
-            rh = s_rh;
-            rd = s_rd;
-            rstride = 1;
-        } else {
-            rh = (const uint32_t *)(a.l_ent + rb);
-            rd = rh + 1;
-            rstride = 2;
-        }
-        if (tid == 0) {
-            __stcg(&key[v], 1u);
-            vis[0] = v;
-            fa[0] = v;
-            sh.nf = 1;
-            sh.nvis = 1;
-            sh.ql = 1;
-            sh.stop = 0;
-        }
-        __syncthreads();
-        uint32_t dmin = 0;
-        uint32_t *cur = fa, *nxt = fb;
-        while (true) {
-            const uint32_t nf = sh.nf;
-            if (nf == 0 || sh.stop) break;
-            __syncthreads();
-            if (tid == 0) {
-                sh.ns = 0;
-                sh.nnext = 0;
-                sh.dnext = kInf;
-            }
-            __syncthreads();
-            // ---- phase 1: split the frontier into settle list and next frontier
-            uint32_t dn = kInf;
-            for (uint32_t c0 = warp * 32; c0 < nf; c0 += NT) {
-                const uint32_t i = c0 + lane;
-                const bool valid = i < nf;
-                const uint32_t x = valid ? cur[i] : 0u;
-                const uint32_t kx = valid ? __ldcg(&key[x]) : kInf;
-                const bool take = valid && (uint64_t)(kx >> 1) < (uint64_t)dmin + win[x];
-                const bool kp = valid && !take;
-                const uint32_t tm = __ballot_sync(kFull, take), km = __ballot_sync(kFull, kp);
-                uint32_t bs = 0, bk = 0;
-                if (lane == 0) {
-                    if (tm) bs = atomicAdd(&sh.ns, (uint32_t)__popc(tm));
-                    if (km) bk = atomicAdd(&sh.nnext, (uint32_t)__popc(km));
-                }
-                bs = __shfl_sync(kFull, bs, 0);
-                bk = __shfl_sync(kFull, bk, 0);
-                if (take) S[bs + __popc(tm & lanemask_lt())] = x;
-                if (kp) {
-                    nxt[bk + __popc(km & lanemask_lt())] = x;
-                    dn = min(dn, kx >> 1);
-                }
-            }
-            dn = __reduce_min_sync(kFull, dn);
-            if (lane == 0 && dn != kInf) atomicMin(&sh.dnext, dn);
-            __syncthreads();
-            const uint32_t ns = sh.ns;
-            // ---- phase 2: settle the list in batches of kBatchC
-            for (uint32_t b0 = 0; b0 < ns; b0 += kBatchC) {
-                const uint32_t nb = min((uint32_t)kBatchC, ns - b0);
-                int nvb = 0;
-                for (uint32_t j = tid; j < nb; j += NT) {
-                    const uint32_t x = S[b0 + j];
-                    const uint32_t kx = __ldcg(&key[x]);
-                    const uint32_t rx = a.rank[x];
-                    s_bv[j] = x;
-                    s_bk[j] = kx;
-                    if (PLANT) {
-                        nvb += (int)(kx & 1u);
-                        s_bp[j] = rx < a.r0 ? 1u : 0u;
-                    } else {
-                        s_bp[j] = rx < r ? 1u : 0u;
-                    }
-                }
-                if (PLANT) {
-                    nvb = __reduce_add_sync(kFull, nvb);
-                    if (lane == 0 && nvb) atomicSub(&sh.ql, nvb);
-                }
-                if (tid == 0) sh.t_size += nb;
-                __syncthreads();
-                if (R > 0) {
-                    // 32 groups of 4 lanes: 32 vertices per block step
-                    for (uint32_t j0 = warp * 8; j0 < nb; j0 += 8 * kWarpsPerBlock) {
-                        const uint32_t j = j0 + g;
-                        const bool has = j < nb && s_bp[j] == 0;
-                        uint64_t lb = 0, le = 0;
-                        uint32_t dj = 0;
-                        if (has) {
-                            const uint32_t xu = lidx(s_bv[j], 1 - f, a.sides);
-                            lb = a.l_off[xu];
-                            le = a.l_off[xu + 1];
-                            dj = s_bk[j] >> 1;
-                        }
-                        const uint64_t st = lb & ~1ull;
-                        const uint32_t nch = has ? (uint32_t)((le - st + 31) >> 5) : 0u;
-                        bool found = false;
-                        uint32_t nread = 0;
-                        for (uint32_t k = 0;; ++k) {
-                            const bool act = !found && k < nch;
-                            if (!__any_sync(kFull, act)) break;
-                            bool hit = false;
-                            if (act) {
-                                const uint32_t ck = a.scan_back ? nch - 1 - k : k;
-                                const uint64_t e0 = st + 32ull * ck + 8 * sub;
-                                uint4 q[4];
-#pragma unroll
-                                for (int t = 0; t < 4; ++t) {
-                                    q[t] = make_uint4(0, 0, 0, 0);
-                                    if (e0 + 2 * t < le) q[t] = *(const uint4 *)(a.l_ent + e0 + 2 * t);
-                                }
-                                uint32_t p = 0;
-                                bool first = true;
-#pragma unroll
-                                for (int t = 0; t < 8; ++t) {
-                                    const uint64_t e = e0 + t;
-                                    const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
-                                    const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
-                                    if (e >= lb && e < le) {
-                                        if (first) {
-                                            p = bsearch_hub(rh, rstride, R, hh);
-                                            first = false;
-                                        } else {
-                                            p = gallop_hub(rh, rstride, R, p, hh);
-                                        }
-                                        if (p < R && rh[(size_t)p * rstride] == hh &&
-                                            rd[(size_t)p * rstride] + dd <= dj)
-                                            hit = true;
-                                    }
-                                }
-                                nread += 8;
-                            }
-                            const uint32_t hm = __ballot_sync(kFull, hit) & gmask;
-                            if (act && hm) found = true;
-                        }
-                        c_reads += nread;
-                        if (has && sub == 0 && found) s_bp[j] = 1;
-                    }
-                    __syncthreads();
-                }
-                // labels
-                for (uint32_t j0 = warp * 32; j0 < nb; j0 += NT) {
-                    const uint32_t j = j0 + lane;
-                    bool emit = false;
-                    uint32_t xu = 0, dj = 0;
-                    if (j < nb && s_bp[j] == 0) {
-                        const uint32_t kx = s_bk[j];
-                        emit = !PLANT || (kx & 1u);
-                        xu = lidx(s_bv[j], 1 - f, a.sides);
-                        dj = kx >> 1;
-                    }
-                    const uint32_t em = __ballot_sync(kFull, emit);
-                    if (em) {
-                        unsigned long long bb = 0;
-                        if (lane == 0) {
-                            bb = atomicAdd(&a.ctl->nlab, (unsigned long long)__popc(em));
-                            atomicAdd(&sh.t_lab, (uint32_t)__popc(em));
-                        }
-                        bb = __shfl_sync(kFull, bb, 0);
-                        if (emit) {
-                            const unsigned long long p = bb + __popc(em & lanemask_lt());
-                            if (p < a.out_cap) {
-                                a.out_key[p] = ((uint64_t)xu << a.hub_bits) | (uint64_t)(r - a.r0);
-                                a.out_val[p] = dj;
-                            } else {
-                                a.ctl->overflow = 1;
-                            }
-                        }
-                    }
-                }
-                // degree prefix over the batch: each thread owns 4 consecutive entries
-                {
-                    uint32_t dl[4];
-                    uint32_t sum = 0;
-#pragma unroll
-                    for (int t = 0; t < 4; ++t) {
-                        const uint32_t j = tid * 4 + t;
-                        uint32_t deg = 0;
-                        if (j < nb && s_bp[j] == 0) {
-                            const uint32_t x = s_bv[j];
-                            const uint64_t ab = goff[x];
-                            deg = (uint32_t)(goff[x + 1] - ab);
-                            s_ba[j] = ab;
-                        }
-                        dl[t] = deg;
-                        sum += deg;
-                    }
-                    uint32_t incl = sum;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const uint32_t y = __shfl_up_sync(kFull, incl, o);
-                        if (lane >= (uint32_t)o) incl += y;
-                    }
-                    // warp totals through the settle-list slots past the batch
-                    __shared__ uint32_t wtot[kWarpsPerBlock];
-                    if (lane == 31) wtot[warp] = incl;
-                    __syncthreads();
-                    uint32_t off = 0;
-                    for (uint32_t w2 = 0; w2 < warp; ++w2) off += wtot[w2];
-                    uint32_t run = off + incl - sum;
-#pragma unroll
-                    for (int t = 0; t < 4; ++t) {
-                        const uint32_t j = tid * 4 + t;
-                        if (j < nb) s_bx[j] = run;
-                        run += dl[t];
-                    }
-                    if (tid == NT - 1) {
-                        uint32_t tot = 0;
-                        for (uint32_t w2 = 0; w2 < kWarpsPerBlock; ++w2) tot += wtot[w2];
-                        s_bx[nb] = tot;
-                        sh.total = tot;
-                    }
-                    __syncthreads();
-                }
-                const uint32_t total = sh.total;
-                if (tid == 0) c_arcs += total;
-                // relaxations, flattened over all threads
-                uint32_t dn2 = kInf;
-                for (uint32_t t0 = warp * 32; t0 < total; t0 += NT) {
-                    const uint32_t t = t0 + lane;
-                    bool upd = false;
-                    uint32_t w = 0, nk = 0, old = kInf;
-                    if (t < total) {
-                        uint32_t lo = 0, hi = nb;
-                        while (hi - lo > 1) {
-                            const uint32_t mid = (lo + hi) >> 1;
-                            if (s_bx[mid] <= t) lo = mid;
-                            else hi = mid;
-                        }
-                        const uint64_t e = s_ba[lo] + (t - s_bx[lo]);
-                        uint32_t len;
-                        if (UNIT) {
-                            w = ghead[e];
-                            len = 1;
-                        } else {
-                            const uint2 hl = garc[e];
-                            w = hl.x;
-                            len = hl.y;
-                        }
-                        const uint32_t kx = s_bk[lo];
-                        const uint64_t dd64 = (uint64_t)(kx >> 1) + len;
-                        if (dd64 < 0x7FFFFFFFull) {
-                            uint32_t nv = 1u;
-                            if (PLANT) nv = ((kx & 1u) && a.rank[w] >= r) ? 1u : 0u;
-                            nk = (uint32_t)dd64 * 2u + nv;
-                            old = atomicMin(&key[w], nk);
-                            upd = nk < old;
-                            if (upd) dn2 = min(dn2, nk >> 1);
-                        } else {
-                            a.ctl->err = 1;
-                        }
-                    }
-                    const bool fresh = upd && old == kInf;
-                    const uint32_t fm = __ballot_sync(kFull, fresh);
-                    if (fm) {
-                        uint32_t bn = 0, bv = 0;
-                        if (lane == 0) {
-                            bn = atomicAdd(&sh.nnext, (uint32_t)__popc(fm));
-                            bv = atomicAdd(&sh.nvis, (uint32_t)__popc(fm));
-                        }
-                        bn = __shfl_sync(kFull, bn, 0);
-                        bv = __shfl_sync(kFull, bv, 0);
-                        if (fresh) {
-                            const uint32_t o = __popc(fm & lanemask_lt());
-                            if (bn + o < a.n && bv + o < a.n) {
-                                nxt[bn + o] = w;
-                                vis[bv + o] = w;
-                            } else {
-                                a.ctl->err = 2;
-                            }
-                        }
-                    }
-                    if (PLANT) {
-                        int dq = 0;
-                        if (upd) dq = (int)(nk & 1u) - (old == kInf ? 0 : (int)(old & 1u));
-                        dq = __reduce_add_sync(kFull, dq);
-                        if (lane == 0 && dq) atomicAdd(&sh.ql, dq);
-                    }
-                }
-                dn2 = __reduce_min_sync(kFull, dn2);
-                if (lane == 0 && dn2 != kInf) atomicMin(&sh.dnext, dn2);
-                __syncthreads();
-                if (tid == 0 && PLANT && sh.ql == 0) sh.stop = 1;
-                __syncthreads();
-                if (sh.stop) break;
-            }
-            if (sh.stop) break;
-            uint32_t *tmp = cur;
-            cur = nxt;
-            nxt = tmp;
-            dmin = sh.dnext;
-            __syncthreads();
-            if (tid == 0) sh.nf = min(sh.nnext, a.n);
-            __syncthreads();
-        }
-        __syncthreads();
-        const uint32_t nvis = min(sh.nvis, a.n);
-        for (uint32_t k = tid; k < nvis; k += NT) __stcg(&key[vis[k]], kInf);
-        __syncthreads();
-    }
-    if (tid == 0) {
-        c_vis += sh.t_size;
-        t_size_out = sh.t_size;
-        t_lab_out = sh.t_lab;
-    }
-}
-
 template <bool UNIT, bool PLANT>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, CHL_BATCH_MIN_BLOCKS)
 batch_kernel(TreeArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
     const uint32_t slot = blockIdx.x * kWarpsPerBlock + wib;
-    unsigned char *base = smem + wib * batch_smem_per_warp(a.rcap);
+    unsigned char *base = smem + wib * batch_smem_per_warp(a.hash_slots);
     uint64_t *s_ba = (uint64_t *)base;                 // arc begin of batch vertex
-    uint32_t *s_rh = (uint32_t *)(s_ba + kBatch);
-    uint64_t *s_tab = (uint64_t *)s_rh;                // root hash table (same space as s_rh, s_rd)
-    uint32_t *s_rd = s_rh + a.rcap;
-    uint32_t *s_bv = s_rd + a.rcap;                    // batch vertex
+    uint64_t *s_tab = s_ba + kBatch;                   // root label hash table
+    uint32_t *s_bv = (uint32_t *)(s_tab + a.hash_slots);   // batch vertex
     uint32_t *s_bk = s_bv + kBatch;                    // batch key
     uint32_t *s_bp = s_bk + kBatch;                    // 1: pruned or skipped
     uint32_t *s_bx = s_bp + kBatch;                    // arc prefix (kBatch + 1)
     uint32_t *s_tl = s_bx + kBatch + 1;                // batch indices still to test
-    uint32_t *s_bl = s_tl + kBatch;                    // label list length (chunk schedule)
-    uint32_t *s_nch = s_bl + kBatch;                   // label list chunks (chunk schedule)
+    uint32_t *s_bl = s_tl + kBatch;                    // label list length
+    uint32_t *s_nch = s_bl + kBatch;                   // label list chunks
     uint32_t *s_as = s_nch + kBatch;                   // items of the step (up to 32)
     uint64_t *s_ek = (uint64_t *)(((uintptr_t)(s_as + 32) + 7) & ~(uintptr_t)7);   // staged label keys
     uint32_t *s_ev = (uint32_t *)(s_ek + kEmit);       // staged label distances
@@ -1091,50 +264,7 @@ batch_kernel(TreeArgs a) {
     long long cyc[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};   // phase cycles (diagnostics)
     unsigned long long dcnt[4] = {0, 0, 0, 0};      // scanned, rounds, settles, far pile entries
     const long long k_start = phase_clock();
-    const uint32_t g = lane >> 2, sub = lane & 3;
-    const uint32_t gmask = 0xFu << (4 * g);
 
-    // ---- block-per-tree phase for the superstep's first (largest) roots
-    uint32_t pending = kInf;
-    bool pending_nominal = false;
-    if (a.r_big > a.r0) {
-        CtaShared &sh = *(CtaShared *)smem;
-        const size_t s0 = (size_t)blockIdx.x * kWarpsPerBlock;
-        uint32_t *key0 = a.ws_key + s0 * a.n;
-        uint32_t *vis0 = a.ws_vis + s0 * a.n;
-        uint32_t *f0 = a.ws_front + s0 * 3 * a.n;
-        uint32_t *f1 = f0 + a.n;
-        uint32_t *f2 = a.ws_front + (s0 + 1) * 3 * a.n;
-        while (true) {
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                bool nom = false;
-                sh.root = fetch_root(a, nom);
-                sh.pad[0] = nom ? 1u : 0u;
-            }
-            __syncthreads();
-            const uint32_t rc = sh.root;
-            const bool rc_nominal = sh.pad[0] != 0;
-            if (rc == kInf) break;
-            if (rc >= a.r_big) {
-                if (wib == 0) {
-                    pending = rc;   // warp 0 builds this one alone
-                    pending_nominal = rc_nominal;
-                }
-                break;
-            }
-            uint32_t ts = 0, tl = 0;
-            cta_tree<UNIT, PLANT>(a, rc, smem, a.smem_block, key0, vis0, f0, f1, f2, c_vis, c_reads, c_arcs, ts,
-                                  tl);
-            if (threadIdx.x == 0) {
-                a.tree_size[rc - a.r0] = ts;
-                a.tree_labels[rc - a.r0] = tl;
-                finish_root(a, rc_nominal);
-            }
-        }
-        __syncthreads();   // the block leaves the shared layout before warps reuse it
-    }
-    // ---- warp-per-tree phase
     // emitted labels are staged in shared memory and appended to the new
     // label arrays kEmit at a time (one atomic per flush instead of one
     // per settle round)
@@ -1158,22 +288,14 @@ batch_kernel(TreeArgs a) {
         n_emit = 0;
         __syncwarp();
     };
-    if (a.hash_slots) {
-        for (uint32_t k = lane; k < a.hash_slots; k += 32) s_tab[k] = kSlotEmpty;
-        __syncwarp();
-    }
+    for (uint32_t k = lane; k < a.hash_slots; k += 32) s_tab[k] = kSlotEmpty;
+    __syncwarp();
     while (true) {
         uint32_t r = kInf;
         bool r_nominal = false;
-        if (pending != kInf) {
-            r = pending;
-            r_nominal = pending_nominal;
-            pending = kInf;
-        } else {
-            if (lane == 0) r = fetch_root(a, r_nominal);
-            r = __shfl_sync(kFull, r, 0);
-            r_nominal = __shfl_sync(kFull, r_nominal ? 1u : 0u, 0) != 0;
-        }
+        if (lane == 0) r = fetch_root(a, r_nominal);
+        r = __shfl_sync(kFull, r, 0);
+        r_nominal = __shfl_sync(kFull, r_nominal ? 1u : 0u, 0) != 0;
         if (r == kInf) break;
         uint32_t t_size = 0, t_lab = 0;
         const uint32_t v = a.order[r];
@@ -1182,48 +304,31 @@ batch_kernel(TreeArgs a) {
             const int f = (a.sides == 1) ? 1 : sd;
             const uint64_t *goff = a.g_off[f];
             const uint32_t *win = a.win[f];
-            const uint32_t *wout = a.wout[f];
             const uint4 *farc = a.g_farc[f];
             const uint2 *fhead = a.g_fhead[f];
-            // label entries the prune tests scan: distance-ordered copy or the
-            // hub-ordered lists
-            const uint2 *lscan = a.dist_order ? a.l_dent : a.l_ent;
+            // label entries the prune tests scan: the distance-ordered copy
+            const uint2 *lscan = a.l_dent;
             const uint32_t ridx = lidx(v, f, a.sides);
             const uint64_t rb = a.l_off[ridx], re = a.l_off[ridx + 1];
             const uint32_t R = (uint32_t)(re - rb);
-            RootView root;
-            root.sh = s_rh;
-            root.sd = s_rd;
-            root.g = (const uint2 *)(a.l_ent + rb);
-            root.R = R;
-            root.Rs = a.hash_slots ? 0u : min(R, a.rcap);
-            for (uint32_t k = lane; k < root.Rs; k += 32) {
-                const uint2 e = a.l_ent[rb + k];
-                s_rh[k] = e.x;
-                s_rd[k] = e.y;
-            }
             RootHash rhash;
             rhash.tab = s_tab;
             rhash.mask = a.hash_slots - 1;
-            rhash.g = root.g;
+            rhash.g = a.l_ent + rb;
             rhash.R = R;
-            rhash.Th = 0;
             rhash.hlast = 0;
-            if (a.hash_slots) {
-                rhash.Th = min(R, a.hash_slots / 2);
-                for (uint32_t k = lane; k < rhash.Th; k += 32) {
-                    const uint2 e = a.l_ent[rb + k];
-                    const uint64_t val = ((uint64_t)e.x << 32) | e.y;
-                    uint32_t sl = slot_of(e.x, a.hash_shift);
-                    while (atomicCAS((unsigned long long *)&s_tab[sl], (unsigned long long)kSlotEmpty,
-                                     (unsigned long long)val) != (unsigned long long)kSlotEmpty)
-                        sl = (sl + 1) & rhash.mask;
-                }
-                if (rhash.Th) rhash.hlast = a.l_ent[rb + rhash.Th - 1].x;
+            rhash.Th = min(R, a.hash_slots / 2);
+            for (uint32_t k = lane; k < rhash.Th; k += 32) {
+                const uint2 e = a.l_ent[rb + k];
+                const uint64_t val = ((uint64_t)e.x << 32) | e.y;
+                uint32_t sl = slot_of(e.x, a.hash_shift);
+                while (atomicCAS((unsigned long long *)&s_tab[sl], (unsigned long long)kSlotEmpty,
+                                 (unsigned long long)val) != (unsigned long long)kSlotEmpty)
+                    sl = (sl + 1) & rhash.mask;
             }
+            if (rhash.Th) rhash.hlast = a.l_ent[rb + rhash.Th - 1].x;
             // Prune test of one lane's 16 consecutive entries of the
-            // distance-ordered L(u) against the hashed root label (the default
-            // configuration).  vm marks the entries that belong to the list;
+            // distance-ordered L(u) against the hashed root label.  vm marks the entries that belong to the list;
             // an entry beyond d(r, u) witnesses nothing and, the list being
             // in distance order, marks the list exhausted.
             auto test16d = [&](const uint4 (&q)[8], uint32_t vm, uint32_t gdj, bool &exhausted) -> bool {
@@ -1272,101 +377,6 @@ batch_kernel(TreeArgs a) {
                 }
                 return hit;
             };
-            // Prune test of one lane's (up to) 8 consecutive entries of L(u)
-            // (entries [e0, e0 + 8) of which [glb, gle) belong to the list):
-            // does some (h, dd) with the root's (h, dr) give dr + dd <= gdj?
-            auto test8 = [&](const auto &q, uint64_t e0, uint64_t glb, uint64_t gle, uint32_t gdj) -> bool {
-                constexpr int NE = (int)(sizeof(q) / sizeof(uint4)) * 2;   // entries per lane
-                bool hit = false;
-                if (a.hash_slots) {
-                    // independent first probes, then the rare collision chains
-                    uint64_t v[NE];
-                    uint32_t sl[NE];
-#pragma unroll
-                    for (int t = 0; t < NE; ++t) {
-                        const uint64_t e = e0 + t;
-                        const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
-                        v[t] = kSlotEmpty;
-                        sl[t] = 0;
-                        if (e >= glb && e < gle && hh <= rhash.hlast && rhash.Th) {
-                            sl[t] = slot_of(hh, a.hash_shift);
-                            v[t] = s_tab[sl[t]];
-                        }
-                    }
-                    // resolve the probes in rounds: every pending entry
-                    // checks its slot and loads the next one, so the probes
-                    // of one round are independent; long chains (rare at
-                    // load <= 1/2) finish one by one
-                    uint32_t pend = 0;
-#pragma unroll
-                    for (int t = 0; t < NE; ++t) {
-                        const uint64_t e = e0 + t;
-                        const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
-                        const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
-                        if (e < glb || e >= gle) continue;
-                        if (rhash.Th && hh <= rhash.hlast) {
-                            pend |= 1u << t;
-                        } else if (rhash.Th < R) {
-                            uint32_t dr;
-                            if (rhash.find_tail(hh, dr) && dr + dd <= gdj) hit = true;
-                        }
-                    }
-#pragma unroll
-                    for (int round = 0; round < CHL_PROBE_ROUNDS; ++round) {
-                        if (!pend) break;
-#pragma unroll
-                        for (int t = 0; t < NE; ++t) {
-                            if (!(pend >> t & 1u)) continue;
-                            const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
-                            const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
-                            const uint64_t w = v[t];
-                            if (w == kSlotEmpty) {
-                                pend &= ~(1u << t);
-                            } else if ((uint32_t)(w >> 32) == hh) {
-                                if ((uint32_t)w + dd <= gdj) hit = true;
-                                pend &= ~(1u << t);
-                            } else {
-                                sl[t] = (sl[t] + 1) & rhash.mask;
-                                v[t] = s_tab[sl[t]];
-                            }
-                        }
-                    }
-#pragma unroll
-                    for (int t = 0; t < NE; ++t) {
-                        if (!(pend >> t & 1u)) continue;
-                        const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
-                        const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
-                        uint64_t w = v[t];
-                        uint32_t z = sl[t];
-                        while (w != kSlotEmpty && (uint32_t)(w >> 32) != hh) {
-                            z = (z + 1) & rhash.mask;
-                            w = s_tab[z];
-                        }
-                        if (w != kSlotEmpty && (uint32_t)w + dd <= gdj) hit = true;
-                    }
-                    return hit;
-                }
-                // sorted list: the lane's 8 hubs ascend, so one binary search,
-                // then short gallops from the previous lower bound
-                uint32_t p = 0;
-                bool first = true;
-#pragma unroll
-                for (int t = 0; t < NE; ++t) {
-                    const uint64_t e = e0 + t;
-                    const uint32_t hh = (t & 1) ? q[t >> 1].z : q[t >> 1].x;
-                    const uint32_t dd = (t & 1) ? q[t >> 1].w : q[t >> 1].y;
-                    if (e >= glb && e < gle) {
-                        if (first) {
-                            p = root.lower(hh);
-                            first = false;
-                        } else {
-                            p = root.gallop(p, hh);
-                        }
-                        if (p < R && root.hub(p) == hh && root.dist(p) + dd <= gdj) hit = true;
-                    }
-                }
-                return hit;
-            };
             if (lane == 0) {
                 __stcg(&key[v], 1u);
                 vis[0] = v;
@@ -1393,16 +403,7 @@ batch_kernel(TreeArgs a) {
             // a queued vertex lowers dnext, so dnext is the exact minimum of
             // the queue after the round.
             uint32_t dnext = kInf;
-            // OUT criterion (Crauser et al.): v is also final when
-            // d(v) < min over queued u of (d(u) + shortest arc out of u) --
-            // no queued vertex can reach it with d <= d(v), so its distance
-            // and via flag are final.  omin is that minimum over the queue
-            // at the start of the round; it holds only until the first
-            // settle of the round changes the queue (out_ok).
-            uint32_t onext = kInf, omin = 0;
-            bool out_ok = false;
             auto settle = [&]() {
-                out_ok = false;
                 long long tc0 = phase_clock();
                 if (kPhaseTiming) dcnt[2]++;
                 t_size += nb;
@@ -1425,13 +426,13 @@ batch_kernel(TreeArgs a) {
                 __syncwarp();
                 long long tc1 = phase_clock();
                 cyc[1] += tc1 - tc0;
-                if (R > 0 && a.chunk_sched) {
-                    // Prune tests flattened to (vertex, 32-entry chunk) items,
+                if (R > 0) {
+                    // Prune tests flattened to (vertex, 16-entry chunk) items,
                     // chunk-major (chunk 0 of every vertex, then chunk 1, ...),
-                    // 8 lane groups taking the next 8 live items each step: a
-                    // round costs about (total chunks) / 8 steps instead of
-                    // the longest list's chunks, and an item of a vertex that
-                    // already has a witness is skipped.
+                    // one item per lane and step: a round costs about (total
+                    // chunks) / 32 steps instead of the longest list's chunks,
+                    // and an item of a vertex that already has a witness, or
+                    // whose list has passed d(r, u), is skipped.
                     uint32_t ntest = 0, maxnch = 0;
                     for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
                         const uint32_t j = j0 + lane;
@@ -1444,9 +445,7 @@ batch_kernel(TreeArgs a) {
                             const uint64_t lb = a.l_off[xu], le = a.l_off[xu + 1];
                             s_ba[j] = lb;
                             s_bl[j] = (uint32_t)(le - lb);
-                            nch = a.lane_items ? (uint32_t)((le - (lb & ~1ull) + 15) >> 4)
-                                  : a.wide     ? (uint32_t)((le - (lb & ~1ull) + 63) >> 6)
-                                               : (uint32_t)((le - (lb & ~1ull) + 31) >> 5);
+                            nch = (uint32_t)((le - (lb & ~1ull) + 15) >> 4);
                             s_nch[j] = nch;
                         }
                         maxnch = max(maxnch, __reduce_max_sync(kFull, nch));
@@ -1459,13 +458,11 @@ batch_kernel(TreeArgs a) {
                     const uint64_t inv = ((1ull << 32) + ntest - 1) / max(ntest, 1u);
                     const bool mul_div = (uint64_t)maxnch * ntest * ntest < (1ull << 32);
                     uint32_t cursor = 0, nread = 0;
-                    // items per step: one per lane group, or one per lane
-                    const uint32_t G = a.lane_items ? 32u : 8u;
                     while (true) {
-                        // the next (up to) G live items, in item order
+                        // the next (up to) 32 live items, in item order
                         uint32_t got = 0;
                         const long long tsel = phase_clock();
-                        while (got < G && cursor < nitems) {
+                        while (got < 32 && cursor < nitems) {
                             if (kPhaseTiming) cyc[9]++;
                             const uint32_t i = cursor + lane;
                             bool live = false;
@@ -1478,7 +475,7 @@ batch_kernel(TreeArgs a) {
                             }
                             const uint32_t lm = __ballot_sync(kFull, live);
                             const uint32_t nl = (uint32_t)__popc(lm);
-                            const uint32_t take = min(G - got, nl);
+                            const uint32_t take = min(32u - got, nl);
                             const uint32_t rk = __popc(lm & lanemask_lt());
                             if (live && rk < take) s_as[got + rk] = item;
                             if (take < nl) {
@@ -1493,156 +490,37 @@ batch_kernel(TreeArgs a) {
                         __syncwarp();
                         cyc[8] += phase_clock() - tsel;
                         if (got == 0) break;
-                        if (a.lane_items) {
-                            // one 16-entry item per lane (8 loads of one
-                            // 128-byte line in flight per lane)
-                            bool hit = false, exhausted = false;
-                            uint32_t lj = 0;
-                            if (lane < got) {
-                                const uint32_t item = s_as[lane];
-                                lj = item & 0xFFu;
-                                const uint32_t c = item >> 8;
-                                const uint64_t glb = s_ba[lj];
-                                const uint64_t gle = glb + s_bl[lj];
-                                const uint32_t gdj = s_bk[lj] >> 1;
-                                const uint32_t ck = (a.scan_back && !a.dist_order) ? s_nch[lj] - 1 - c : c;
-                                const uint64_t e0 = (glb & ~1ull) + 16ull * ck;
-                                uint4 q[8];
-                                if (a.dist_order && a.hash_slots) {
-                                    // entries [lo, hi) of the 16 belong to the list:
-                                    // lo is 1 only in chunk 0 of an odd start, and a
-                                    // live item has e0 < gle
-                                    const uint32_t lo = (uint32_t)(glb - min(glb, e0));
-                                    const uint64_t span = gle - e0;
-                                    const uint32_t hi = span < 16 ? (uint32_t)span : 16u;
-                                    const uint32_t vm = ((1u << hi) - 1u) & ~((1u << lo) - 1u);
-#pragma unroll
-                                    for (int t = 0; t < 8; ++t) {
-                                        q[t] = make_uint4(0, 0, 0, 0);
-                                        if ((vm >> (2 * t)) & 3u) q[t] = *(const uint4 *)(lscan + e0 + 2 * t);
-                                    }
-                                    hit = test16d(q, vm, gdj, exhausted);
-                                    nread += 16;
-                                } else {
-                                    // hub-ordered lists (the distance-ordered copy
-                                    // exists only with the hashed root label)
-#pragma unroll
-                                    for (int t = 0; t < 8; ++t) {
-                                        q[t] = make_uint4(0, 0, 0, 0);
-                                        if (e0 + 2 * t < gle) q[t] = *(const uint4 *)(lscan + e0 + 2 * t);
-                                    }
-                                    hit = test8(q, e0, glb, gle, gdj);
-                                    nread += 16;
-                                }
-                            }
-                            if (hit) s_bp[lj] = 1;
-                            else if (exhausted) atomicOr(&s_bp[lj], 2u);
-                            __syncwarp();
-                            continue;
-                        }
-                        const bool act = g < got;
-                        bool hit = false;
-                        uint32_t gj = 0;
-                        if (act) {
-                            const uint32_t item = s_as[g];
-                            gj = item & 0xFFu;
+                        // one 16-entry item per lane (8 loads of one 128-byte
+                        // line in flight per lane)
+                        bool hit = false, exhausted = false;
+                        uint32_t lj = 0;
+                        if (lane < got) {
+                            const uint32_t item = s_as[lane];
+                            lj = item & 0xFFu;
                             const uint32_t c = item >> 8;
-                            const uint64_t glb = s_ba[gj];
-                            const uint64_t gle = glb + s_bl[gj];
-                            const uint32_t gdj = s_bk[gj] >> 1;
-                            const uint32_t ck = a.scan_back ? s_nch[gj] - 1 - c : c;
-                            if (a.wide) {
-                                // 64-entry items: 16 entries (8 loads in flight) per lane
-                                const uint64_t e0 = (glb & ~1ull) + 64ull * ck + 16 * sub;
-                                uint4 q[8];
+                            const uint64_t glb = s_ba[lj];
+                            const uint64_t gle = glb + s_bl[lj];
+                            const uint32_t gdj = s_bk[lj] >> 1;
+                            const uint64_t e0 = (glb & ~1ull) + 16ull * c;
+                            // entries [lo, hi) of the 16 belong to the list: lo
+                            // is 1 only in chunk 0 of an odd start, and a live
+                            // item has e0 < gle
+                            const uint32_t lo = (uint32_t)(glb - min(glb, e0));
+                            const uint64_t span = gle - e0;
+                            const uint32_t hi = span < 16 ? (uint32_t)span : 16u;
+                            const uint32_t vm = ((1u << hi) - 1u) & ~((1u << lo) - 1u);
+                            uint4 q[8];
 #pragma unroll
-                                for (int t = 0; t < 8; ++t) {
-                                    q[t] = make_uint4(0, 0, 0, 0);
-                                    if (e0 + 2 * t < gle) q[t] = *(const uint4 *)(a.l_ent + e0 + 2 * t);
-                                }
-                                hit = test8(q, e0, glb, gle, gdj);
-                                nread += 16;
-                            } else {
-                                const uint64_t e0 = (glb & ~1ull) + 32ull * ck + 8 * sub;
-                                uint4 q[4];
-#pragma unroll
-                                for (int t = 0; t < 4; ++t) {
-                                    q[t] = make_uint4(0, 0, 0, 0);
-                                    if (e0 + 2 * t < gle) q[t] = *(const uint4 *)(a.l_ent + e0 + 2 * t);
-                                }
-                                hit = test8(q, e0, glb, gle, gdj);
-                                nread += 8;
-                            }
-                        }
-                        const uint32_t hm = __ballot_sync(kFull, hit) & gmask;
-                        if (act && hm && sub == 0) s_bp[gj] = 1;
-                        __syncwarp();
-                    }
-                    c_reads += nread;
-                    __syncwarp();
-                } else if (R > 0) {
-                    // Prune tests, dynamically scheduled over 8 lane groups:
-                    // a group of 4 lanes scans one vertex's list, each lane
-                    // reading 8 consecutive entries (256 contiguous bytes per
-                    // group and step); a group that finds a witness or reaches
-                    // the end of its list takes the next untested vertex at
-                    // once, so one long list does not hold the other groups.
-                    uint32_t ntest = 0;
-                    for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
-                        const uint32_t j = j0 + lane;
-                        const bool t = j < nb && s_bp[j] == 0;
-                        const uint32_t m = __ballot_sync(kFull, t);
-                        if (t) s_tl[ntest + __popc(m & lanemask_lt())] = j;
-                        ntest += __popc(m);
-                    }
-                    __syncwarp();
-                    const uint32_t gbase = lane & ~3u;
-                    uint32_t gj = kInf, gk = 0, gnch = 0, gdj = 0, handed = 0, nread = 0;
-                    uint64_t glb = 0, gle = 0, gst = 0;
-                    while (true) {
-                        const bool need = gj == kInf || gk >= gnch;
-                        if (need) gj = kInf;
-                        const uint32_t nm = __ballot_sync(kFull, need && sub == 0);
-                        if (need) {
-                            const uint32_t idx = handed + __popc(nm & ((1u << gbase) - 1u));
-                            if (idx < ntest) {
-                                gj = s_tl[idx];
-                                const uint32_t xu = lidx(s_bv[gj], 1 - f, a.sides);
-                                glb = a.l_off[xu];
-                                gle = a.l_off[xu + 1];
-                                gdj = s_bk[gj] >> 1;
-                                gst = glb & ~1ull;   // 16-byte aligned start
-                                gnch = (uint32_t)((gle - gst + 31) >> 5);
-                                gk = 0;
-                            }
-                        }
-                        handed = min(handed + (uint32_t)__popc(nm), ntest);
-                        const bool act = gj != kInf && gk < gnch;
-                        if (!__any_sync(kFull, act) && handed >= ntest) break;
-                        bool hit = false;
-                        if (act) {
-                            // chunk order: from the end of the list when
-                            // a.scan_back (recent, local hubs first)
-                            const uint32_t ck = a.scan_back ? gnch - 1 - gk : gk;
-                            const uint64_t e0 = gst + 32ull * ck + 8 * sub;
-                            uint4 q[4];
-#pragma unroll
-                            for (int t = 0; t < 4; ++t) {
+                            for (int t = 0; t < 8; ++t) {
                                 q[t] = make_uint4(0, 0, 0, 0);
-                                if (e0 + 2 * t < gle) q[t] = *(const uint4 *)(a.l_ent + e0 + 2 * t);
+                                if ((vm >> (2 * t)) & 3u) q[t] = *(const uint4 *)(lscan + e0 + 2 * t);
                             }
-                            hit = test8(q, e0, glb, gle, gdj);
-                            nread += 8;
+                            hit = test16d(q, vm, gdj, exhausted);
+                            nread += 16;
                         }
-                        const uint32_t hm = __ballot_sync(kFull, hit) & gmask;
-                        if (act) {
-                            if (hm) {
-                                if (sub == 0) s_bp[gj] = 1;
-                                gk = gnch;   // released next step
-                            } else {
-                                ++gk;
-                            }
-                        }
+                        if (hit) s_bp[lj] = 1;
+                        else if (exhausted) atomicOr(&s_bp[lj], 2u);
+                        __syncwarp();
                     }
                     c_reads += nread;
                     __syncwarp();
@@ -1775,10 +653,7 @@ batch_kernel(TreeArgs a) {
                             nk[c] = (uint32_t)dd64 * 2u + nv[c];
                             old[c] = atomicMin(&key[w[c]], nk[c]);
                             upd[c] = nk[c] < old[c];
-                            if (upd[c]) {
-                                dnext = min(dnext, nk[c] >> 1);
-                                if (a.out_crit) onext = min(onext, sat_add(nk[c] >> 1, wout[w[c]]));
-                            }
+                            if (upd[c]) dnext = min(dnext, nk[c] >> 1);
                         } else {
                             a.ctl->err = 1;   // the reference asserts dd < infty
                         }
@@ -1909,8 +784,6 @@ batch_kernel(TreeArgs a) {
                 const uint32_t nf0 = nf;
                 nn = 0;
                 dnext = kInf;
-                onext = kInf;
-                out_ok = a.out_crit != 0;
                 if (kPhaseTiming) {
                     dcnt[0] += nf0;
                     dcnt[1]++;
@@ -1918,8 +791,7 @@ batch_kernel(TreeArgs a) {
                 // several 32-entry chunks per step: their loads are issued
                 // together
                 auto classify = [&](bool valid, uint32_t x, uint32_t kx, uint32_t wx, uint32_t rx) {
-                    const bool take = valid && ((uint64_t)(kx >> 1) < (uint64_t)dmin + wx ||
-                                                (out_ok && (kx >> 1) < omin));
+                    const bool take = valid && (uint64_t)(kx >> 1) < (uint64_t)dmin + wx;
                     const uint32_t tm = __ballot_sync(kFull, take);
                     if (take) {
                         const uint32_t at = nb + __popc(tm & lanemask_lt());
@@ -1933,7 +805,6 @@ batch_kernel(TreeArgs a) {
                     if (kp) {
                         fnext[nn + __popc(km & lanemask_lt())] = x;
                         dnext = min(dnext, kx >> 1);
-                        if (a.out_crit) onext = min(onext, sat_add(kx >> 1, wout[x]));
                     }
                     nn += __popc(km);
                 };
@@ -1971,7 +842,6 @@ batch_kernel(TreeArgs a) {
                 }
                 nf = nn;
                 dmin = __reduce_min_sync(kFull, dnext);
-                omin = __reduce_min_sync(kFull, onext);
                 if (thr == kInf && nf > a.near_on && a.near_on) {
                     // the queue grew large: all of it goes to the far pile,
                     // and the next refill splits it
@@ -1987,9 +857,7 @@ batch_kernel(TreeArgs a) {
             c_vis += t_size;
             const long long tz0 = phase_clock();
             for (uint32_t k = lane; k < nvis; k += 32) __stcg(&key[vis[k]], kInf);
-            if (a.hash_slots) {
-                for (uint32_t k = lane; k < a.hash_slots; k += 32) s_tab[k] = kSlotEmpty;
-            }
+            for (uint32_t k = lane; k < a.hash_slots; k += 32) s_tab[k] = kSlotEmpty;
             cyc[6] += phase_clock() - tz0;
             __syncwarp();
         }
@@ -2018,414 +886,6 @@ batch_kernel(TreeArgs a) {
     }
 }
 
-// ------------------------------------------------------ settle kernel (v3)
-//
-// Per-warp trees like batch_kernel, with two changes that remove most of its
-// dependent memory round trips:
-//  * the queue is a log of (vertex, distance snapshot) entries; a key
-//    decrease appends a new entry instead of updating one in place.  The
-//    round's scan reads the log sequentially plus a 16-bit copy of win
-//    (L2-resident); only candidates read their key, and an entry whose
-//    snapshot differs from the key is stale and dropped.  The minimum
-//    snapshot over the log is the minimum queued distance (a stale entry
-//    always has a larger snapshot than its vertex's current entry).
-//  * prune tests stage the label lists of the whole batch into shared
-//    memory with cp.async, up to kStageEnt entries per fill (kStageCap per
-//    vertex per fill, round robin), so a round costs a few memory round
-//    trips instead of one per 32-entry step of every vertex.
-constexpr int kSB = 64;           // batch capacity (vertices)
-constexpr int kStageEnt = 512;    // label entries staged per fill
-constexpr int kStageCap = 128;    // entries per vertex per fill
-constexpr int kSeg = 32;          // segments (vertex pieces) per fill
-
-__host__ __device__ constexpr size_t settle_smem_per_warp(uint32_t rcap) {
-    return ((size_t)8 * kStageEnt + (size_t)8 * 4 * kSB + (size_t)8 * kSeg +
-            (size_t)4 * (4 * kSB + kSB + 1 + 3 * kSeg + 2 * rcap) + 64 + 15) &
-           ~(size_t)15;
-}
-
-__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
-    const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gsrc) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() {
-    asm volatile("cp.async.wait_all;\n" ::: "memory");
-}
-
-template <bool UNIT, bool PLANT>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
-settle_kernel(TreeArgs a) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
-    const uint32_t slot = blockIdx.x * kWarpsPerBlock + wib;
-    unsigned char *base = smem + wib * settle_smem_per_warp(a.rcap);
-    uint2 *s_buf = (uint2 *)base;                                  // staged label entries
-    uint64_t *s_ba = (uint64_t *)(s_buf + kStageEnt);              // arc begin
-    uint64_t *s_lo = s_ba + kSB;                                   // next entry to stage
-    uint64_t *s_le = s_lo + kSB;                                   // list end
-    uint64_t *s_lb = s_le + kSB;                                   // list begin
-    uint64_t *s_sge = s_lb + kSB;                                  // segment: first entry
-    uint32_t *s_bv = (uint32_t *)(s_sge + kSeg);
-    uint32_t *s_bk = s_bv + kSB;
-    uint32_t *s_bp = s_bk + kSB;
-    uint32_t *s_tl = s_bp + kSB;
-    uint32_t *s_bx = s_tl + kSB;                                   // kSB + 1
-    uint32_t *s_sgb = s_bx + kSB + 1;                              // segment: buffer start
-    uint32_t *s_sgn = s_sgb + kSeg;                                // segment: entries
-    uint32_t *s_sgj = s_sgn + kSeg;                                // segment: batch index
-    uint32_t *s_rh = s_sgj + kSeg;
-    uint32_t *s_rd = s_rh + a.rcap;
-
-    uint32_t *key = a.ws_key + (size_t)slot * a.n;
-    uint32_t *vis = a.ws_vis + (size_t)slot * a.n;
-    uint2 *fq = a.ws_fq + (size_t)slot * a.fq_cap;
-    unsigned long long c_vis = 0, c_reads = 0, c_arcs = 0;
-
-    while (true) {
-        uint32_t r = kInf;
-        if (lane == 0) {
-            unsigned long long used = *(volatile unsigned long long *)&a.ctl->nlab;
-            if (used < a.budget) {
-                unsigned long long t = atomicAdd(&a.ctl->next_root, 1ull);
-                if (t < a.r_end) r = (uint32_t)t;
-            }
-        }
-        r = __shfl_sync(kFull, r, 0);
-        if (r == kInf) break;
-        uint32_t t_size = 0, t_lab = 0;
-        const uint32_t v = a.order[r];
-        for (int sd = 0; sd < a.sides; ++sd) {
-            const int f = (a.sides == 1) ? 1 : sd;
-            const uint64_t *goff = a.g_off[f];
-            const uint2 *garc = a.g_arc[f];
-            const uint32_t *ghead = a.g_head[f];
-            const uint16_t *win = a.win16[f];
-            const uint32_t ridx = lidx(v, f, a.sides);
-            const uint64_t rb = a.l_off[ridx], re = a.l_off[ridx + 1];
-            const uint32_t R = (uint32_t)(re - rb);
-            const uint32_t *rh, *rd;
-            int rstride;
-            if (R <= a.rcap) {
-                for (uint32_t k = lane; k < R; k += 32) {
-                    const uint2 e = a.l_ent[rb + k];
-                    s_rh[k] = e.x;
-                    s_rd[k] = e.y;
-                }
-                rh = s_rh;
-                rd = s_rd;
-                rstride = 1;
-            } else {
-                rh = (const uint32_t *)(a.l_ent + rb);
-                rd = rh + 1;
-                rstride = 2;
-            }
-            if (lane == 0) {
-                __stcg(&key[v], 1u);
-                vis[0] = v;
-                fq[0] = make_uint2(v, 0u);
-            }
-            __syncwarp();
-            uint32_t nvis = 1, nf = 1;
-            int ql = 1;
-            uint32_t dmin = 0, dnext = kInf;
-            bool stop = false;
-            uint32_t nb = 0;
-
-            auto settle = [&]() {
-                t_size += nb;
-                int nv_batch = 0;
-                for (uint32_t j = lane; j < nb; j += 32) {
-                    const uint32_t kx = s_bk[j];
-                    const uint32_t rx = a.rank[s_bv[j]];
-                    uint32_t skip;
-                    if (PLANT) {
-                        nv_batch += (int)(kx & 1u);
-                        skip = rx < a.r0 ? 1u : 0u;   // committed: always pruned
-                    } else {
-                        skip = rx < r ? 1u : 0u;      // iteration_gll :92
-                    }
-                    s_bp[j] = skip;
-                }
-                if (PLANT) ql -= __reduce_add_sync(kFull, nv_batch);
-                __syncwarp();
-                if (R > 0) {
-                    // list bounds of the vertices to test
-                    uint32_t ntest = 0;
-                    for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
-                        const uint32_t j = j0 + lane;
-                        const bool t = j < nb && s_bp[j] == 0;
-                        const uint32_t m = __ballot_sync(kFull, t);
-                        if (t) {
-                            s_tl[ntest + __popc(m & lanemask_lt())] = j;
-                            const uint32_t xu = lidx(s_bv[j], 1 - f, a.sides);
-                            const uint64_t lb = a.l_off[xu], le = a.l_off[xu + 1];
-                            s_lb[j] = lb;
-                            s_le[j] = le;
-                            s_lo[j] = lb & ~1ull;   // 16-byte aligned
-                        }
-                        ntest += __popc(m);
-                    }
-                    __syncwarp();
-                    uint32_t cursor = 0;
-                    while (true) {
-                        // plan one fill (lane 0): round robin over open vertices
-                        uint32_t pos = 0, nseg = 0;
-                        if (lane == 0) {
-                            uint32_t scanned = 0;
-                            while (pos < (uint32_t)kStageEnt && nseg < (uint32_t)kSeg && scanned < ntest) {
-                                const uint32_t j = s_tl[cursor];
-                                cursor = cursor + 1 == ntest ? 0 : cursor + 1;
-                                ++scanned;
-                                const uint64_t lo = s_lo[j], le = s_le[j];
-                                if (s_bp[j] || lo >= le) continue;
-                                uint64_t take = le - lo;
-                                if (take > (uint64_t)kStageCap) take = kStageCap;
-                                if (take > (uint64_t)(kStageEnt - pos)) take = kStageEnt - pos;
-                                take = (take + 1) & ~1ull;   // whole 16-byte pairs
-                                s_sgb[nseg] = pos;
-                                s_sgn[nseg] = (uint32_t)take;
-                                s_sge[nseg] = lo;
-                                s_sgj[nseg] = j;
-                                s_lo[j] = lo + take;
-                                pos += (uint32_t)take;
-                                ++nseg;
-                            }
-                        }
-                        pos = __shfl_sync(kFull, pos, 0);
-                        nseg = __shfl_sync(kFull, nseg, 0);
-                        if (pos == 0) break;
-                        __syncwarp();
-                        // issue the copies: 16 bytes (two entries) per lane op
-                        for (uint32_t sgi = 0; sgi < nseg; ++sgi) {
-                            const uint32_t bs = s_sgb[sgi], cnt = s_sgn[sgi];
-                            const uint2 *src = a.l_ent + s_sge[sgi];
-                            for (uint32_t k = 2 * lane; k < cnt; k += 64) cp_async16(s_buf + bs + k, src + k);
-                        }
-                        cp_async_wait_all();
-                        __syncwarp();
-                        // search: each lane takes 16 consecutive staged entries
-                        const uint32_t b0 = lane * (kStageEnt / 32);
-                        const uint32_t b1 = min(b0 + (uint32_t)(kStageEnt / 32), pos);
-                        uint32_t sg = 0;
-                        {
-                            uint32_t lo = 0, hi = nseg;
-                            while (hi - lo > 1) {
-                                const uint32_t mid = (lo + hi) >> 1;
-                                if (s_sgb[mid] <= b0) lo = mid;
-                                else hi = mid;
-                            }
-                            sg = lo;
-                        }
-                        uint32_t p = 0;
-                        bool fresh_seg = true;
-                        uint32_t nread = 0;
-                        for (uint32_t b = b0; b < b1; ++b) {
-                            while (sg + 1 < nseg && s_sgb[sg + 1] <= b) {
-                                ++sg;
-                                fresh_seg = true;
-                            }
-                            const uint32_t j = s_sgj[sg];
-                            const uint64_t e = s_sge[sg] + (b - s_sgb[sg]);
-                            if (e < s_lb[j] || e >= s_le[j] || s_bp[j]) continue;
-                            const uint2 ent = s_buf[b];
-                            if (fresh_seg) {
-                                p = bsearch_hub(rh, rstride, R, ent.x);
-                                fresh_seg = false;
-                            } else {
-                                p = gallop_hub(rh, rstride, R, p, ent.x);
-                            }
-                            ++nread;
-                            if (p < R && rh[(size_t)p * rstride] == ent.x &&
-                                rd[(size_t)p * rstride] + ent.y <= (s_bk[j] >> 1))
-                                s_bp[j] = 1;
-                        }
-                        c_reads += nread;
-                        __syncwarp();
-                    }
-                }
-                // labels of unpruned (PLaNT: and not via) vertices
-                for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
-                    const uint32_t j = j0 + lane;
-                    bool emit = false;
-                    uint32_t xu = 0, dj = 0;
-                    if (j < nb && s_bp[j] == 0) {
-                        const uint32_t kx = s_bk[j];
-                        emit = !PLANT || (kx & 1u);
-                        xu = lidx(s_bv[j], 1 - f, a.sides);
-                        dj = kx >> 1;
-                    }
-                    const uint32_t em = __ballot_sync(kFull, emit);
-                    if (em) {
-                        unsigned long long bb = 0;
-                        if (lane == 0) bb = atomicAdd(&a.ctl->nlab, (unsigned long long)__popc(em));
-                        bb = __shfl_sync(kFull, bb, 0);
-                        if (emit) {
-                            const unsigned long long q = bb + __popc(em & lanemask_lt());
-                            if (q < a.out_cap) {
-                                a.out_key[q] = ((uint64_t)xu << a.hub_bits) | (uint64_t)(r - a.r0);
-                                a.out_val[q] = dj;
-                            } else {
-                                a.ctl->overflow = 1;
-                            }
-                        }
-                        t_lab += __popc(em);
-                    }
-                }
-                // arcs of the unpruned batch vertices
-                uint32_t total = 0;
-                for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
-                    const uint32_t j = j0 + lane;
-                    uint32_t deg = 0;
-                    if (j < nb && s_bp[j] == 0) {
-                        const uint32_t x = s_bv[j];
-                        const uint64_t ab = goff[x];
-                        deg = (uint32_t)(goff[x + 1] - ab);
-                        s_ba[j] = ab;
-                    }
-                    uint32_t incl = deg;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const uint32_t y = __shfl_up_sync(kFull, incl, o);
-                        if (lane >= (uint32_t)o) incl += y;
-                    }
-                    if (j < nb) s_bx[j] = total + incl - deg;
-                    total += __shfl_sync(kFull, incl, 31);
-                }
-                if (lane == 0) s_bx[nb] = total;
-                __syncwarp();
-                c_arcs += total;
-                for (uint32_t t0 = 0; t0 < total; t0 += 32) {
-                    const uint32_t t = t0 + lane;
-                    bool upd = false;
-                    uint32_t w = 0, nk = 0, old = kInf;
-                    if (t < total) {
-                        uint32_t lo = 0, hi = nb;
-                        while (hi - lo > 1) {
-                            const uint32_t mid = (lo + hi) >> 1;
-                            if (s_bx[mid] <= t) lo = mid;
-                            else hi = mid;
-                        }
-                        const uint64_t e = s_ba[lo] + (t - s_bx[lo]);
-                        uint32_t len;
-                        if (UNIT) {
-                            w = ghead[e];
-                            len = 1;
-                        } else {
-                            const uint2 hl = garc[e];
-                            w = hl.x;
-                            len = hl.y;
-                        }
-                        const uint32_t kx = s_bk[lo];
-                        const uint64_t dd64 = (uint64_t)(kx >> 1) + len;
-                        if (dd64 < 0x7FFFFFFFull) {
-                            uint32_t nv = 1u;
-                            if (PLANT) nv = ((kx & 1u) && a.rank[w] >= r) ? 1u : 0u;
-                            nk = (uint32_t)dd64 * 2u + nv;
-                            old = atomicMin(&key[w], nk);
-                            upd = nk < old;
-                        } else {
-                            a.ctl->err = 1;   // the reference asserts dd < infty
-                        }
-                    }
-                    // a new distance (fresh vertex or a strict decrease) gets
-                    // a log entry; a via flip at equal distance does not
-                    const bool fresh = upd && old == kInf;
-                    const bool logit = upd && (old == kInf || (old >> 1) != (nk >> 1));
-                    const uint32_t lm = __ballot_sync(kFull, logit);
-                    if (logit) {
-                        const uint32_t o = __popc(lm & lanemask_lt());
-                        if (nf + o < a.fq_cap) fq[nf + o] = make_uint2(w, nk >> 1);
-                        else a.ctl->err = 2;
-                        dnext = min(dnext, nk >> 1);
-                    }
-                    nf = min(nf + __popc(lm), a.fq_cap);
-                    const uint32_t fm = __ballot_sync(kFull, fresh);
-                    if (fresh) {
-                        const uint32_t o = __popc(fm & lanemask_lt());
-                        if (nvis + o < a.n) vis[nvis + o] = w;
-                        else a.ctl->err = 2;
-                    }
-                    nvis = min(nvis + __popc(fm), a.n);
-                    if (PLANT) {
-                        int dq = 0;
-                        if (upd) dq = (int)(nk & 1u) - (old == kInf ? 0 : (int)(old & 1u));
-                        ql += __reduce_add_sync(kFull, dq);
-                    }
-                }
-                __syncwarp();
-                nb = 0;
-                if (PLANT && ql == 0) stop = true;   // plant :95 early exit
-            };
-
-            while (nf > 0 && !stop) {
-                const uint32_t nf0 = nf;
-                uint32_t keep = 0;
-                dnext = kInf;
-                for (uint32_t c0 = 0; c0 < nf0 && !stop; c0 += 32) {
-                    if (nb > (uint32_t)kSB - 32) settle();
-                    if (stop) break;
-                    const uint32_t i = c0 + lane;
-                    const bool valid = i < nf0;
-                    uint2 ent = make_uint2(0u, kInf);
-                    if (valid) ent = fq[i];
-                    bool cand = false;
-                    if (valid) cand = (uint64_t)ent.y < (uint64_t)dmin + win[ent.x];
-                    bool take = false;
-                    uint32_t kx = kInf;
-                    if (cand) {
-                        kx = __ldcg(&key[ent.x]);
-                        take = (kx >> 1) == ent.y;   // else a stale entry: dropped
-                    }
-                    const uint32_t tm = __ballot_sync(kFull, take);
-                    if (take) {
-                        const uint32_t at = nb + __popc(tm & lanemask_lt());
-                        s_bv[at] = ent.x;
-                        s_bk[at] = kx;
-                    }
-                    nb += __popc(tm);
-                    const bool kp = valid && !cand;
-                    const uint32_t km = __ballot_sync(kFull, kp);
-                    if (kp) {
-                        fq[keep + __popc(km & lanemask_lt())] = ent;
-                        dnext = min(dnext, ent.y);
-                    }
-                    keep += __popc(km);
-                    __syncwarp();
-                }
-                if (nb && !stop) settle();
-                if (stop) break;
-                const uint32_t app = nf - nf0;
-                for (uint32_t t0 = 0; t0 < app; t0 += 32) {
-                    const uint32_t t = t0 + lane;
-                    uint2 x = make_uint2(0u, 0u);
-                    if (t < app) x = fq[nf0 + t];
-                    __syncwarp();
-                    if (t < app) fq[keep + t] = x;
-                    __syncwarp();
-                }
-                nf = keep + app;
-                dmin = __reduce_min_sync(kFull, dnext);
-            }
-            c_vis += t_size;
-            for (uint32_t k = lane; k < nvis; k += 32) __stcg(&key[vis[k]], kInf);
-            __syncwarp();
-        }
-        if (lane == 0) {
-            a.tree_size[r - a.r0] = t_size;
-            a.tree_labels[r - a.r0] = t_lab;
-        }
-    }
-    if (lane == 0) {
-        atomicAdd(&a.ctl->visits, c_vis);
-        atomicAdd(&a.ctl->arcs, c_arcs);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) c_reads += __shfl_xor_sync(kFull, c_reads, o);
-    if (lane == 0) atomicAdd(&a.ctl->label_reads, c_reads);
-}
-
-// Per-build arc arrays carrying the head's rank, so a relaxation reads the
-// head, the length and the rank (PLaNT's via test) with one load.
 __global__ void fat_arcs(uint64_t m, const uint2 *arc, const uint32_t *rank, uint4 *out) {
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
         const uint2 a = arc[e];
@@ -2674,18 +1134,12 @@ struct DevGraph {
     uint2 *arc[2] = {nullptr, nullptr};
     uint32_t *head[2] = {nullptr, nullptr};
     uint32_t *win[2] = {nullptr, nullptr};   // shortest arc into v, per direction
-    uint16_t *win16[2] = {nullptr, nullptr};
-    uint32_t *wout[2] = {nullptr, nullptr};  // shortest arc out of v, per direction
     void release() {
         // side 1 may alias side 0 (symmetric graphs): free each buffer once
         if (off[1] != off[0]) cudaFree(off[1]);
         if (arc[1] != arc[0]) cudaFree(arc[1]);
         if (head[1] != head[0]) cudaFree(head[1]);
         if (win[1] != win[0]) cudaFree(win[1]);
-        if (win16[1] != win16[0]) cudaFree(win16[1]);
-        if (wout[1] != wout[0]) cudaFree(wout[1]);
-        cudaFree(wout[0]);
-        cudaFree(win16[0]);
         cudaFree(off[0]);
         cudaFree(arc[0]);
         cudaFree(head[0]);
@@ -2695,8 +1149,6 @@ struct DevGraph {
             arc[s] = nullptr;
             head[s] = nullptr;
             win[s] = nullptr;
-            win16[s] = nullptr;
-            wout[s] = nullptr;
         }
     }
 };
@@ -2735,26 +1187,12 @@ int upload_graph(const chl_graph *g, DevGraph &dg, cudaStream_t st) {
         int rc = dalloc(&dg.win[s], (size_t)g->n);
         if (rc) return rc;
         CHL_CUDA(cudaMemcpy(dg.win[s], w.data(), (size_t)g->n * 4, cudaMemcpyHostToDevice));
-        std::vector<uint16_t> w16(g->n);
-        for (uint32_t v = 0; v < g->n; ++v) w16[v] = (uint16_t)std::min<uint32_t>(w[v], 65535u);
-        rc = dalloc(&dg.win16[s], (size_t)g->n);
-        if (rc) return rc;
-        CHL_CUDA(cudaMemcpy(dg.win16[s], w16.data(), (size_t)g->n * 2, cudaMemcpyHostToDevice));
-        std::vector<uint32_t> wo(g->n, 0x7FFFFFFFu);
-        for (uint32_t v = 0; v < g->n; ++v)
-            for (uint64_t i = g->off[src][v]; i < g->off[src][v + 1]; ++i)
-                wo[v] = std::min<uint32_t>(wo[v], (uint32_t)g->len[src][i]);
-        rc = dalloc(&dg.wout[s], (size_t)g->n);
-        if (rc) return rc;
-        CHL_CUDA(cudaMemcpy(dg.wout[s], wo.data(), (size_t)g->n * 4, cudaMemcpyHostToDevice));
     }
     if (nsides == 1) {
         dg.off[1] = dg.off[0];
         dg.arc[1] = dg.arc[0];
         dg.head[1] = dg.head[0];
         dg.win[1] = dg.win[0];
-        dg.win16[1] = dg.win16[0];
-        dg.wout[1] = dg.wout[0];
     }
     return CHL_OK;
 }
@@ -2796,18 +1234,14 @@ struct Build {
     uint32_t *keep = nullptr;
     uint64_t *kpre = nullptr;
     uint32_t *tsize = nullptr, *tlab = nullptr;
-    uint32_t *ws_key = nullptr, *ws_vis = nullptr, *ws_pos = nullptr, *ws_front = nullptr;
-    uint2 *ws_fq = nullptr;
-    uint32_t fq_cap = 0;
-    uint64_t *ws_heap = nullptr;
+    uint32_t *ws_key = nullptr, *ws_vis = nullptr, *ws_front = nullptr;
     BuildCtl *ctl = nullptr;
     void *tmp = nullptr;
     size_t tmp_bytes = 0;
     cudaStream_t st = nullptr;
     uint32_t warps = 0;   // warps the schedule is sized for
     uint32_t slots = 0;   // warp slots launched (workspace slots)
-    uint32_t rcap = 0;
-    uint32_t auto_stage = 2048;              // default root-label staging (batch kernel)
+    uint32_t hash_max = 2048;                // root hash slots that keep the block occupancy
     uint4 *farc[2] = {nullptr, nullptr};     // (head, length, rank[head], 0) per arc
     uint2 *fhead[2] = {nullptr, nullptr};    // (head, rank[head]) per arc, unit lengths
     cudaGraphExec_t commit_exec = nullptr;   // captured commit chain
@@ -2840,10 +1274,7 @@ struct Build {
         cudaFree(tlab);
         cudaFree(ws_key);
         cudaFree(ws_vis);
-        cudaFree(ws_pos);
         cudaFree(ws_front);
-        cudaFree(ws_fq);
-        cudaFree(ws_heap);
         cudaFree(ctl);
         cudaFree(tmp);
         if (st) cudaStreamDestroy(st);
@@ -2970,12 +1401,8 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     const bool unit = g->unit;
     size_t free_b = 0, total_b = 0;
     CHL_CUDA(cudaMemGetInfo(&free_b, &total_b));
-    // tree kernels: 0/2 batch_kernel (default; also used when block-per-tree
-    // roots are requested), 1 tree_kernel (binary heap), 3 settle_kernel
-    const bool use_settle = opts.tree_algo == 3 && opts.cta_roots <= 0;
-    const bool use_batch = opts.tree_algo == 0 || opts.tree_algo == 2 || (opts.tree_algo == 3 && opts.cta_roots > 0);
     unsigned long long prep_kernels = 0;
-    if (use_batch) {
+    {
         // arcs with their head's rank for this order
         const int nsides_g = g->symmetric ? 1 : 2;
         for (int s = 0; s < nsides_g; ++s) {
@@ -2997,50 +1424,39 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             b.fhead[1] = b.fhead[0];
         }
     }
-    const size_t per_slot = (size_t)n * (use_settle ? 24 : use_batch ? 20 : (unit ? 8 : 20));
+    // key, vis and three queue arrays per warp slot
+    const size_t per_slot = (size_t)n * 20;
     uint32_t want = (uint32_t)sms * 48;   // 12 blocks of 4 warps per SM at most
     if (opts.max_warps) want = std::min<uint32_t>(want, opts.max_warps);
     const size_t ws_budget = free_b / 3;
     uint32_t fit = (uint32_t)std::max<size_t>(1, ws_budget / std::max<size_t>(per_slot, 1));
     b.warps = std::max<uint32_t>(kWarpsPerBlock, std::min(want, fit));
     b.warps = (b.warps / kWarpsPerBlock) * kWarpsPerBlock;
-    if (use_batch) {
-        // Only the blocks resident from the start build trees: a block
-        // leaves when no root is left for the superstep, and every refusal
-        // of a root is final for it.  The grid and the workspace cover
-        // those alone (b.warps still sets the first superstep's size).
-        int nbo = 0;
-        CHL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &nbo, unit ? batch_kernel<true, true> : batch_kernel<false, true>, kWarpsPerBlock * 32, 0));
-        const uint32_t resident = (uint32_t)std::max(nbo, 1) * (uint32_t)sms * kWarpsPerBlock;
-        b.slots = std::min(b.warps, resident);
-    } else {
-        b.slots = b.warps;
-    }
+    // Only the blocks resident from the start build trees: a block leaves
+    // when no root is left for the superstep, and every refusal of a root is
+    // final for it.  The grid and the workspace cover those alone (b.warps
+    // still sets the first superstep's size).
+    int nbo = 0;
+    CHL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &nbo, unit ? batch_kernel<true, true> : batch_kernel<false, true>, kWarpsPerBlock * 32, 0));
+    nbo = std::max(nbo, 1);
+    const uint32_t resident = (uint32_t)nbo * (uint32_t)sms * kWarpsPerBlock;
+    b.slots = std::min(b.warps, resident);
     const size_t slots = b.slots;
     if ((rc = dalloc(&b.ws_key, slots * n)) || (rc = dalloc(&b.ws_vis, slots * n))) return rc;
     CHL_CUDA(cudaMemsetAsync(b.ws_key, 0xFF, slots * n * 4, b.st));
-    if (use_settle) {
-        b.fq_cap = (uint32_t)std::min<uint64_t>(2ull * n + 64, 0xFFFFFFF0ull);
-        if ((rc = dalloc(&b.ws_fq, slots * b.fq_cap))) return rc;
-    } else if (use_batch) {
-        if ((rc = dalloc(&b.ws_front, slots * 3 * (size_t)n))) return rc;   // front, fnext, far pile
-    } else if (!unit) {
-        if ((rc = dalloc(&b.ws_pos, slots * n)) || (rc = dalloc(&b.ws_heap, slots * n))) return rc;
-    }
-
-    if (use_batch) {
-        // staging capacity that keeps the register-limited block count per SM
-        int smem_sm = 0, reserved = 0, nb = 0;
+    if ((rc = dalloc(&b.ws_front, slots * 3 * (size_t)n))) return rc;   // front, fnext, far pile
+    {
+        // root hash slots that keep the register-limited block count per SM
+        int smem_sm = 0, reserved = 0;
         CHL_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, 0));
         CHL_CUDA(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, 0));
-        CHL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &nb, unit ? batch_kernel<true, true> : batch_kernel<false, true>, kWarpsPerBlock * 32, 0));
-        nb = std::max(nb, 1);
-        const size_t per_warp = ((size_t)smem_sm / nb - (size_t)reserved) / kWarpsPerBlock;
+        const size_t per_warp = ((size_t)smem_sm / nbo - (size_t)reserved) / kWarpsPerBlock;
         const size_t fixed0 = batch_smem_per_warp(0) + 16;
-        size_t cap = per_warp > fixed0 ? ((per_warp - fixed0) / 8) & ~(size_t)3 : 32;
-        b.auto_stage = (uint32_t)std::min<size_t>(2048, std::max<size_t>(32, cap));
+        const size_t cap = per_warp > fixed0 ? (per_warp - fixed0) / 8 : 64;
+        uint32_t t = 64;
+        while (2 * t <= std::min<size_t>(cap, 2048)) t *= 2;
+        b.hash_max = t;
     }
 
     // Schedule defaults from graph statistics (measured on RMAT scale 18 and
@@ -3062,20 +1478,6 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         auto_growth = heavy ? 2.0 : 0.5;
         heavy_tail = heavy;
     }
-    // prune-test defaults of the batched settle (measured on RMAT scale 18
-    // and 512/1024-square grids): 16-entry items, one per lane, root label hashed in
-    // shared memory, lists read from the end (recent, local hubs first) on
-    // road-like graphs and from the start on heavy-tailed ones
-    const int prune_sched = opts.prune_sched ? opts.prune_sched : 4;
-    const int root_probe = opts.root_probe ? opts.root_probe : 2;
-    const int scan_back = opts.scan_order ? (opts.scan_order == 1 ? 1 : 0) : (heavy_tail ? 0 : 1);
-    // OUT criterion: measured slower on the 512/1024-square grids and RMAT
-    // scale 18 (the extra loads outweigh the larger batches), so opt-in
-    const int out_crit = opts.settle_rule == 2 ? 1 : 0;
-    // prune tests over a distance-ordered copy of the labels (lane items and
-    // the hashed root label only; the copy is merged at every commit)
-    const int dist_order = (prune_sched == 4 && root_probe == 2 && opts.prune_order != 1) ? 1 : 0;
-
     // superstep loop
     // label budget per superstep (the reference's sf * N); auto: 32 on
     // heavy-tailed graphs, 1024 on road-like ones.  On road-like graphs a
@@ -3128,39 +1530,12 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         if (opts.root_limit) r_end = std::min<uint32_t>(r_end, opts.root_limit);
         BuildCtl hc;
         bool rerun = false;
-        // root label staging capacity: longest committed list, bounded by smem
-        int max_smem = 0;
-        CHL_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0));
-        const size_t fixed = use_settle ? settle_smem_per_warp(0)
-                             : use_batch ? batch_smem_per_warp(0)
-                                         : (unit ? 0 : kHeapSmem * 8) + kStage * 12;
-        size_t rcap = std::min<uint32_t>(std::max<uint32_t>(max_list, 32), 2048);
-        const size_t smem_cap = std::min<size_t>((size_t)max_smem, CHL_SMEM_CAP_KB * 1024);
-        if (use_batch) {
-            // The batch kernel stages a prefix of the root label and reads the
-            // rest from global memory, so the staging capacity trades against
-            // occupancy: by default the largest capacity that keeps the
-            // register-limited number of blocks resident per SM.
-            uint32_t cap = opts.root_stage ? opts.root_stage : b.auto_stage;
-            rcap = std::min<size_t>(rcap, std::max<uint32_t>(cap, 32));
-        }
-        uint32_t hash_slots = 0;
-        if (use_batch && root_probe == 2) {
-            // hash table: a power of two at least twice the longest root label
-            uint32_t t = 64;
-            const uint32_t tmax = opts.root_stage ? std::max<uint32_t>(opts.root_stage, 64) : 2048;
-            while (t < 2 * std::max<uint32_t>(max_list, 32) && 2 * t <= tmax) t *= 2;
-            hash_slots = t;
-            rcap = t;
-        }
-        if (kWarpsPerBlock * (rcap * 8 + fixed) > smem_cap) {
-            rcap = (smem_cap / kWarpsPerBlock - fixed) / 8;
-            while (hash_slots > rcap) hash_slots /= 2;
-        }
-        b.rcap = (uint32_t)rcap;
-        const size_t smem = use_settle  ? kWarpsPerBlock * settle_smem_per_warp(b.rcap)
-                            : use_batch ? kWarpsPerBlock * batch_smem_per_warp(b.rcap)
-                                        : kWarpsPerBlock * ((size_t)b.rcap * 8 + fixed);
+        // root hash table: a power of two at least twice the longest committed
+        // list, within the occupancy-preserving size (entries beyond half the
+        // table are searched in the global list)
+        uint32_t hash_slots = 64;
+        while (hash_slots < 2 * std::max<uint32_t>(max_list, 32) && 2 * hash_slots <= b.hash_max) hash_slots *= 2;
+        const size_t smem = kWarpsPerBlock * batch_smem_per_warp(hash_slots);
         while (true) {
             std::memset(&hc, 0, sizeof(hc));
             hc.next_root = r0;
@@ -3170,24 +1545,22 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             ta.sides = b.sides;
             for (int s = 0; s < 2; ++s) {
                 ta.g_off[s] = b.dg->off[s];
-                ta.g_arc[s] = b.dg->arc[s];
-                ta.g_head[s] = b.dg->head[s];
                 ta.g_farc[s] = b.farc[s];
                 ta.g_fhead[s] = b.fhead[s];
+                ta.win[s] = b.dg->win[s];
             }
             ta.order = b.order;
             ta.rank = b.rank;
             ta.l_off = b.off_a;
             ta.l_ent = b.ent_a;
             ta.l_dent = b.dent_a;
-            ta.dist_order = dist_order;
             ta.r0 = r0;
             ta.r_end = r_end;
-            // work-conserving extension (batch kernel): up to ext x the
-            // nominal size while nominal trees run; none on a rerun
+            // work-conserving extension: up to ext x the nominal size while
+            // nominal trees run; none on a rerun
             uint32_t ext = opts.superstep_extend == 0 ? (heavy_tail ? 1u : 4u)
                                                       : (uint32_t)std::max(1, opts.superstep_extend);
-            if (!use_batch || rerun) ext = 1;
+            if (rerun) ext = 1;
             ta.r_hard = (uint32_t)std::min<uint64_t>(n, (uint64_t)r0 + (uint64_t)ext * (r_end - r0));
             if (opts.root_limit) ta.r_hard = std::min<uint32_t>(ta.r_hard, std::max(opts.root_limit, r_end));
             ta.budget = rerun ? ~0ull : budget;
@@ -3199,38 +1572,13 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             ta.tree_labels = b.tlab;
             ta.ws_key = b.ws_key;
             ta.ws_vis = b.ws_vis;
-            ta.ws_pos = b.ws_pos;
-            ta.ws_heap = b.ws_heap;
-            ta.ctl = b.ctl;
-            ta.rcap = b.rcap;
-            const int blocks = (int)(b.slots / kWarpsPerBlock);
-            for (int s2 = 0; s2 < 2; ++s2) ta.win[s2] = b.dg->win[s2];
-            for (int s2 = 0; s2 < 2; ++s2) ta.wout[s2] = b.dg->wout[s2];
-            ta.out_crit = out_crit;
             ta.ws_front = b.ws_front;
-            ta.scan_back = scan_back;
-            ta.chunk_sched = prune_sched == 2 ? 1 : 0;
+            ta.ctl = b.ctl;
             ta.hash_slots = hash_slots;
-            ta.wide = prune_sched == 3 ? 1 : 0;
-            ta.lane_items = prune_sched == 4 ? 1 : 0;
-            if (ta.wide || ta.lane_items) ta.chunk_sched = 1;
             ta.hash_shift = 32;
             for (uint32_t t = hash_slots; t > 1; t >>= 1) --ta.hash_shift;
-            ta.smem_block = (uint32_t)smem;
-            ta.r_big = r0;
-            if (use_batch) {
-                // block-per-tree for the superstep's first roots, on request
-                // only (measured slower than warp-per-tree on the road-like and
-                // scale-free benchmarks)
-                uint32_t kb = 0;
-                if (opts.cta_roots > 0) kb = (uint32_t)opts.cta_roots;
-                ta.r_big = (uint32_t)std::min<uint64_t>((uint64_t)r0 + kb, r_end);
-            }
-            for (int s2 = 0; s2 < 2; ++s2) ta.win16[s2] = b.dg->win16[s2];
-            ta.ws_fq = b.ws_fq;
-            ta.fq_cap = b.fq_cap;
-            // near/far queue (batch kernel; the OUT criterion needs the whole
-            // queue every round).  Auto: split above 1024 queued vertices on
+            const int blocks = (int)(b.slots / kWarpsPerBlock);
+            // near/far queue.  Auto: split above 1024 queued vertices on
             // road-like graphs, whose queues are long rings of close keys
             // (1.25x faster builds of the 512/1024-square grids); off on
             // heavy-tailed ones, whose few-level queues gain nothing (RMAT
@@ -3238,22 +1586,13 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             ta.near_on = 0;
             ta.near_target = 1;
             const int qs = opts.queue_split ? opts.queue_split : (heavy_tail ? 1 : 1024);
-            if (use_batch && !out_crit && qs > 1) {
+            if (qs > 1) {
                 ta.near_on = (uint32_t)qs;
                 ta.near_target = std::max<uint32_t>(1, ta.near_on / 4);
             }
             void (*kern)(TreeArgs);
-            if (use_settle) {
-                if (unit) kern = plant_now ? settle_kernel<true, true> : settle_kernel<true, false>;
-                else kern = plant_now ? settle_kernel<false, true> : settle_kernel<false, false>;
-            } else if (use_batch) {
-                if (unit) kern = plant_now ? batch_kernel<true, true> : batch_kernel<true, false>;
-                else kern = plant_now ? batch_kernel<false, true> : batch_kernel<false, false>;
-            } else if (unit) {
-                kern = plant_now ? tree_kernel<true, true> : tree_kernel<true, false>;
-            } else {
-                kern = plant_now ? tree_kernel<false, true> : tree_kernel<false, false>;
-            }
+            if (unit) kern = plant_now ? batch_kernel<true, true> : batch_kernel<true, false>;
+            else kern = plant_now ? batch_kernel<false, true> : batch_kernel<false, false>;
             CHL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             CHL_CUDA(cudaEventRecord(ev_a, b.st));
             kern<<<blocks, kWarpsPerBlock * 32, smem, b.st>>>(ta);
@@ -3312,7 +1651,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         // array is sized for every new label before the chain (the clean
         // only removes labels).
         if ((rc = ensure_ent(&b.ent_b, &b.ent_cap_b, committed + M))) return rc;
-        if (dist_order && (rc = ensure_ent(&b.dent_b, &b.dent_cap_b, committed + M))) return rc;
+        if ((rc = ensure_ent(&b.dent_b, &b.dent_cap_b, committed + M))) return rc;
         const bool clean_now = !plant_now && M > 0;
         auto chain = [&]() -> int {
             int rc2;
@@ -3351,7 +1690,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             copy_old_lists<<<cgrid, 256, 0, b.st>>>(b.off_a, b.ent_a, b.off_b, b.ent_b, b.nl);
             place_new<<<cgrid, 256, 0, b.st>>>(sk, sv, d_count, b.new_cap, b.hub_bits, r0, b.pre, b.off_a,
                                                b.off_b, b.ent_b);
-            if (dist_order) {
+            {
                 // the same labels by (list, distance, hub), merged into the
                 // distance-ordered copy (the sort is stable: equal distances
                 // keep hub order)
@@ -3370,7 +1709,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             return CHL_OK;
         };
         kernels += 3 * ((b.key_bits + 7) / 8) + (clean_now ? 9 : 0) + 8 +
-                   (dist_order ? 2 + 3 * ((b.key_bits - b.hub_bits + 32 + 7) / 8) : 0);
+                   2 + 3 * ((b.key_bits - b.hub_bits + 32 + 7) / 8);
         CHL_CUDA(cudaEventRecord(ev_a, b.st));
         if (opts.use_graphs) {
             CHL_CUDA(cudaStreamBeginCapture(b.st, cudaStreamCaptureModeThreadLocal));
@@ -3406,10 +1745,8 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         std::swap(b.off_a, b.off_b);
         std::swap(b.ent_a, b.ent_b);
         std::swap(b.ent_cap_a, b.ent_cap_b);
-        if (dist_order) {
-            std::swap(b.dent_a, b.dent_b);
-            std::swap(b.dent_cap_a, b.dent_cap_b);
-        }
+        std::swap(b.dent_a, b.dent_b);
+        std::swap(b.dent_cap_a, b.dent_cap_b);
         CHL_CUDA(cudaMemcpyAsync(&hc, b.ctl, sizeof(hc), cudaMemcpyDeviceToHost, b.st));
         CHL_CUDA(cudaStreamSynchronize(b.st));
         M = hc.nlab;
@@ -3421,7 +1758,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         ++supersteps;
         r0 = r1;
         unsigned long long tstat[2] = {0, 0};
-        if ((use_batch || use_settle) && opts.verbose >= 2) {
+        if (opts.verbose >= 2) {
             CHL_CUDA(cudaMemsetAsync(&b.ctl->max_ratio_num, 0, 16, b.st));
             tree_stats<<<sms, 256, 0, b.st>>>(b.tsize, r1 - r_begin, &b.ctl->max_ratio_num);
             CHL_CUDA(cudaMemcpyAsync(tstat, &b.ctl->max_ratio_num, 16, cudaMemcpyDeviceToHost, b.st));
@@ -3447,11 +1784,11 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         if (opts.verbose >= 2)
             fprintf(stderr,
                     "superstep %u: roots [%u,%u) %s tree_ms %.2f labels %llu visits %llu reads %llu arcs %llu "
-                    "committed %llu max_list %u rcap %u\n",
+                    "committed %llu max_list %u\n",
                     supersteps, r_begin, r1, plant_now ? "plant" : "gll",
                     step_tree_ms, (unsigned long long)M, (unsigned long long)hc.visits,
                     (unsigned long long)hc.label_reads, (unsigned long long)hc.arcs, (unsigned long long)committed,
-                    max_list, b.rcap);
+                    max_list);
     }
     CHL_CUDA(cudaEventRecord(ev1, b.st));
     CHL_CUDA(cudaStreamSynchronize(b.st));

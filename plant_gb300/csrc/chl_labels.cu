@@ -262,6 +262,48 @@ __global__ void query_bytes(const uint64_t *off, int sym, const uint32_t *pairs,
     if ((threadIdx.x & 31) == 0) atomicAdd(bytes, acc);
 }
 
+// ---- label digest (no reference counterpart)
+// A position-dependent 64-bit fingerprint of the content hl::Labeling::write
+// emits (shared_memory/labeling.hpp:167-183): n, then for every list
+// i = 2v + side its size and its (hub, dist) entries in order.  One term per
+// item, added modulo 2^64 so the sum can be taken in any order:
+//   M(n + C_N) + sum_i M(B_i ^ size_i) + sum_ij M(B_i ^ M(j + C_E) ^ (hub << 32 | dist)),
+// B_i = M(i + C_L), M = the SplitMix64 finaliser (Steele, Lea and Flood,
+// OOPSLA 2014).  A symmetric build stores one list per vertex and stands for
+// both sides.
+constexpr uint64_t kDigN = 0x243F6A8885A308D3ull, kDigL = 0x13198A2E03707344ull,
+                   kDigE = 0xA4093822299F31D0ull;
+
+__host__ __device__ __forceinline__ uint64_t dig_mix(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// One warp per vertex (both sides), grid-stride; one atomic per warp.
+__global__ void label_digest(const uint64_t *__restrict__ off, const uint2 *__restrict__ ent, uint32_t n, int sym,
+                             unsigned long long *acc) {
+    const uint32_t lane = lane_id();
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    uint64_t sum = 0;
+    for (uint32_t v = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); v < n; v += warps) {
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const uint32_t x = sym ? v : 2 * v + (uint32_t)side;
+            const uint64_t b = off[x], e = off[x + 1];
+            const uint64_t base = dig_mix(2ull * v + (uint64_t)side + kDigL);
+            if (lane == 0) sum += dig_mix(base ^ (e - b));
+            for (uint64_t k = b + lane; k < e; k += 32) {
+                const uint2 q = ent[k];
+                sum += dig_mix(base ^ dig_mix((k - b) + kDigE) ^ (((uint64_t)q.x << 32) | q.y));
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
+    if (lane == 0) atomicAdd(acc, (unsigned long long)sum);
+}
+
 __global__ void hub_count(const uint2 *ent, uint64_t total, uint32_t *cnt) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
          i += (uint64_t)gridDim.x * blockDim.x)
@@ -385,6 +427,25 @@ extern "C" int chl_labels_hub_freq(const chl_labels *l, const uint32_t *order, u
     cudaFree(d_cnt);
     if (e != cudaSuccess) return cuda_status(e, "hub_freq", __FILE__, __LINE__);
     for (uint32_t h = 0; h < l->n; ++h) freq[order[h]] = cnt[h] * (l->sym ? 2u : 1u);
+    return CHL_OK;
+}
+
+extern "C" int chl_labels_digest(const chl_labels *l, uint64_t *digest) {
+    if (!l || !digest) return CHL_ERR_INVALID;
+    int rc = labels_ensure_device(l);
+    if (rc) return rc;
+    unsigned long long *d_acc = nullptr;
+    CHL_CUDA(cudaMalloc(&d_acc, sizeof(unsigned long long)));
+    unsigned long long acc = 0;
+    cudaError_t e = cudaMemset(d_acc, 0, sizeof(acc));
+    if (e == cudaSuccess && l->n) {
+        label_digest<<<device_sms() * 8, 256>>>(l->d_off, (const uint2 *)l->d_ent, l->n, l->sym ? 1 : 0, d_acc);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(&acc, d_acc, sizeof(acc), cudaMemcpyDeviceToHost);
+    cudaFree(d_acc);
+    if (e != cudaSuccess) return cuda_status(e, "label digest", __FILE__, __LINE__);
+    *digest = dig_mix((uint64_t)l->n + kDigN) + (uint64_t)acc;
     return CHL_OK;
 }
 

@@ -15,7 +15,7 @@
 //                line (modes 0-5 all answer on this GPU)
 //   -rq <file>   query pairs `u v` per line (default: 1,000,000 pairs from
 //                rand() % N, as distributed_memory/query.hpp:43-51)
-//   --gpu-mode hybrid|gll|plant, --gpu-algo batch|heap, --gpu-first <roots>,
+//   --gpu-mode hybrid|gll|plant, --gpu-first <roots>,
 //   --gpu-growth <factor>, --gpu-verbose
 #include <chl.h>
 
@@ -48,8 +48,6 @@ int main(int argc, char **argv) {
         else if (!strcmp(argv[i], "--gpu-mode") && has) {
             std::string m = argv[i + 1];
             opts.mode = m == "gll" ? CHL_MODE_GLL : m == "plant" ? CHL_MODE_PLANT : CHL_MODE_HYBRID;
-        } else if (!strcmp(argv[i], "--gpu-algo") && has) {
-            opts.tree_algo = std::string(argv[i + 1]) == "heap" ? 1 : 0;
         } else if (!strcmp(argv[i], "--gpu-first") && has) {
             opts.first_superstep = (uint32_t)atol(argv[i + 1]);
         } else if (!strcmp(argv[i], "--gpu-growth") && has) {

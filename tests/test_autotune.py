@@ -17,12 +17,11 @@ def test_search_and_cache(P, tmp_path, monkeypatch):
     from plant_gb300 import autotune as A
     calls = []
 
-    def fake_build(g, order, root_limit=0, first_superstep=0, growth=0.0, sf=0.0, cta_roots=0, queue_split=0,
-                   **kw):
-        calls.append((root_limit, first_superstep, growth, sf, cta_roots, queue_split))
-        # minimum at first=1024, growth=2.0, sf=128, cta=-1, queue_split=512
+    def fake_build(g, order, root_limit=0, first_superstep=0, growth=0.0, sf=0.0, queue_split=0, **kw):
+        calls.append((root_limit, first_superstep, growth, sf, queue_split))
+        # minimum at first=1024, growth=2.0, sf=128, queue_split=512
         ms = (100 + abs(first_superstep - 1024) / 10 + abs(growth - 2.0) * 7 + abs(sf - 128) / 50
-              + (5 if cta_roots > 0 else 0) + (0 if queue_split == 512 else 3))
+              + (0 if queue_split == 512 else 3))
         return FakeLabels(ms)
 
     monkeypatch.setattr(A, "build", fake_build)
@@ -30,10 +29,10 @@ def test_search_and_cache(P, tmp_path, monkeypatch):
     order = np.arange(g.get_n(), dtype=np.uint32)
     cache = str(tmp_path / "tune.json")
     cfg = A.tune(g, order, fraction=0.1, min_roots=10, cache=cache)
-    assert cfg == {"first_superstep": 1024, "growth": 2.0, "sf": 128.0, "cta_roots": -1, "queue_split": 512}
+    assert cfg == {"first_superstep": 1024, "growth": 2.0, "sf": 128.0, "queue_split": 512}
     assert all(c[0] == max(10, int(0.1 * g.get_n())) for c in calls)
     n_calls = len(calls)
-    assert n_calls <= len(A.FIRST) + len(A.GROWTH) + len(A.SF) + len(A.CTA) + len(A.QSPLIT)
+    assert n_calls <= len(A.FIRST) + len(A.GROWTH) + len(A.SF) + len(A.QSPLIT)
     data = json.load(open(cache))
     assert A.graph_key(g) in data and data[A.graph_key(g)]["config"] == cfg
     # cached: no further builds

@@ -15,7 +15,6 @@ from conftest import label_case
 pytestmark = pytest.mark.gpu
 
 MODES = {"hybrid": 0, "gll": 1, "plant": 2}
-ALGOS = {"batch": 0, "heap": 1, "settle": 3}
 CASES = ["grid12", "grid20hw", "rmat8", "directed60", "unit_path"]
 
 
@@ -30,13 +29,13 @@ def same_labels(L, ref, n):
 
 @pytest.mark.parametrize("case", CASES)
 @pytest.mark.parametrize("mode", list(MODES))
-@pytest.mark.parametrize("algo", list(ALGOS))
-def test_golden_label_files(P, case, mode, algo, tmp_path):
+@pytest.mark.parametrize("sched", ["default", "small"])
+def test_golden_label_files(P, case, mode, sched, tmp_path):
     c = label_case(case)
     g = P.Graph.read(c["gr"])
     order = P.Order.read(c["order"])
-    L = P.build(g, order, mode=MODES[mode], tree_algo=ALGOS[algo], first_superstep=7, growth=0.3,
-                cta_roots=3)
+    kw = {"first_superstep": 7, "growth": 0.3} if sched == "small" else {}
+    L = P.build(g, order, mode=MODES[mode], **kw)
     out = str(tmp_path / "gpu.labels")
     L.write(out)
     assert filecmp.cmp(out, c["labels"], shallow=False)
@@ -44,14 +43,13 @@ def test_golden_label_files(P, case, mode, algo, tmp_path):
 
 @pytest.mark.parametrize("mode", list(MODES))
 @pytest.mark.parametrize("sf", [32.0, 0.05])
-@pytest.mark.parametrize("algo", list(ALGOS))
-def test_config1_grid_matches_oracle(P, O, mode, sf, algo):
+def test_config1_grid_matches_oracle(P, O, mode, sf):
     g = P.Graph.grid(100, 100, seed=1)
     order = P.Order.degree(g, seed=1)
     off, head, ln = g.csr(True)
     og = O.OGraph.from_csr(g.get_n(), off, head, ln)
     ref, _ = O.gll(og, order)
-    L = P.build(g, order, mode=MODES[mode], sf=sf, tree_algo=ALGOS[algo])
+    L = P.build(g, order, mode=MODES[mode], sf=sf)
     assert same_labels(L, ref, g.get_n())
     st = L.stats()
     assert st["supersteps"] >= 1 and st["labels"] == ref.total()
@@ -76,22 +74,20 @@ def test_queue_split_matches_oracle(P, O, split, kind):
 
 
 @pytest.mark.parametrize("mode", list(MODES))
-@pytest.mark.parametrize("algo", list(ALGOS))
-def test_rmat_unit_lengths_matches_oracle(P, O, mode, algo):
+def test_rmat_unit_lengths_matches_oracle(P, O, mode):
     g = P.Graph.rmat(12, 16, seed=5)
     order = P.Order.degree(g, seed=2)
     off, head, ln = g.csr(True)
     og = O.OGraph.from_csr(g.get_n(), off, head, ln)
     ref, _ = O.gll(og, order)
-    L = P.build(g, order, mode=MODES[mode], sf=1.0, tree_algo=ALGOS[algo])
+    L = P.build(g, order, mode=MODES[mode], sf=1.0)
     assert same_labels(L, ref, g.get_n())
-    L = P.build(g, order, mode=MODES[mode], sf=1.0, tree_algo=ALGOS[algo], cta_roots=1 << 30)
+    L = P.build(g, order, mode=MODES[mode], sf=1.0, first_superstep=1, growth=0.05)
     assert same_labels(L, ref, g.get_n())
 
 
 @pytest.mark.parametrize("mode", list(MODES))
-@pytest.mark.parametrize("algo", list(ALGOS))
-def test_directed_weighted_matches_oracle(P, O, mode, algo, tmp_path):
+def test_directed_weighted_matches_oracle(P, O, mode, tmp_path):
     rng = np.random.default_rng(7)
     n, m = 700, 4000
     src = rng.integers(0, n, m).astype(np.uint32)
@@ -105,7 +101,7 @@ def test_directed_weighted_matches_oracle(P, O, mode, algo, tmp_path):
     og = O.OGraph.read_dimacs(p)
     order = og.degree_order(3)
     ref, _ = O.gll(og, order)
-    L = P.build(g, order, mode=MODES[mode], sf=0.5, tree_algo=ALGOS[algo])
+    L = P.build(g, order, mode=MODES[mode], sf=0.5)
     assert same_labels(L, ref, n)
 
 
@@ -176,35 +172,21 @@ def test_build_is_deterministic(P):
     g = P.Graph.grid(60, 60, highways=40, hw_steps=16, seed=9)
     order = P.Order.degree(g, seed=4)
     a = P.build(g, order, sf=0.2).export()
-    for kw in ({"max_warps": 64}, {"first_superstep": 1, "growth": 0.05},
-               {"first_superstep": 5000, "growth": 4.0}, {"tree_algo": 1, "max_warps": 8},
-               {"tree_algo": 3}, {"tree_algo": 3, "first_superstep": 3},
-               {"cta_roots": -1}, {"cta_roots": 1 << 30}, {"cta_roots": 7, "first_superstep": 50},
-               {"cta_roots": 1 << 30, "mode": 1}, {"scan_order": 1}, {"scan_order": 2},
-               {"use_graphs": 0}, {"use_graphs": 0, "mode": 1}, {"use_graphs": 1, "mode": 1, "tree_algo": 3},
-               {"root_stage": 32}, {"root_stage": 32, "mode": 1}, {"root_stage": 36, "cta_roots": 5},
-               {"root_stage": 4096}, {"prune_sched": 2}, {"prune_sched": 2, "root_stage": 32},
-               {"prune_sched": 2, "scan_order": 1}, {"prune_sched": 2, "mode": 1}, {"prune_sched": 1},
-               {"root_probe": 2}, {"root_probe": 2, "prune_sched": 2}, {"root_probe": 2, "root_stage": 64},
-               {"root_probe": 2, "mode": 1, "cta_roots": 3}, {"root_probe": 2, "root_stage": 64, "prune_sched": 2},
-               {"prune_sched": 3}, {"prune_sched": 3, "root_probe": 2, "scan_order": 1},
-               {"prune_sched": 3, "root_probe": 2, "root_stage": 64, "mode": 1},
+    for kw in ({"max_warps": 64}, {"max_warps": 8}, {"first_superstep": 1, "growth": 0.05},
+               {"first_superstep": 5000, "growth": 4.0}, {"first_superstep": 3},
+               {"use_graphs": 0}, {"use_graphs": 0, "mode": 1}, {"use_graphs": 1, "mode": 1},
                {"superstep_extend": 1}, {"superstep_extend": 16, "first_superstep": 9, "growth": 0.2},
                {"superstep_extend": 16, "mode": 1, "first_superstep": 9},
-               {"settle_rule": 2}, {"settle_rule": 2, "mode": 1}, {"settle_rule": 2, "prune_sched": 1},
-               {"prune_sched": 4}, {"prune_sched": 4, "mode": 1}, {"prune_sched": 4, "root_stage": 64},
-               {"prune_sched": 4, "scan_order": 2, "root_probe": 1},
-               {"prune_order": 1}, {"prune_order": 1, "mode": 1}, {"prune_order": 0, "mode": 1, "root_stage": 64},
                {"first_superstep": 1, "growth": 0.01, "superstep_extend": 1},
                # new-label buffers far below a superstep's labels: every
                # overflowed superstep re-runs its root range
-               {"label_cap": 1000}, {"label_cap": 1000, "mode": 1}, {"label_cap": 4000, "tree_algo": 1},
-               {"label_cap": 3000, "tree_algo": 3}, {"label_cap": 2000, "cta_roots": 1 << 30},
+               {"label_cap": 1000}, {"label_cap": 1000, "mode": 1}, {"label_cap": 4000, "max_warps": 8},
+               {"label_cap": 3000, "first_superstep": 3}, {"label_cap": 2000, "mode": 2},
                # near/far queue split at tiny queue sizes (refills, stale
                # far entries, threshold doubling and halving), and off
                {"queue_split": 1}, {"queue_split": 2}, {"queue_split": 8}, {"queue_split": 8, "mode": 1},
                {"queue_split": 33, "first_superstep": 1, "growth": 0.05}, {"queue_split": 200},
-               {"queue_split": 8, "settle_rule": 2}, {"queue_split": 8, "cta_roots": 5}):
+               {"queue_split": 8, "mode": 2}, {"queue_split": 8, "max_warps": 4}):
         b = P.build(g, order, sf=0.2, **kw).export()
         for x, y in zip(a, b):
             assert np.array_equal(x, y), kw
