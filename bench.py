@@ -23,11 +23,15 @@ label build (all roots, canonical labels) with the graph resident in HBM.
            without such a file, the closed form over the labelled vertices
            (a lower bound) stands in
   cpu_baseline: the CPU restatement of the reference GLL (OpenMP, all host
-           cores) on a bounded sample: the first R roots of the same build
+           cores), estimated for the whole build from replays of a sample of
+           its supersteps, each from its committed state (the complete labels
+           are the GPU's, identical to the CPU's)
 
 --impl reference times that CPU restatement (the reference itself does not
 build on this host: shared_memory/akiba.hpp includes <immintrin.h>, x86 only,
-and its sources are not present on the GPU host) on the same bounded sample.
+and its sources are not present on the GPU host) with no product code
+loaded: the oracle generates the same graph and order, builds the whole
+labeling once (set-up), and every step replays a sample of its supersteps.
 """
 from __future__ import annotations
 
@@ -195,24 +199,14 @@ def profile_trace(args):
     return t if t.get("workload") == workload_name(args) else None
 
 
-def make_workload(P, args, cpu_order=False):
-    """The graph (host-side seeded generator) and its order: on the GPU, or
-    with the CPU oracle's identical degree / betweenness order when the
-    reference arm must not touch the GPU engine."""
+def make_workload(P, args):
+    """The graph (host-side seeded generator) and its order, computed on the
+    GPU."""
     if args.workload == "rmat":
         g = P.Graph.rmat(args.scale, 16, 0.57, 0.19, 0.19, seed=1)
-    else:
-        g = P.Graph.grid(args.side, args.side, del_frac=0.05, diag_frac=0.01, wmin=1, wmax=1000,
-                         highways=args.highways, hw_steps=64, hw_factor=150.0, seed=1)
-    if cpu_order:
-        from oracle import oracle as O
-        off, head, ln = g.csr(True)
-        og = O.OGraph.from_csr(g.get_n(), off, head, ln)
-        if args.workload == "rmat":
-            return g, og.degree_order(1)
-        return g, og.betweenness_order(args.sources, 1)
-    if args.workload == "rmat":
         return g, P.Order.degree(g, seed=1)
+    g = P.Graph.grid(args.side, args.side, del_frac=0.05, diag_frac=0.01, wmin=1, wmax=1000,
+                     highways=args.highways, hw_steps=64, hw_factor=150.0, seed=1)
     return g, P.Order.betweenness(g, args.sources, seed=1)
 
 
@@ -242,20 +236,87 @@ def cpu_full(g, order, L):
     return secs, int(ref.total()), bool(same)
 
 
-def cpu_sample(g, order, seconds, threads=None):
-    """Oracle GLL restatement on the first R roots; R sized to ~`seconds`."""
-    from oracle import oracle as O
-    off, head, ln = g.csr(True)
-    og = O.OGraph.from_csr(g.get_n(), off, head, ln)
-    threads = threads or os.cpu_count() or 1
-    # grow R until one sample takes at least 2/3 of the target (the first
-    # roots cost the most, so time grows slower than R)
-    r = 32
-    labels, secs = O.gll_sample(og, order, r, threads)
-    while secs < seconds * 2 / 3 and r < len(order):
-        r = min(len(order), int(r * max(1.5, min(8.0, seconds / max(secs, 1e-3)))))
-        labels, secs = O.gll_sample(og, order, r, threads)
-    return og, r, threads, labels, secs
+def oracle_workload(O, args):
+    """The workload built by the CPU oracle alone: its restatements of the
+    package's seeded generators (og_gen_grid / og_gen_rmat, identical graphs)
+    and of the plain orders.  The reference arm uses this and loads no
+    product code."""
+    if args.workload == "rmat":
+        og = O.OGraph.rmat(args.scale, 16, 0.57, 0.19, 0.19, 1)
+        return og, og.degree_order(1)
+    og = O.OGraph.grid(args.side, args.side, 0.05, 0.01, 1, 1000, args.highways, 64, 150.0, 1)
+    return og, og.betweenness_order(args.sources, 1)
+
+
+def pps_sample(sizes, target, rng):
+    """Systematic sample of supersteps with inclusion probability
+    proportional to their size (capped at 1), sized so that the expected
+    cost sum(pi_i * size_i) is about `target`.  Returns [(index, pi)]; the
+    Horvitz-Thompson sum of t_i / pi_i over the sample is an unbiased
+    estimate of the whole build's sum of t_i."""
+    sizes = np.asarray(sizes, np.float64)
+    k = len(sizes)
+    pi = np.zeros(k)
+    capped = np.zeros(k, bool)
+    for _ in range(k + 1):
+        rest = ~capped & (sizes > 0)
+        budget = target - float(sizes[capped].sum())
+        denom = float((sizes[rest] ** 2).sum())
+        c = budget / denom if denom > 0 and budget > 0 else 0.0
+        pi[rest] = c * sizes[rest]
+        over = rest & (pi >= 1.0)
+        if not over.any():
+            break
+        capped |= over
+        pi[capped] = 1.0
+    # every superstep keeps a positive probability (unbiasedness)
+    pi = np.clip(np.where(sizes > 0, np.maximum(pi, 1e-4), 0.0), 0.0, 1.0)
+    u = rng.random()
+    cum = np.cumsum(pi)
+    prev = cum - pi
+    hits = np.ceil(cum - u) > np.ceil(prev - u)
+    return [(int(i), float(pi[i])) for i in np.nonzero(hits)[0]]
+
+
+def replay_rate(rp, labels_total, starts, ends, sizes, target, steps, warmup, seed=12345):
+    """CPU GLL build rate from superstep replays: every step replays a PPS
+    sample of whole supersteps (pps_sample) with each one's committed state
+    taken from the complete labels, and estimates the whole build's time by
+    Horvitz-Thompson.  Returns (rate, per-step estimates, replay seconds per
+    step, supersteps replayed per step)."""
+    rng = np.random.default_rng(seed)
+    ests, walls, counts = [], [], []
+    for it in range(warmup + steps):
+        plan = pps_sample(sizes, target, rng)
+        est = wall = 0.0
+        for i, pi in plan:
+            _, t = rp.run(int(starts[i]), int(starts[i]), int(ends[i]))
+            est += t / pi
+            wall += t
+        if it >= warmup:
+            ests.append(est)
+            walls.append(wall)
+            counts.append(len(plan))
+    return labels_total / float(np.mean(ests)), ests, walls, counts
+
+
+def supersteps_from_labels(hub_count_by_rank, N, sf=32.0):
+    """Superstep boundaries a CPU GLL build (run_paraPLL with label_limit =
+    sf * N, shared_memory/akiba.hpp:152-185) would have, estimated from the
+    final label counts per hub rank (the CPU counts its labels before the
+    clean, so its supersteps are somewhat shorter)."""
+    cum = np.cumsum(np.asarray(hub_count_by_rank, np.float64))
+    limit = sf * N
+    ends = []
+    start_labels = 0.0
+    r = 0
+    while r < N:
+        e = int(np.searchsorted(cum, start_labels + limit, side="left")) + 1
+        e = max(r + 1, min(N, e))
+        ends.append(e)
+        start_labels = cum[e - 1]
+        r = e
+    return np.asarray(ends, np.int64)
 
 
 def build_work_bytes(L, g):
@@ -337,31 +398,41 @@ def serve_test(P, L, n, qps, seconds, seed=11):
 
 
 def run_reference(args, ws, rank):
+    """The reference's CPU path (the oracle's byte-identical restatement of
+    run_paraPLL, all host cores) on the same workload, with no product code
+    loaded.  Set-up (untimed): the graph and order from the oracle's own
+    generators, one whole CPU build, which records its supersteps.  Each
+    step then replays a probability-proportional-to-size sample of whole
+    supersteps from their recorded committed state (oracle Replay) and
+    estimates the whole build's time; the value is the labels of the whole
+    build over the mean estimate."""
     if rank != 0:
         return
-    import plant_gb300 as P
     from oracle import oracle as O
-    P.lib()
-    g, order = make_workload(P, args, cpu_order=True)
-    # one step's sample sized so that the W + K steps take about two minutes
-    # (at most --cpu-seconds each)
-    target = max(2.0, min(args.cpu_seconds, 120.0 / max(1, args.steps + args.warmup)))
-    og, r, threads, labels, secs = cpu_sample(g, order, target)
-    vals = []
-    for _ in range(args.warmup):
-        O.gll_sample(og, order, r, threads)
-    for _ in range(args.steps):
-        lab, s = O.gll_sample(og, order, r, threads)
-        vals.append(lab / s)
-    v = float(np.mean(vals))
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean([labels / x for x in vals])),
+    threads = os.cpu_count() or 1
+    t0 = time.time()
+    og, order = oracle_workload(O, args)
+    t_gen = time.time() - t0
+    L, full_secs, ends, step_secs = O.gll_steps(og, order, threads)
+    labels = int(L.total())
+    starts = np.concatenate([[0], ends[:-1]])
+    rp = O.Replay(og, order, L, threads)
+    target = max(1.0, min(args.cpu_seconds, 75.0 / max(1, args.steps + args.warmup)))
+    rate, ests, walls, counts = replay_rate(rp, labels, starts, ends, step_secs, target, args.steps, args.warmup)
+    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(walls)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-            "data": "synthetic",
-            "config": {"workload": workload_name(args), "sample_roots": r},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"first {r} of {len(order)} roots (both sides), GLL restatement"},
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "data": "synthetic (the oracle's restatement of the seeded generators)",
+            "config": {"workload": workload_name(args) + ", full build", "vertices": int(og.n),
+                       "same_config": True},
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": (f"per step, a PPS sample of whole supersteps (mean {np.mean(counts):.1f} of "
+                                        f"{len(ends)}) of the GLL restatement (run_paraPLL, sf 32) replayed from "
+                                        "their committed state; Horvitz-Thompson estimate of the whole build")},
+            "full_build": {"seconds": full_secs, "labels": labels, "labels_per_s": labels / full_secs,
+                           "supersteps": int(len(ends)), "estimate_over_full": float(np.mean(ests)) / full_secs},
+            "setup_s": {"workload": round(t_gen, 1), "full_build": round(full_secs, 1)},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -470,15 +541,33 @@ def run_ours(args, ws, rank):
                   "hot_achieved_gbs": qh_bytes / (qh_ms / 1e3) / 1e9},
     }
     if rank == 0 and not args.no_cpu:
-        og, r, threads, lab, secs = cpu_sample(g, order, args.cpu_seconds)
-        line["cpu_baseline"] = {"value": lab / secs, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"GLL restatement on the first {r} of {n} roots (both sides)",
-                                "seconds": secs}
-        # CPU queries: the batchLocalQuery loop (OpenMP over pairs) on the same labels
+        # CPU GLL rate: replays of a PPS sample of CPU supersteps (boundaries
+        # estimated from the labels), each from its committed state, the
+        # complete labels being the GPU's (identical to the CPU's)
         from oracle import oracle as O
         o2, h2, d2 = L.export()
         ol = O.OLabels.from_csr(n, o2, h2, d2)
         del o2, h2, d2
+        off, head, ln = g.csr(True)
+        og = O.OGraph.from_csr(n, off, head, ln)
+        threads = os.cpu_count() or 1
+        per_rank = L.hub_freq(order)[order]
+        ends = supersteps_from_labels(per_rank, n)
+        starts = np.concatenate([[0], ends[:-1]])
+        sizes = np.add.reduceat(per_rank.astype(np.float64), starts)
+        rp = O.Replay(og, order, ol, threads)
+        # sizes are labels; scale the target from seconds with a first replay
+        _, t1 = rp.run(int(starts[0]), int(starts[0]), int(ends[0]))
+        per_label = t1 / max(sizes[0], 1.0)
+        rate, ests, walls, counts = replay_rate(rp, labels, starts, ends, sizes * per_label, args.cpu_seconds / 3,
+                                                3, 0)
+        del rp
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": (f"3 PPS samples of whole supersteps (mean {np.mean(counts):.1f} of "
+                                           f"{len(ends)}, boundaries estimated from the labels at 32 n per "
+                                           "superstep) of the GLL restatement, replayed from their committed "
+                                           "state; Horvitz-Thompson estimate of the whole build"),
+                                "seconds": float(np.sum(walls)) + t1}
         pairs = P.generate_query(1 << 20, n, seed=7)
         ol.query(pairs[:1024])
         t = time.time()

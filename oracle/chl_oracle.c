@@ -195,6 +195,265 @@ void og_free(og_graph *g) {
     free(g);
 }
 
+/* ------------------------------------------------- workload generators */
+/* Restatements of the package's own seeded generators (chl_gen_grid and
+ * chl_gen_rmat; the reference has none: its datasets are external files), so
+ * the CPU baseline can build the benchmark's graphs without loading the
+ * product library.  Same splitmix64 stream, same draws in the same order,
+ * same edge lists; the graph is then built as a DIMACS file listing every
+ * undirected edge in both directions would be (og_from_arcs = init_arcs). */
+
+typedef struct {
+    uint64_t s;
+} og_rng;
+static inline uint64_t og_rng_next(og_rng *r) {
+    r->s += 0x9E3779B97F4A7C15ull;
+    uint64_t z = r->s;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static inline uint64_t og_rng_below(og_rng *r, uint64_t range) { return og_rng_next(r) % range; }
+static inline double og_rng_unit(og_rng *r) { return (double)(og_rng_next(r) >> 11) * (1.0 / 9007199254740992.0); }
+static inline uint64_t og_mix_seed(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+/* open-addressing set of undirected edge keys (min << 32 | max) */
+typedef struct {
+    uint64_t *t;
+    uint64_t mask;
+} og_eset;
+static void eset_init(og_eset *e, uint64_t expect) {
+    uint64_t c = 1024;
+    while (c < 2 * expect + 16) c <<= 1;
+    e->t = malloc(c * sizeof(uint64_t));
+    memset(e->t, 0xFF, c * sizeof(uint64_t));
+    e->mask = c - 1;
+}
+/* 1 if inserted, 0 if present */
+static int eset_add(og_eset *e, uint64_t k) {
+    uint64_t h = og_mix_seed(k) & e->mask;
+    while (e->t[h] != ~0ull) {
+        if (e->t[h] == k) return 0;
+        h = (h + 1) & e->mask;
+    }
+    e->t[h] = k;
+    return 1;
+}
+static inline uint64_t ekey(uint32_t a, uint32_t b) {
+    if (a > b) {
+        uint32_t t = a;
+        a = b;
+        b = t;
+    }
+    return ((uint64_t)a << 32) | b;
+}
+
+static uint32_t uf_find(uint32_t *par, uint32_t x) {
+    while (par[x] != x) {
+        par[x] = par[par[x]];
+        x = par[x];
+    }
+    return x;
+}
+
+static og_graph *og_from_edges(uint32_t n, const uint64_t *uv, const int32_t *w, size_t k) {
+    uint32_t *src = malloc((k + 1) * sizeof(uint32_t)), *dst = malloc((k + 1) * sizeof(uint32_t));
+    for (size_t i = 0; i < k; ++i) {
+        src[i] = (uint32_t)(uv[i] >> 32);
+        dst[i] = (uint32_t)uv[i];
+    }
+    /* both directions of every edge, as a DIMACS file listing each twice */
+    og_tmp *a = malloc((4 * k + 1) * sizeof(og_tmp));
+    for (size_t i = 0; i < k; ++i) {
+        a[4 * i] = (og_tmp){src[i], dst[i], w[i], 1, 0};
+        a[4 * i + 1] = (og_tmp){dst[i], src[i], w[i], 0, 1};
+        a[4 * i + 2] = (og_tmp){dst[i], src[i], w[i], 1, 0};
+        a[4 * i + 3] = (og_tmp){src[i], dst[i], w[i], 0, 1};
+    }
+    og_graph *g = og_finalize(n, a, 4 * k);
+    free(a);
+    free(src);
+    free(dst);
+    return g;
+}
+
+/* chl_gen_grid: rows x cols 4-neighbour grid, del_frac of its edges deleted,
+ * largest component kept, floor(diag_frac * n) diagonal shortcuts, then
+ * `highways` edges of length round(hw_factor * Manhattan steps) between
+ * vertices at most hw_steps apart.  NULL on invalid arguments. */
+og_graph *og_gen_grid(uint32_t rows, uint32_t cols, double del_frac, double diag_frac, int32_t wmin,
+                      int32_t wmax, uint32_t highways, uint32_t hw_steps, double hw_factor, uint64_t seed) {
+    if (rows == 0 || cols == 0 || wmin < 1 || wmax < wmin || (uint64_t)rows * cols >= (1ull << 30) ||
+        del_frac < 0 || del_frac >= 1)
+        return NULL;
+    og_rng rng = {seed};
+    const uint64_t N0 = (uint64_t)rows * cols;
+    typedef struct {
+        uint32_t a, b;
+        int32_t w;
+    } E;
+    E *edges = malloc((2 * N0 + 1) * sizeof(E));
+    uint64_t E0 = 0;
+    for (uint32_t r = 0; r < rows; ++r)
+        for (uint32_t c = 0; c < cols; ++c) {
+            uint32_t id = r * cols + c;
+            if (c + 1 < cols) edges[E0++] = (E){id, id + 1, 0};
+            if (r + 1 < rows) edges[E0++] = (E){id, id + cols, 0};
+        }
+    for (uint64_t k = 0; k < E0; ++k) edges[k].w = wmin + (int32_t)og_rng_below(&rng, (uint64_t)(wmax - wmin) + 1);
+    uint64_t ndel = (uint64_t)llround(del_frac * (double)E0);
+    if (ndel > E0) ndel = E0;
+    for (uint64_t k = 0; k < ndel; ++k) {
+        uint64_t j = k + og_rng_below(&rng, E0 - k);
+        E t = edges[k];
+        edges[k] = edges[j];
+        edges[j] = t;
+    }
+    uint32_t *par = malloc(N0 * sizeof(uint32_t));
+    for (uint64_t i = 0; i < N0; ++i) par[i] = (uint32_t)i;
+    for (uint64_t k = ndel; k < E0; ++k) {
+        uint32_t a = uf_find(par, edges[k].a), b = uf_find(par, edges[k].b);
+        if (a != b) {
+            if (a > b) par[a] = b;
+            else par[b] = a;
+        }
+    }
+    uint32_t *sz = calloc(N0, sizeof(uint32_t));
+    for (uint64_t i = 0; i < N0; ++i) sz[uf_find(par, (uint32_t)i)]++;
+    uint32_t best = 0;
+    for (uint64_t i = 0; i < N0; ++i)
+        if (sz[i] > sz[best]) best = (uint32_t)i;
+    uint32_t *newid = malloc(N0 * sizeof(uint32_t)), *oldid = malloc(N0 * sizeof(uint32_t));
+    uint32_t n = 0;
+    for (uint64_t i = 0; i < N0; ++i) {
+        newid[i] = 0xFFFFFFFFu;
+        if (uf_find(par, (uint32_t)i) == best) {
+            newid[i] = n;
+            oldid[n++] = (uint32_t)i;
+        }
+    }
+    const uint64_t ndiag = (uint64_t)floor(diag_frac * (double)n);
+    const uint64_t cap = (E0 - ndel) + ndiag + highways + 1;
+    uint64_t *uv = malloc(cap * sizeof(uint64_t));
+    int32_t *w = malloc(cap * sizeof(int32_t));
+    size_t k = 0;
+    og_eset present;
+    eset_init(&present, cap);
+    for (uint64_t e = ndel; e < E0; ++e) {
+        if (newid[edges[e].a] == 0xFFFFFFFFu) continue;
+        uint64_t key = ekey(newid[edges[e].a], newid[edges[e].b]);
+        uv[k] = key;
+        w[k++] = edges[e].w;
+        eset_add(&present, key);
+    }
+    uint64_t added = 0, tries = 0;
+    while (added < ndiag && tries < 64 * (ndiag + 16)) {
+        ++tries;
+        uint32_t x = oldid[og_rng_below(&rng, n)];
+        uint32_t dir = (uint32_t)og_rng_below(&rng, 4);
+        int r = (int)(x / cols), c = (int)(x % cols);
+        int r2 = r + ((dir & 1) ? 1 : -1), c2 = c + ((dir & 2) ? 1 : -1);
+        int32_t len = wmin + (int32_t)og_rng_below(&rng, (uint64_t)(wmax - wmin) + 1);
+        if (r2 < 0 || c2 < 0 || r2 >= (int)rows || c2 >= (int)cols) continue;
+        uint32_t y = (uint32_t)r2 * cols + (uint32_t)c2;
+        if (newid[y] == 0xFFFFFFFFu) continue;
+        uint64_t key = ekey(newid[x], newid[y]);
+        if (!eset_add(&present, key)) continue;
+        uv[k] = key;
+        w[k++] = len;
+        ++added;
+    }
+    added = 0;
+    tries = 0;
+    const int S = (int)hw_steps;
+    while (S >= 2 && added < highways && tries < 64 * ((uint64_t)highways + 16)) {
+        ++tries;
+        uint32_t x = oldid[og_rng_below(&rng, n)];
+        int dr = (int)og_rng_below(&rng, 2 * (uint64_t)S + 1) - S;
+        int rem = S - abs(dr);
+        int dc = (int)og_rng_below(&rng, 2 * (uint64_t)rem + 1) - rem;
+        int steps = abs(dr) + abs(dc);
+        if (steps < 2) continue;
+        int r2 = (int)(x / cols) + dr, c2 = (int)(x % cols) + dc;
+        if (r2 < 0 || c2 < 0 || r2 >= (int)rows || c2 >= (int)cols) continue;
+        uint32_t y = (uint32_t)r2 * cols + (uint32_t)c2;
+        if (newid[y] == 0xFFFFFFFFu) continue;
+        uint64_t key = ekey(newid[x], newid[y]);
+        if (!eset_add(&present, key)) continue;
+        uv[k] = key;
+        w[k++] = (int32_t)llround(hw_factor * steps);
+        ++added;
+    }
+    og_graph *g = og_from_edges(n, uv, w, k);
+    free(present.t);
+    free(uv);
+    free(w);
+    free(newid);
+    free(oldid);
+    free(sz);
+    free(par);
+    free(edges);
+    return g;
+}
+
+static int cmp_u64(const void *pa, const void *pb) {
+    const uint64_t x = *(const uint64_t *)pa, y = *(const uint64_t *)pb;
+    return x < y ? -1 : (x > y);
+}
+
+/* chl_gen_rmat: 2^scale vertices, ef * 2^scale edge draws with quadrant
+ * probabilities (a, b, c, 1 - a - b - c), draw k from its own stream seeded
+ * by mix(seed ^ k * 0xD1B54A32D192ED03); self loops and duplicates dropped,
+ * unit lengths. */
+og_graph *og_gen_rmat(uint32_t scale, uint32_t ef, double a, double b, double c, uint64_t seed) {
+    if (scale == 0 || scale > 29 || ef == 0) return NULL;
+    const uint64_t n = 1ull << scale, M = (uint64_t)ef * n;
+    uint64_t *uv = malloc(M * sizeof(uint64_t));
+    const double ab = a + b, abc = a + b + c;
+#pragma omp parallel for schedule(static)
+    for (long long k = 0; k < (long long)M; ++k) {
+        og_rng r = {og_mix_seed(seed ^ ((uint64_t)k * 0xD1B54A32D192ED03ull))};
+        uint64_t u = 0, v = 0;
+        for (uint32_t l = 0; l < scale; ++l) {
+            double x = og_rng_unit(&r);
+            uint64_t bu, bv;
+            if (x < a) { bu = 0; bv = 0; }
+            else if (x < ab) { bu = 0; bv = 1; }
+            else if (x < abc) { bu = 1; bv = 0; }
+            else { bu = 1; bv = 1; }
+            u = (u << 1) | bu;
+            v = (v << 1) | bv;
+        }
+        if (u == v) {
+            uv[k] = ~0ull;
+        } else {
+            if (u > v) {
+                uint64_t t = u;
+                u = v;
+                v = t;
+            }
+            uv[k] = (u << 32) | v;
+        }
+    }
+    qsort(uv, M, sizeof(uint64_t), cmp_u64);
+    size_t k = 0;
+    for (uint64_t i = 0; i < M; ++i) {
+        if (uv[i] == ~0ull) break;
+        if (k == 0 || uv[k - 1] != uv[i]) uv[k++] = uv[i];
+    }
+    int32_t *w = malloc((k + 1) * sizeof(int32_t));
+    for (size_t i = 0; i < k; ++i) w[i] = 1;
+    og_graph *g = og_from_edges((uint32_t)n, uv, w, k);
+    free(w);
+    free(uv);
+    return g;
+}
+
 /* ------------------------------------------------------------- labels */
 
 typedef struct {
@@ -497,9 +756,12 @@ static inline void spin_unlock(volatile uint8_t *l) {
 }
 
 /* Akiba::iteration_gll (shared_memory/akiba.hpp:65-125). */
+/* glob_lim: only global entries with hub < glob_lim exist (UINT32_MAX in a
+ * build; a replay reads a complete labeling as the committed state of an
+ * earlier superstep). */
 static uint32_t iteration_gll(o_akiba *a, const og_graph *g, uint32_t i, int forward,
                               volatile uint8_t *lck, const uint32_t *order, const uint32_t *rev,
-                              ol_labels *glob, ol_labels *loc) {
+                              const ol_labels *glob, ol_labels *loc, uint32_t glob_lim) {
     ak_clear(a);
     uint32_t v = order[i];
     uint32_t lcknum = (forward ? 1 : 0) + v * 2;
@@ -515,8 +777,8 @@ static uint32_t iteration_gll(o_akiba *a, const og_graph *g, uint32_t i, int for
     }
     spin_unlock(&lck[lcknum]);
     {
-        ol_list *x = &glob->l[2 * (size_t)v + forward];
-        for (uint32_t k = 0; k < x->n; ++k) ak_update_tmp(a, x->h[k], x->d[k]);
+        const ol_list *x = &glob->l[2 * (size_t)v + forward];
+        for (uint32_t k = 0; k < x->n && x->h[k] < glob_lim; ++k) ak_update_tmp(a, x->h[k], x->d[k]);
     }
     const int s = forward ? 1 : 0;
     while (a->q.size) {
@@ -524,8 +786,8 @@ static uint32_t iteration_gll(o_akiba *a, const og_graph *g, uint32_t i, int for
         int32_t d = a->distance[u];
         if (rev[u] < i) continue;
         {
-            ol_list *x = &glob->l[2 * (size_t)u + !forward];
-            for (uint32_t k = 0; k < x->n; ++k) {
+            const ol_list *x = &glob->l[2 * (size_t)u + !forward];
+            for (uint32_t k = 0; k < x->n && x->h[k] < glob_lim; ++k) {
                 uint32_t hub = x->h[k];
                 if (hub > i) continue;
                 if (a->label_tmp[hub] != INFTY && a->label_tmp[hub] + x->d[k] <= d) goto pruned;
@@ -588,8 +850,22 @@ static int clean_cover(const ol_labels *L, uint32_t u, uint32_t v, int f, int32_
 /* run_paraPLL (shared_memory/akiba.hpp:132-217): supersteps of label_limit
  * labels, sort, clean, append to the global labeling.  Returns the labels;
  * *secs gets the reference's "total time" (labeling + sort + clean). */
+ol_labels *og_gll_steps(const og_graph *g, const uint32_t *order, uint32_t N, int threads,
+                        uint64_t label_limit, double *secs, uint32_t max_steps, uint32_t *nsteps,
+                        uint32_t *step_end, double *step_secs);
+
 ol_labels *og_gll(const og_graph *g, const uint32_t *order, uint32_t N, int threads,
                   uint64_t label_limit, double *secs) {
+    return og_gll_steps(g, order, N, threads, label_limit, secs, 0, NULL, NULL, NULL);
+}
+
+/* The same build, recording its supersteps: superstep k covers the roots
+ * [step_end[k-1], step_end[k]) (step_end[-1] = 0) and took step_secs[k]
+ * (labeling + sort + clean); at most max_steps are recorded, *nsteps gets
+ * the count (which may exceed max_steps). */
+ol_labels *og_gll_steps(const og_graph *g, const uint32_t *order, uint32_t N, int threads,
+                        uint64_t label_limit, double *secs, uint32_t max_steps, uint32_t *nsteps,
+                        uint32_t *step_end, double *step_secs) {
     ol_labels *glob = ol_new(N), *loc = ol_new(N);
     volatile uint8_t *lck = calloc(2 * (size_t)N + 2, 1);
     uint32_t *rev = malloc((size_t)N * sizeof(uint32_t));
@@ -598,6 +874,7 @@ ol_labels *og_gll(const og_graph *g, const uint32_t *order, uint32_t N, int thre
     for (int t = 0; t < threads; ++t) ak_init(&ak[t], g->n);
     double lt = 0, st = 0, ct = 0;
     uint32_t cnt = 0;
+    if (nsteps) *nsteps = 0;
     while (cnt < 2 * N) {
         uint64_t label_sum = 0;
         ol_clear(loc);
@@ -613,9 +890,9 @@ ol_labels *og_gll(const og_graph *g, const uint32_t *order, uint32_t N, int thre
                 }
                 uint32_t root = r / 2;
                 int side = (r % 2) == 1;
-                label_sum_thread += iteration_gll(&ak[th], g, root, side, lck, order, rev, glob, loc);
+                label_sum_thread += iteration_gll(&ak[th], g, root, side, lck, order, rev, glob, loc, UINT32_MAX);
                 side = (r % 2) == 0;
-                label_sum_thread += iteration_gll(&ak[th], g, root, side, lck, order, rev, glob, loc);
+                label_sum_thread += iteration_gll(&ak[th], g, root, side, lck, order, rev, glob, loc, UINT32_MAX);
                 if (label_sum_thread > N / 32) {
                     if (__sync_fetch_and_add(&label_sum, label_sum_thread) >= label_limit - label_sum_thread)
                         break;
@@ -662,7 +939,15 @@ ol_labels *og_gll(const og_graph *g, const uint32_t *order, uint32_t N, int thre
                 }
             }
         }
-        ct += omp_get_wtime() - se;
+        const double ce = omp_get_wtime();
+        ct += ce - se;
+        if (nsteps) {
+            if (*nsteps < max_steps) {
+                step_end[*nsteps] = cnt / 2 < N ? cnt / 2 : N;
+                step_secs[*nsteps] = ce - ls;
+            }
+            ++*nsteps;
+        }
     }
     if (secs) *secs = lt + st + ct;
     for (int t = 0; t < threads; ++t) ak_free(&ak[t]);
@@ -673,8 +958,6 @@ ol_labels *og_gll(const og_graph *g, const uint32_t *order, uint32_t N, int thre
     return glob;
 }
 
-/* Time the GLL restatement on the first `roots` roots only (a bounded sample
- * of a build for baselines); returns labels produced, *secs the time. */
 /* Sequential PLL trace: the work model of the build roofline.  Roots in
  * rank order, one at a time, both sides as iteration_gll does them
  * (shared_memory/akiba.hpp:65-125), every label committed at once, so each
@@ -748,79 +1031,122 @@ void og_pll_trace(const og_graph *g, const uint32_t *order, uint32_t N, uint64_t
     ol_free(L);
 }
 
-uint64_t og_gll_sample(const og_graph *g, const uint32_t *order, uint32_t N, int threads,
-                       uint32_t roots, double *secs) {
-    ol_labels *glob = ol_new(N), *loc = ol_new(N);
-    volatile uint8_t *lck = calloc(2 * (size_t)N + 2, 1);
-    uint32_t *rev = malloc((size_t)N * sizeof(uint32_t));
-    for (uint32_t i = 0; i < N; ++i) rev[order[i]] = i;
-    o_akiba *ak = malloc(sizeof(o_akiba) * threads);
-    for (int t = 0; t < threads; ++t) ak_init(&ak[t], g->n);
-    uint32_t cnt = 0, lim = 2 * (roots < N ? roots : N);
-    uint64_t total = 0;
-    double t0 = omp_get_wtime();
-    while (cnt < lim) {
-        uint64_t label_sum = 0;
-        uint64_t label_limit = 32ull * N;
-        ol_clear(loc);
-#pragma omp parallel for num_threads(threads) schedule(static, 1)
-        for (int th = 0; th < threads; ++th) {
-            uint64_t s = 0;
-            while (1) {
-                uint32_t r = __sync_fetch_and_add(&cnt, 2);
-                if (r >= lim) {
-                    __sync_fetch_and_add(&label_sum, s);
-                    break;
-                }
-                uint32_t root = r / 2;
-                s += iteration_gll(&ak[th], g, root, 0, lck, order, rev, glob, loc);
-                s += iteration_gll(&ak[th], g, root, 1, lck, order, rev, glob, loc);
-                if (s > N / 32) {
-                    if (__sync_fetch_and_add(&label_sum, s) >= label_limit - s) break;
-                    s = 0;
-                }
-            }
+/* ------------------------------------------------- superstep replay */
+/* Re-runs roots [r_begin, r_end) of one superstep of og_gll_steps with the
+ * state that superstep had: the committed labels are the complete labeling's
+ * entries with hub < s_begin (the superstep's first root: labels of
+ * committed hubs are final, and the complete labeling holds exactly them),
+ * the local labels start empty; then Labeling::sort and the clean pass
+ * (shared_memory/akiba.hpp:152-208) over the replayed roots' labels.  The
+ * CPU baseline times replays of sampled root ranges of every superstep to
+ * estimate a whole build's time without re-running it. */
+typedef struct {
+    const og_graph *g;
+    const uint32_t *order;
+    uint32_t N;
+    int threads;
+    const ol_labels *complete;
+    ol_labels *loc;
+    ol_labels *sink;   /* receives the kept labels, as the global labeling does */
+    volatile uint8_t *lck;
+    uint32_t *rev;
+    o_akiba *ak;
+} og_replay;
+
+og_replay *og_replay_new(const og_graph *g, const uint32_t *order, uint32_t N, int threads,
+                         const ol_labels *complete) {
+    og_replay *c = calloc(1, sizeof(og_replay));
+    c->g = g;
+    c->order = order;
+    c->N = N;
+    c->threads = threads;
+    c->complete = complete;
+    c->loc = ol_new(N);
+    c->sink = ol_new(N);
+    c->lck = calloc(2 * (size_t)N + 2, 1);
+    c->rev = malloc((size_t)N * sizeof(uint32_t));
+    for (uint32_t i = 0; i < N; ++i) c->rev[order[i]] = i;
+    c->ak = malloc(sizeof(o_akiba) * threads);
+    for (int t = 0; t < threads; ++t) ak_init(&c->ak[t], g->n);
+    return c;
+}
+
+void og_replay_free(og_replay *c) {
+    if (!c) return;
+    for (int t = 0; t < c->threads; ++t) ak_free(&c->ak[t]);
+    free(c->ak);
+    free(c->rev);
+    free((void *)c->lck);
+    ol_free(c->loc);
+    ol_free(c->sink);
+    free(c);
+}
+
+/* Labels kept by the clean pass; *secs = labeling + sort + clean time. */
+uint64_t og_replay_run(og_replay *c, uint32_t s_begin, uint32_t r_begin, uint32_t r_end, double *secs) {
+    const uint32_t N = c->N;
+    const int threads = c->threads;
+    ol_labels *loc = c->loc;
+    ol_clear(loc);
+    /* the kept labels are appended to lists that start empty (released
+     * outside the timed region) */
+    for (size_t x = 0; x < 2 * (size_t)N; ++x) {
+        ol_list *l = &c->sink->l[x];
+        if (l->cap) {
+            free(l->h);
+            free(l->d);
+            l->h = NULL;
+            l->d = NULL;
+            l->n = l->cap = 0;
         }
-#pragma omp parallel num_threads(threads)
-        {
-            o_pair *tmp = NULL;
-            uint32_t tcap = 0;
-#pragma omp for schedule(dynamic, 64)
-            for (long long x = 0; x < 2 * (long long)N; ++x) {
-                ol_list *l = &loc->l[x];
-                if (l->n < 2) continue;
-                if (l->n > tcap) {
-                    tcap = l->n;
-                    tmp = realloc(tmp, tcap * sizeof(o_pair));
-                }
-                for (uint32_t k = 0; k < l->n; ++k) tmp[k] = (o_pair){l->h[k], l->d[k]};
-                qsort(tmp, l->n, sizeof(o_pair), cmp_pair);
-                for (uint32_t k = 0; k < l->n; ++k) {
-                    l->h[k] = tmp[k].h;
-                    l->d[k] = tmp[k].d;
-                }
-            }
-            free(tmp);
-        }
-#pragma omp parallel for num_threads(threads) schedule(dynamic, 64) reduction(+ : total)
-        for (long long vi = 0; vi < (long long)N; ++vi)
-            for (int side = 0; side < 2; ++side) {
-                ol_list *l = &loc->l[2 * vi + side];
-                for (uint32_t k = 0; k < l->n; ++k)
-                    if (!clean_cover(loc, (uint32_t)vi, order[l->h[k]], side, l->d[k], l->h[k])) {
-                        ol_push(&glob->l[2 * vi + side], l->h[k], l->d[k]);
-                        total++;
-                    }
-            }
     }
+    uint32_t cnt = 2 * r_begin;
+    const uint32_t lim = 2 * (r_end < N ? r_end : N);
+    const double t0 = omp_get_wtime();
+#pragma omp parallel for num_threads(threads) schedule(static, 1)
+    for (int th = 0; th < threads; ++th) {
+        while (1) {
+            uint32_t r = __sync_fetch_and_add(&cnt, 2);
+            if (r >= lim) break;
+            uint32_t root = r / 2;
+            iteration_gll(&c->ak[th], c->g, root, 0, c->lck, c->order, c->rev, c->complete, loc, s_begin);
+            iteration_gll(&c->ak[th], c->g, root, 1, c->lck, c->order, c->rev, c->complete, loc, s_begin);
+        }
+    }
+#pragma omp parallel num_threads(threads)
+    {
+        o_pair *tmp = NULL;
+        uint32_t tcap = 0;
+#pragma omp for schedule(dynamic, 64)
+        for (long long x = 0; x < 2 * (long long)N; ++x) {
+            ol_list *l = &loc->l[x];
+            if (l->n < 2) continue;
+            if (l->n > tcap) {
+                tcap = l->n;
+                tmp = realloc(tmp, tcap * sizeof(o_pair));
+            }
+            for (uint32_t k = 0; k < l->n; ++k) tmp[k] = (o_pair){l->h[k], l->d[k]};
+            qsort(tmp, l->n, sizeof(o_pair), cmp_pair);
+            for (uint32_t k = 0; k < l->n; ++k) {
+                l->h[k] = tmp[k].h;
+                l->d[k] = tmp[k].d;
+            }
+        }
+        free(tmp);
+    }
+    uint64_t kept = 0;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 64) reduction(+ : kept)
+    for (long long vi = 0; vi < (long long)N; ++vi)
+        for (int side = 0; side < 2; ++side) {
+            const ol_list *l = &loc->l[2 * vi + side];
+            for (uint32_t k = 0; k < l->n; ++k)
+                if (!clean_cover(loc, (uint32_t)vi, c->order[l->h[k]], side, l->d[k], l->h[k])) {
+                    ol_push(&c->sink->l[2 * vi + side], l->h[k], l->d[k]);
+                    kept++;
+                }
+        }
     if (secs) *secs = omp_get_wtime() - t0;
-    for (int t = 0; t < threads; ++t) ak_free(&ak[t]);
-    free(ak);
-    free(rev);
-    free((void *)lck);
-    ol_free(loc);
-    ol_free(glob);
-    return total;
+    return kept;
 }
 
 /* ------------------------------------------------------------ PLaNT */

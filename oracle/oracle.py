@@ -43,7 +43,10 @@ _SIG = {
     "ol_query_batch": (None, [_P, _U32P, C.c_size_t, _I32P, C.c_int]),
     "og_dijkstra": (None, [_P, C.c_uint32, C.c_int, _I32P]),
     "og_gll": (_P, [_P, _U32P, C.c_uint32, C.c_int, C.c_uint64, _F64P]),
-    "og_gll_sample": (C.c_uint64, [_P, _U32P, C.c_uint32, C.c_int, C.c_uint32, _F64P]),
+    "og_gll_steps": (_P, [_P, _U32P, C.c_uint32, C.c_int, C.c_uint64, _F64P, C.c_uint32, _U32P, _U32P, _F64P]),
+    "og_replay_new": (_P, [_P, _U32P, C.c_uint32, C.c_int, _P]),
+    "og_replay_free": (None, [_P]),
+    "og_replay_run": (C.c_uint64, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _F64P]),
     "og_pll_trace": (None, [_P, _U32P, C.c_uint32, _U64P]),
     "og_plant_all": (_P, [_P, _U32P, C.c_uint32, _U32P, _U32P]),
     "og_canonical_check": (C.c_uint64, [_P, _U32P, _P]),
@@ -52,6 +55,9 @@ _SIG = {
     "og_betweenness": (None, [_P, _U32P, C.c_uint32, _F64P]),
     "og_betweenness_order": (None, [_P, C.c_uint32, C.c_uint64, _U32P]),
     "ol_digest": (C.c_uint64, [_P]),
+    "og_gen_grid": (_P, [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_int32, C.c_int32, C.c_uint32,
+                         C.c_uint32, C.c_double, C.c_uint64]),
+    "og_gen_rmat": (_P, [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_uint64]),
     "og_order_digest": (C.c_uint64, [_U32P, C.c_uint32]),
 }
 
@@ -108,6 +114,18 @@ class OGraph:
         w = np.ascontiguousarray(length, np.int32)
         return cls(lib().og_from_arcs(n, len(src), src.ctypes.data_as(_U32P), h.ctypes.data_as(_U32P),
                                       w.ctypes.data_as(_I32P)))
+
+    @classmethod
+    def grid(cls, rows, cols, del_frac=0.05, diag_frac=0.01, wmin=1, wmax=1000, highways=0, hw_steps=64,
+             hw_factor=150.0, seed=1):
+        """The package's seeded road-like grid (og_gen_grid), built on the CPU."""
+        return cls(lib().og_gen_grid(rows, cols, del_frac, diag_frac, wmin, wmax, highways, hw_steps, hw_factor,
+                                     seed))
+
+    @classmethod
+    def rmat(cls, scale, ef=16, a=0.57, b=0.19, c=0.19, seed=1):
+        """The package's seeded RMAT graph (og_gen_rmat), built on the CPU."""
+        return cls(lib().og_gen_rmat(scale, ef, a, b, c, seed))
 
     @property
     def n(self):
@@ -212,12 +230,45 @@ def gll(g: OGraph, order, threads=None, sf=32):
     return OLabels(h), secs.value
 
 
-def gll_sample(g: OGraph, order, roots, threads=None):
+def gll_steps(g: OGraph, order, threads=None, sf=32, max_steps=1 << 16):
+    """gll() that also returns its supersteps: (labels, secs, ends, step_secs);
+    superstep k covers roots [ends[k-1], ends[k])."""
     o = _u32(order)
     secs = C.c_double()
-    labels = lib().og_gll_sample(g.h, o.ctypes.data_as(_U32P), len(o), threads or os.cpu_count() or 1,
-                                 roots, C.byref(secs))
-    return labels, secs.value
+    n = len(o)
+    ends = np.zeros(max_steps, np.uint32)
+    ss = np.zeros(max_steps, np.float64)
+    ns = C.c_uint32()
+    h = lib().og_gll_steps(g.h, o.ctypes.data_as(_U32P), n, threads or os.cpu_count() or 1, int(sf * n),
+                           C.byref(secs), max_steps, C.byref(ns), ends.ctypes.data_as(_U32P),
+                           ss.ctypes.data_as(_F64P))
+    k = min(ns.value, max_steps)
+    return OLabels(h), secs.value, ends[:k].copy(), ss[:k].copy()
+
+
+class Replay:
+    """Re-runs root ranges of one superstep of a GLL build with that
+    superstep's committed state taken from the complete labels
+    (og_replay_run)."""
+
+    def __init__(self, g: OGraph, order, complete: OLabels, threads=None):
+        self._order = _u32(order)
+        self._g, self._complete = g, complete   # kept alive for the C side
+        self.threads = threads or os.cpu_count() or 1
+        self.h = C.c_void_p(lib().og_replay_new(g.h, self._order.ctypes.data_as(_U32P), len(self._order),
+                                                self.threads, complete.h))
+
+    def run(self, s_begin, r_begin, r_end):
+        """(labels kept, seconds) of roots [r_begin, r_end) of the superstep
+        that starts at root s_begin."""
+        secs = C.c_double()
+        kept = lib().og_replay_run(self.h, s_begin, r_begin, r_end, C.byref(secs))
+        return int(kept), secs.value
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.og_replay_free(self.h)
+            self.h = None
 
 
 def pll_trace(g: OGraph, order) -> dict:

@@ -1241,7 +1241,7 @@ struct Build {
     cudaStream_t st = nullptr;
     uint32_t warps = 0;   // warps the schedule is sized for
     uint32_t slots = 0;   // warp slots launched (workspace slots)
-    uint32_t hash_max = 2048;                // root hash slots that keep the block occupancy
+    uint32_t hash_max = 2048;                // largest root hash table (slots)
     uint4 *farc[2] = {nullptr, nullptr};     // (head, length, rank[head], 0) per arc
     uint2 *fhead[2] = {nullptr, nullptr};    // (head, rank[head]) per arc, unit lengths
     cudaGraphExec_t commit_exec = nullptr;   // captured commit chain
@@ -1447,15 +1447,15 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     CHL_CUDA(cudaMemsetAsync(b.ws_key, 0xFF, slots * n * 4, b.st));
     if ((rc = dalloc(&b.ws_front, slots * 3 * (size_t)n))) return rc;   // front, fnext, far pile
     {
-        // root hash slots that keep the register-limited block count per SM
-        int smem_sm = 0, reserved = 0;
-        CHL_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, 0));
-        CHL_CUDA(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, 0));
-        const size_t per_warp = ((size_t)smem_sm / nbo - (size_t)reserved) / kWarpsPerBlock;
-        const size_t fixed0 = batch_smem_per_warp(0) + 16;
-        const size_t cap = per_warp > fixed0 ? (per_warp - fixed0) / 8 : 64;
+        // root hash slots: at most 2048, and within CHL_SMEM_CAP_KB of shared
+        // memory per block (measured on the 1024-square grid: 2048 slots at 2
+        // resident blocks per SM beat 1024 slots at 3 by 1.3x -- entries past
+        // half the table are searched in global memory)
+        int max_smem = 0;
+        CHL_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0));
+        const size_t smem_cap = std::min<size_t>((size_t)max_smem, CHL_SMEM_CAP_KB * 1024);
         uint32_t t = 64;
-        while (2 * t <= std::min<size_t>(cap, 2048)) t *= 2;
+        while (2 * t <= 2048 && kWarpsPerBlock * batch_smem_per_warp(2 * t) <= smem_cap) t *= 2;
         b.hash_max = t;
     }
 
@@ -1770,6 +1770,13 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
                             "stage %.1f%% reset %.1f%% (sum of warp residencies %.3g cycles)\n",
                     100 * hc.cyc[0] / tot, 100 * hc.cyc[1] / tot, 100 * hc.cyc[2] / tot, 100 * hc.cyc[3] / tot,
                     100 * hc.cyc[4] / tot, 100 * hc.cyc[5] / tot, 100 * hc.cyc[6] / tot, tot);
+            if (kPhaseTiming) {
+                // warp slots busy: summed residencies over (slots x superstep time)
+                int khz = 0;
+                cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, 0);
+                const double avail = (double)b.slots * step_tree_ms * 1e-3 * khz * 1e3;
+                fprintf(stderr, "  warp slots busy %.1f%% (at the maximum SM clock)\n", 100 * tot / std::max(avail, 1.0));
+            }
             fprintf(stderr, "  prune item selection %.1f%% of warp cycles, %llu passes (%.2f per visit)\n",
                     100 * hc.cyc[8] / tot, hc.cyc[9],
                     (double)hc.cyc[9] / std::max<unsigned long long>(1, hc.visits));
