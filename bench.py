@@ -78,7 +78,9 @@ def parse():
                     help="graph ingestion: host parsers against the GPU path on DIMACS and SNAP files "
                          "of the grid workload")
     ap.add_argument("--serve", action="store_true",
-                    help="also run the open-loop serving test (Poisson arrivals) on the built labels")
+                    help="also run the open-loop serving test (Poisson arrivals) on the grid labels")
+    ap.add_argument("--no-rmat", action="store_true",
+                    help="skip the RMAT-20 leg (GLL vs hybrid builds, queries, serving) of the default run")
     ap.add_argument("--serve-qps", type=float, default=2e8, help="offered pair rate (pairs/s)")
     ap.add_argument("--serve-seconds", type=float, default=5.0)
     ap.add_argument("--rank", action="store_true",
@@ -217,6 +219,13 @@ def workload_slug(args):
     return f"grid{args.side}_hw{args.highways}_bc{args.sources}"
 
 
+def reference_key(args):
+    """Entry of tests/golden/scale_digests.json for this workload."""
+    if args.workload == "rmat":
+        return f"rmat{args.scale}"
+    return f"grid{args.side}_hw{args.highways}_bc{args.sources}"
+
+
 def workload_name(args):
     if args.workload == "rmat":
         return f"rmat{args.scale} ef16 (0.57,0.19,0.19,0.05), degree order"
@@ -333,6 +342,68 @@ def build_work_bytes(L, g):
     return tot
 
 
+def reference_digests():
+    """Digests of the reference's own labels on the benchmark workloads
+    (tests/golden/scale_digests.json, written by
+    tests/golden/make_scale_digests.py from run_paraPLL's output)."""
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "scale_digests.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def parity(L, key):
+    """The device digest of L against the reference's digest of the same
+    workload: equal digests mean byte-identical label files."""
+    ref = reference_digests().get(key)
+    got = f"{L.digest():016x}"
+    if ref is None:
+        return {"labels_digest": got, "labels_checksum_match": None, "reference": "no digest committed"}
+    return {"labels_digest": got, "reference_digest": ref["labels_digest"],
+            "labels_checksum_match": got == ref["labels_digest"] and L.stats()["labels"] == ref["labels_total"],
+            "reference": "run_paraPLL (shared_memory/akiba.hpp:132-217), -s 32, digest of its Labeling"}
+
+
+def rmat_leg(P, args, serve_seconds):
+    """RMAT scale 20 (ef 16, degree order): device-timed builds in hybrid
+    (PLaNT then pruned supersteps) and GLL mode, both checked against the
+    reference digest, then queries and the open-loop serving test on the
+    labels.  Part of the default run."""
+    g = P.Graph.rmat(20, 16, 0.57, 0.19, 0.19, seed=1)
+    order = P.Order.degree(g, seed=1)
+    n = g.get_n()
+    g.to_device()
+    out = {"workload": "rmat20 ef16 (0.57,0.19,0.19,0.05), degree order, full build", "vertices": n,
+           "arcs": int(g.out_arcs())}
+    for name, mode in (("hybrid", P.MODE_HYBRID), ("gll", P.MODE_GLL)):
+        P.build(g, order, mode=mode)
+        st = []
+        for _ in range(3):
+            L = P.build(g, order, mode=mode)
+            st.append(L.stats())
+        ms = float(np.mean([x["build_ms"] for x in st]))
+        out[name] = {"build_ms": ms, "tree_ms": float(np.mean([x["tree_ms"] for x in st])),
+                     "labels": st[-1]["labels"], "labels_per_s": st[-1]["labels"] / (ms / 1e3),
+                     "avg_label": st[-1]["avg_label"], "supersteps": st[-1]["supersteps"],
+                     "plant_roots": st[-1]["plant_roots"], "parity": parity(L, "rmat20")}
+        if name == "gll":
+            del L
+        else:
+            Lh = L
+    out["gll_over_hybrid_build"] = out["gll"]["build_ms"] / out["hybrid"]["build_ms"]
+    qk = 1 << 22
+    q_ms, q_bytes = P.query_bench(Lh, qk, iters=20, seed=7)
+    qh_ms, _ = P.query_bench(Lh, qk, iters=20, seed=7, hot=1000)
+    out["query"] = {"pairs": qk, "qps": qk / (q_ms / 1e3), "achieved_gbs": q_bytes / (q_ms / 1e3) / 1e9,
+                    "hot_qps": qk / (qh_ms / 1e3)}
+    if serve_seconds > 0:
+        out["serving"] = serve_test(P, Lh, n, args.serve_qps, serve_seconds)
+    del Lh
+    g.release_device()
+    return out
+
+
 def serve_test(P, L, n, qps, seconds, seed=11):
     """Open-loop Poisson request stream against the continuous-batching
     server: request sizes log-uniform in [1, 65536] pairs, 10% of the pairs
@@ -363,6 +434,8 @@ def serve_test(P, L, n, qps, seconds, seed=11):
     import queue as _q
     pend = _q.Queue()
 
+    kept = {}
+
     def waiter():
         while True:
             item = pend.get()
@@ -371,6 +444,8 @@ def serve_test(P, L, n, qps, seconds, seed=11):
             i, rid = item
             out, l = srv.wait(rid, len(reqs[i]))
             lat[i] = l
+            if i % 97 == 0:
+                kept[i] = out
 
     th = threading.Thread(target=waiter, daemon=True)
     th.start()
@@ -390,11 +465,14 @@ def serve_test(P, L, n, qps, seconds, seed=11):
     t1 = time.perf_counter()
     st = srv.stats()
     srv.close()
+    # answers of every 97th request against the batch query on the same labels
+    same = all(np.array_equal(v, P.query(L, reqs[i])) for i, v in kept.items())
     la = np.array(lat, np.float64)
     return {"offered_pairs_per_s": qps, "requests": len(reqs), "pairs": int(total),
             "achieved_pairs_per_s": total / (t1 - t0), "p50_ms": float(np.percentile(la, 50)),
             "p99_ms": float(np.percentile(la, 99)), "mean_request_pairs": mean_k,
-            "launches": st["launches"], "hot_fraction": 0.1}
+            "launches": st["launches"], "hot_fraction": 0.1, "answers_checked": len(kept),
+            "answers_equal_batch_query": bool(same)}
 
 
 def run_reference(args, ws, rank):
@@ -540,6 +618,9 @@ def run_ours(args, ws, rank):
                   "hot_qps": qk / (qh_ms / 1e3), "hot_set": 1000,
                   "hot_achieved_gbs": qh_bytes / (qh_ms / 1e3) / 1e9},
     }
+    line["parity"] = parity(L, reference_key(args))
+    if rank == 0 and args.workload == "grid" and not args.no_rmat:
+        line["rmat20"] = rmat_leg(P, args, args.serve_seconds)
     if rank == 0 and not args.no_cpu:
         # CPU GLL rate: replays of a PPS sample of CPU supersteps (boundaries
         # estimated from the labels), each from its committed state, the

@@ -192,7 +192,11 @@ typedef struct chl_build_opts {
                              tree's queue above 1024 vertices is split, about
                              256 kept near; heavy-tailed ones: off), 1 off,
                              q > 1: split above q (about q / 4 near)        */
-    uint32_t reserved[3];
+    uint32_t window_target; /* trees of a superstep with no committed labels
+                             (the first) are searched label-correcting in
+                             distance windows of about this many vertices:
+                             0 auto (1024), 1 off (batched settle rounds)   */
+    uint32_t reserved[2];
 } chl_build_opts;
 
 /* Fill opts with the defaults (hybrid, sf auto, ps 1024, autotune on,
@@ -339,16 +343,24 @@ int chl_server_create(const chl_labels *l, const chl_server_opts *opts,
                       chl_server **out);
 /* Submit k pairs (host memory, copied at admission).  Returns CHL_OK and a
  * request id, or CHL_ERR_OOM if the request can never fit. Blocks while the
- * server is full. */
+ * server is full: admitted pairs that are not yet answered hold 12 bytes of
+ * staging each, up to max_inflight_pairs, and unclaimed requests hold one of
+ * max_requests entries.  A request's pairs are released as soon as its
+ * answers are complete, whether or not they have been collected. */
 int chl_server_submit(chl_server *s, const uint32_t *pairs, size_t k,
                       uint64_t *req_id);
 /* Wait for request `req_id`; copies its k answers into out and releases
- * it.  timeout_ms < 0 waits forever; CHL_ERR_TIMEOUT if it expires. */
+ * its entry.  timeout_ms < 0 waits forever; CHL_ERR_TIMEOUT if it expires.
+ * CHL_ERR_INVALID if the server is freed while the caller waits. */
 int chl_server_wait(chl_server *s, uint64_t req_id, int32_t *out,
                     double timeout_ms, double *latency_ms);
 /* Totals since creation: launches, pairs answered, requests completed. */
 int chl_server_stats(chl_server *s, uint64_t *launches, uint64_t *pairs,
                      uint64_t *requests);
+/* Stops the server: callers blocked in chl_server_submit or chl_server_wait
+ * return CHL_ERR_INVALID, requests not yet launched are dropped, launches in
+ * flight are finished, then everything is released.  No call may start on
+ * the handle once chl_server_free has been called. */
 void chl_server_free(chl_server *s);
 
 /* ------------------------------------------------------- learned ranking */

@@ -886,6 +886,379 @@ batch_kernel(TreeArgs a) {
     }
 }
 
+// ------------------------------------------------------ window kernel
+//
+// Trees of a superstep with no committed labels (the first one) cannot be
+// pruned by labels, so a vertex need not be final before it is expanded:
+// such trees are searched label-correcting in distance windows [t, thr), as
+// delta-stepping does.  Every member of the window is relaxed; a member whose
+// key drops is relaxed again in the next pass, until a pass changes no key
+// below thr.  Then every key below thr is final -- it is the minimum over all
+// paths, and every other queued key is at least thr -- so the window's labels
+// are emitted from the final keys, and the next window, [thr, lo + delta),
+// is taken from the far pile (lo its smallest live key; delta adapts so that
+// a window holds about near_target vertices).  Keys carry PLaNT's via flag
+// (distance * 2 + not-via), and a flag change is a key decrease, so relaxing
+// again on every decrease keeps the flags exact; PLaNT's early exit
+// (distributed_memory/akiba.hpp:95) is tested at window boundaries, where the
+// count of queued not-via keys is exact.  GLL trees (iteration_gll) skip
+// expanding and labelling vertices ranked above the root.  A window takes a
+// few passes over hundreds of vertices where the IN criterion takes one
+// round per few dozen settled vertices.
+constexpr int kWinBatch = 256;   // members relaxed per batch
+
+__host__ __device__ constexpr size_t window_smem_per_warp() {
+    return ((size_t)8 * kWinBatch + (size_t)4 * (4 * kWinBatch + 1) + 8 + (size_t)12 * kEmit + 15) & ~(size_t)15;
+}
+
+template <bool UNIT, bool PLANT>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+window_kernel(TreeArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
+    const uint32_t slot = blockIdx.x * kWarpsPerBlock + wib;
+    unsigned char *base = smem + wib * window_smem_per_warp();
+    uint64_t *s_ba = (uint64_t *)base;                 // arc begin of batch vertex
+    uint32_t *s_bv = (uint32_t *)(s_ba + kWinBatch);   // batch vertex
+    uint32_t *s_bk = s_bv + kWinBatch;                 // batch key
+    uint32_t *s_bx = s_bk + kWinBatch;                 // arc prefix (kWinBatch + 1)
+    uint32_t *s_tl = s_bx + kWinBatch + 1;             // batch index of each vertex with arcs
+    uint64_t *s_ek = (uint64_t *)(((uintptr_t)(s_tl + kWinBatch) + 7) & ~(uintptr_t)7);   // staged label keys
+    uint32_t *s_ev = (uint32_t *)(s_ek + kEmit);       // staged label distances
+
+    uint32_t *key = a.ws_key + (size_t)slot * a.n;
+    uint32_t *vis = a.ws_vis + (size_t)slot * a.n;
+    uint32_t *memb = a.ws_front + (size_t)slot * 3 * a.n;   // window members
+    uint32_t *mkey = memb + a.n;                              // key a member was last relaxed with
+    uint32_t *pile = mkey + a.n;                              // far vertices (first touch beyond thr)
+    unsigned long long c_vis = 0, c_arcs = 0;
+
+    uint32_t n_emit = 0;
+    auto flush_labels = [&]() {
+        __syncwarp();
+        if (n_emit) {
+            unsigned long long b = 0;
+            if (lane == 0) b = atomicAdd(&a.ctl->nlab, (unsigned long long)n_emit);
+            b = __shfl_sync(kFull, b, 0);
+            for (uint32_t k = lane; k < n_emit; k += 32) {
+                const unsigned long long p = b + k;
+                if (p < a.out_cap) {
+                    a.out_key[p] = s_ek[k];
+                    a.out_val[p] = s_ev[k];
+                } else {
+                    a.ctl->overflow = 1;
+                }
+            }
+        }
+        n_emit = 0;
+        __syncwarp();
+    };
+
+    while (true) {
+        uint32_t r = kInf;
+        bool r_nominal = false;
+        if (lane == 0) r = fetch_root(a, r_nominal);
+        r = __shfl_sync(kFull, r, 0);
+        r_nominal = __shfl_sync(kFull, r_nominal ? 1u : 0u, 0) != 0;
+        if (r == kInf) break;
+        uint32_t t_size = 0, t_lab = 0;
+        const uint32_t v = a.order[r];
+        for (int sd = 0; sd < a.sides; ++sd) {
+            const int f = (a.sides == 1) ? 1 : sd;
+            const uint64_t *goff = a.g_off[f];
+            const uint4 *farc = a.g_farc[f];
+            const uint2 *fhead = a.g_fhead[f];
+            if (lane == 0) {
+                __stcg(&key[v], 1u);
+                vis[0] = v;
+                memb[0] = v;
+                mkey[0] = kInf;
+            }
+            __syncwarp();
+            uint32_t nvis = 1, nm = 1, npile = 0;
+            uint32_t thr = 1;            // the first window holds the root alone
+            uint32_t pmin = kInf;        // per lane: lower bound of the live far keys
+            uint32_t delta = 0;          // window width (0: choose at the first refill)
+            int ql = 1;                  // queued not-via keys (PLaNT)
+            bool changed = false;
+
+            // Relax the nb vertices of the batch (arcs flattened over the lanes).
+            auto relax = [&](uint32_t nb) {
+                uint32_t total = 0, ncomp = 0;
+                for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
+                    const uint32_t j = j0 + lane;
+                    uint32_t deg = 0;
+                    if (j < nb) {
+                        const uint32_t x = s_bv[j];
+                        const uint64_t ab = goff[x];
+                        deg = (uint32_t)(goff[x + 1] - ab);
+                        s_ba[j] = ab;
+                    }
+                    uint32_t incl = deg;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const uint32_t y = __shfl_up_sync(kFull, incl, o);
+                        if (lane >= (uint32_t)o) incl += y;
+                    }
+                    const uint32_t nem = __ballot_sync(kFull, deg > 0);
+                    if (deg > 0) {
+                        const uint32_t k = ncomp + __popc(nem & lanemask_lt());
+                        s_tl[k] = j;
+                        s_bx[k] = total + incl - deg;
+                    }
+                    total += __shfl_sync(kFull, incl, 31);
+                    ncomp += __popc(nem);
+                }
+                if (lane == 0) s_bx[ncomp] = total;
+                __syncwarp();
+                c_arcs += total;
+                uint32_t cur = 0;
+                auto owner = [&](uint32_t t0) -> uint32_t {
+                    if (cur + 1 < ncomp && s_bx[cur + 1] <= t0) ++cur;
+                    uint32_t bit = 0;
+                    const uint32_t kk = cur + 1 + lane;
+                    if (kk < ncomp) {
+                        const uint32_t st = s_bx[kk];
+                        if (st < t0 + 32) bit = 1u << (st - t0);
+                    }
+                    const uint32_t starts = __reduce_or_sync(kFull, bit);
+                    const uint32_t upto = lane == 31 ? kFull : ((2u << lane) - 1u);
+                    const uint32_t own = cur + (uint32_t)__popc(starts & upto);
+                    cur += (uint32_t)__popc(starts);
+                    return own;
+                };
+                constexpr int RC = CHL_RELAX_CHUNKS;
+                for (uint32_t t0 = 0; t0 < total; t0 += 32 * RC) {
+                    uint32_t w[RC], nk[RC], old[RC];
+                    bool upd[RC];
+#pragma unroll
+                    for (int c = 0; c < RC; ++c) {
+                        const uint32_t tc = t0 + 32u * c;
+                        const uint32_t own = tc < total ? owner(tc) : 0u;
+                        const uint32_t t = tc + lane;
+                        w[c] = 0;
+                        nk[c] = 0;
+                        old[c] = kInf;
+                        upd[c] = false;
+                        if (t < total) {
+                            const uint32_t lo = s_tl[own];
+                            const uint64_t e = s_ba[lo] + (t - s_bx[own]);
+                            uint32_t len, rk;
+                            if (UNIT) {
+                                const uint2 hr = fhead[e];
+                                w[c] = hr.x;
+                                rk = hr.y;
+                                len = 1;
+                            } else {
+                                const uint4 hl = farc[e];
+                                w[c] = hl.x;
+                                len = hl.y;
+                                rk = hl.z;
+                            }
+                            const uint32_t kx = s_bk[lo];
+                            const uint32_t nv = (!PLANT || ((kx & 1u) && rk >= r)) ? 1u : 0u;
+                            const uint64_t dd64 = (uint64_t)(kx >> 1) + len;
+                            if (dd64 < 0x7FFFFFFFull) {
+                                nk[c] = (uint32_t)dd64 * 2u + nv;
+                                old[c] = atomicMin(&key[w[c]], nk[c]);
+                                upd[c] = nk[c] < old[c];
+                            } else {
+                                a.ctl->err = 1;   // the reference asserts dd < infty
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int c = 0; c < RC; ++c) {
+                        const uint32_t dk = nk[c] >> 1;
+                        const bool fresh = upd[c] && old[c] == kInf;
+                        const bool in_win = upd[c] && dk < thr;
+                        if (in_win) changed = true;
+                        // a new member: first touched inside the window, or a
+                        // far vertex whose key drops into it (its far entry
+                        // goes stale)
+                        const bool join = in_win && (old[c] == kInf || (old[c] >> 1) >= thr);
+                        const uint32_t jm = __ballot_sync(kFull, join);
+                        if (join) {
+                            const uint32_t o = nm + __popc(jm & lanemask_lt());
+                            if (o < a.n) {
+                                memb[o] = w[c];
+                                mkey[o] = kInf;
+                            } else {
+                                a.ctl->err = 2;
+                            }
+                        }
+                        nm = min(nm + __popc(jm), a.n);
+                        const uint32_t vm = __ballot_sync(kFull, fresh);
+                        if (fresh) {
+                            const uint32_t o = nvis + __popc(vm & lanemask_lt());
+                            if (o < a.n) vis[o] = w[c];
+                            else a.ctl->err = 2;
+                        }
+                        nvis = min(nvis + __popc(vm), a.n);
+                        if (upd[c] && dk >= thr) pmin = min(pmin, dk);
+                        const bool to_far = fresh && dk >= thr;
+                        const uint32_t pm = __ballot_sync(kFull, to_far);
+                        if (to_far) {
+                            const uint32_t o = npile + __popc(pm & lanemask_lt());
+                            if (o < a.n) pile[o] = w[c];
+                            else a.ctl->err = 2;
+                        }
+                        npile = min(npile + __popc(pm), a.n);
+                        if (PLANT) {
+                            int dq = 0;
+                            if (upd[c]) dq = (int)(nk[c] & 1u) - (old[c] == kInf ? 0 : (int)(old[c] & 1u));
+                            ql += __reduce_add_sync(kFull, dq);
+                        }
+                    }
+                }
+                __syncwarp();
+            };
+
+            while (true) {
+                // passes over the window's members until no key below thr drops
+                do {
+                    changed = false;
+                    const uint32_t pass_n = nm;
+                    uint32_t nb = 0;
+                    for (uint32_t b0 = 0; b0 < pass_n; b0 += 32) {
+                        const uint32_t i = b0 + lane;
+                        bool need = false;
+                        uint32_t x = 0, k = 0;
+                        if (i < pass_n) {
+                            x = memb[i];
+                            k = __ldcg(&key[x]);
+                            if (k != mkey[i]) {
+                                mkey[i] = k;
+                                // GLL trees do not expand vertices ranked above the root
+                                need = PLANT || __ldg(&a.rank[x]) >= r;
+                            }
+                        }
+                        const uint32_t bm = __ballot_sync(kFull, need);
+                        if (need) {
+                            const uint32_t at = nb + __popc(bm & lanemask_lt());
+                            s_bv[at] = x;
+                            s_bk[at] = k;
+                        }
+                        nb += __popc(bm);
+                        __syncwarp();
+                        if (nb > (uint32_t)kWinBatch - 32) {
+                            relax(nb);
+                            nb = 0;
+                        }
+                    }
+                    if (nb) relax(nb);
+                } while (__any_sync(kFull, changed));
+                // the window is final: its labels, from the final keys
+                int nv_final = 0;
+                for (uint32_t b0 = 0; b0 < nm; b0 += 32) {
+                    const uint32_t i = b0 + lane;
+                    bool emit = false;
+                    uint32_t x = 0, k = 0;
+                    if (i < nm) {
+                        x = memb[i];
+                        k = __ldcg(&key[x]);
+                        if (PLANT) {
+                            nv_final += (int)(k & 1u);
+                            emit = (k & 1u) != 0;
+                        } else {
+                            emit = __ldg(&a.rank[x]) >= r;   // iteration_gll :92
+                        }
+                    }
+                    const uint32_t em = __ballot_sync(kFull, emit);
+                    if (em) {
+                        if (n_emit + 32 > (uint32_t)kEmit) flush_labels();
+                        if (emit) {
+                            const uint32_t at = n_emit + __popc(em & lanemask_lt());
+                            s_ek[at] = ((uint64_t)lidx(x, 1 - f, a.sides) << a.hub_bits) | (uint64_t)(r - a.r0);
+                            s_ev[at] = k >> 1;
+                        }
+                        n_emit += __popc(em);
+                        t_lab += __popc(em);
+                    }
+                }
+                t_size += nm;
+                if (PLANT) {
+                    ql -= __reduce_add_sync(kFull, nv_final);
+                    if (ql == 0) break;   // plant :95 early exit (all queued keys are via)
+                }
+                // next window from the far pile: entries below the old
+                // threshold are stale (they joined a window), entries below
+                // the new one join, the rest stay, compacted in place
+                nm = 0;
+                uint32_t lo = __reduce_min_sync(kFull, pmin);
+                if (delta == 0 && npile > 0) {
+                    uint32_t mn = kInf, mx = 0;
+                    for (uint32_t i = lane; i < npile; i += 32) {
+                        const uint32_t k = __ldcg(&key[pile[i]]) >> 1;
+                        mn = min(mn, k);
+                        mx = max(mx, k);
+                    }
+                    mn = __reduce_min_sync(kFull, mn);
+                    mx = __reduce_max_sync(kFull, mx);
+                    lo = mn;
+                    uint64_t d = (uint64_t)(mx - min(mn, mx)) * a.near_target / max(npile, 1u);
+                    if (d < 1) d = 1;
+                    if (d > 0x7FFFFFFFull) d = 0x7FFFFFFFull;
+                    delta = (uint32_t)d;
+                }
+                for (int pass = 0; pass < 4 && nm == 0 && npile > 0; ++pass) {
+                    const uint32_t t_old = thr;
+                    thr = sat_add(lo, delta);
+                    uint32_t keep = 0, moved = 0, kmin = kInf;
+                    for (uint32_t b0 = 0; b0 < npile; b0 += 32) {
+                        const uint32_t i = b0 + lane;
+                        const bool valid = i < npile;
+                        const uint32_t x = valid ? pile[i] : 0u;
+                        const uint32_t k = valid ? (__ldcg(&key[x]) >> 1) : kInf;
+                        const bool live = valid && k >= t_old;
+                        const bool nr = live && k < thr;
+                        const bool kp = live && !nr;
+                        const uint32_t nmk = __ballot_sync(kFull, nr);
+                        const uint32_t kmk = __ballot_sync(kFull, kp);
+                        // every lane has read its entry (ballots above), and a
+                        // kept entry moves only to a lower index
+                        if (nr) {
+                            const uint32_t o = moved + __popc(nmk & lanemask_lt());
+                            memb[o] = x;
+                            mkey[o] = kInf;
+                        }
+                        if (kp) {
+                            pile[keep + __popc(kmk & lanemask_lt())] = x;
+                            kmin = min(kmin, k);
+                        }
+                        moved += __popc(nmk);
+                        keep += __popc(kmk);
+                    }
+                    __syncwarp();
+                    npile = keep;
+                    nm = moved;
+                    lo = __reduce_min_sync(kFull, kmin);
+                    pmin = lane == 0 ? lo : kInf;
+                    if (moved < a.near_target / 4) delta = delta < 0x40000000u ? 2u * delta : 0x7FFFFFFFu;
+                    else if (moved > 4 * a.near_target) delta = max(delta / 2, 1u);
+                }
+                if (nm == 0) {
+                    if (npile > 0) a.ctl->err = 2;   // not reached: lo is exact from the second pass on
+                    break;
+                }
+            }
+            c_vis += t_size;
+            for (uint32_t k = lane; k < nvis; k += 32) __stcg(&key[vis[k]], kInf);
+            __syncwarp();
+        }
+        flush_labels();
+        if (lane == 0) {
+            a.tree_size[r - a.r0] = t_size;
+            a.tree_labels[r - a.r0] = t_lab;
+            finish_root(a, r_nominal);
+        }
+    }
+    if (lane == 0) {
+        atomicAdd(&a.ctl->visits, c_vis);
+        atomicAdd(&a.ctl->arcs, c_arcs);
+    }
+}
+
 __global__ void fat_arcs(uint64_t m, const uint2 *arc, const uint32_t *rank, uint4 *out) {
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
         const uint2 a = arc[e];
@@ -1240,7 +1613,8 @@ struct Build {
     size_t tmp_bytes = 0;
     cudaStream_t st = nullptr;
     uint32_t warps = 0;   // warps the schedule is sized for
-    uint32_t slots = 0;   // warp slots launched (workspace slots)
+    uint32_t slots = 0;   // warp slots launched by batch_kernel
+    uint32_t slots_win = 0;   // warp slots launched by window_kernel (workspace: the larger)
     uint32_t hash_max = 2048;                // largest root hash table (slots)
     uint4 *farc[2] = {nullptr, nullptr};     // (head, length, rank[head], 0) per arc
     uint2 *fhead[2] = {nullptr, nullptr};    // (head, rank[head]) per arc, unit lengths
@@ -1436,13 +1810,17 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     // when no root is left for the superstep, and every refusal of a root is
     // final for it.  The grid and the workspace cover those alone (b.warps
     // still sets the first superstep's size).
-    int nbo = 0;
+    int nbo = 0, nbw = 0;
     CHL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &nbo, unit ? batch_kernel<true, true> : batch_kernel<false, true>, kWarpsPerBlock * 32, 0));
+    CHL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &nbw, unit ? window_kernel<true, true> : window_kernel<false, true>, kWarpsPerBlock * 32,
+        kWarpsPerBlock * window_smem_per_warp()));
     nbo = std::max(nbo, 1);
-    const uint32_t resident = (uint32_t)nbo * (uint32_t)sms * kWarpsPerBlock;
-    b.slots = std::min(b.warps, resident);
-    const size_t slots = b.slots;
+    nbw = std::max(nbw, 1);
+    b.slots = std::min(b.warps, (uint32_t)nbo * (uint32_t)sms * kWarpsPerBlock);
+    b.slots_win = std::min(b.warps, (uint32_t)nbw * (uint32_t)sms * kWarpsPerBlock);
+    const size_t slots = std::max(b.slots, b.slots_win);
     if ((rc = dalloc(&b.ws_key, slots * n)) || (rc = dalloc(&b.ws_vis, slots * n))) return rc;
     CHL_CUDA(cudaMemsetAsync(b.ws_key, 0xFF, slots * n * 4, b.st));
     if ((rc = dalloc(&b.ws_front, slots * 3 * (size_t)n))) return rc;   // front, fnext, far pile
@@ -1501,7 +1879,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         // beyond that an overflow re-runs the superstep's root range.
         size_t fr = 0, tot = 0;
         CHL_CUDA(cudaMemGetInfo(&fr, &tot));
-        const uint64_t want = (uint64_t)budget_base + (uint64_t)b.slots * b.sides * n;
+        const uint64_t want = (uint64_t)budget_base + (uint64_t)std::max(b.slots, b.slots_win) * b.sides * n;
         const uint64_t fit = (uint64_t)(fr / 4 / 36);
         if ((rc = grow_new(b, std::min(want, fit)))) return rc;
     }
@@ -1514,11 +1892,15 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     double tree_ms = 0, sort_ms = 0, commit_ms = 0;
     uint32_t max_list = 0;   // longest committed list
     float step_tree_ms = 0;
+    uint32_t step_slots = 0;   // warp slots of the last tree launch
     // Superstep schedule: superstep k covers roots [r0, r0 + size) with
     // size = clamp(growth * r0, first, n) -- small while the top hubs are not
     // yet committed (their labels prune everything later), geometric after.
     // The label budget sf * n (the reference's label_limit) also ends a
     // superstep early.
+    // label-correcting windows of the first superstep's trees: about this
+    // many vertices per window (1: IN-criterion rounds instead)
+    const uint32_t win_target = opts.window_target ? opts.window_target : 1024u;
     const uint32_t first = opts.first_superstep ? opts.first_superstep : auto_first;
     const double growth = opts.growth > 0 ? opts.growth : auto_growth;
     while (r0 < n && (opts.root_limit == 0 || r0 < opts.root_limit)) {
@@ -1591,11 +1973,25 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
                 ta.near_target = std::max<uint32_t>(1, ta.near_on / 4);
             }
             void (*kern)(TreeArgs);
-            if (unit) kern = plant_now ? batch_kernel<true, true> : batch_kernel<true, false>;
-            else kern = plant_now ? batch_kernel<false, true> : batch_kernel<false, false>;
-            CHL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            size_t smem_launch = smem;
+            int grid = blocks;
+            if (committed == 0 && win_target > 1) {
+                // no committed labels: no tree can be pruned, so the trees
+                // are searched label-correcting in windows (window_kernel)
+                ta.near_target = win_target;
+                grid = (int)(b.slots_win / kWarpsPerBlock);
+                smem_launch = kWarpsPerBlock * window_smem_per_warp();
+                if (unit) kern = plant_now ? window_kernel<true, true> : window_kernel<true, false>;
+                else kern = plant_now ? window_kernel<false, true> : window_kernel<false, false>;
+            } else if (unit) {
+                kern = plant_now ? batch_kernel<true, true> : batch_kernel<true, false>;
+            } else {
+                kern = plant_now ? batch_kernel<false, true> : batch_kernel<false, false>;
+            }
+            CHL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_launch));
             CHL_CUDA(cudaEventRecord(ev_a, b.st));
-            kern<<<blocks, kWarpsPerBlock * 32, smem, b.st>>>(ta);
+            kern<<<grid, kWarpsPerBlock * 32, smem_launch, b.st>>>(ta);
+            step_slots = (uint32_t)grid * kWarpsPerBlock;
             CHL_CUDA(cudaGetLastError());
             CHL_CUDA(cudaEventRecord(ev_b, b.st));
             ++launches;
@@ -1774,7 +2170,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
                 // warp slots busy: summed residencies over (slots x superstep time)
                 int khz = 0;
                 cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, 0);
-                const double avail = (double)b.slots * step_tree_ms * 1e-3 * khz * 1e3;
+                const double avail = (double)step_slots * step_tree_ms * 1e-3 * khz * 1e3;
                 fprintf(stderr, "  warp slots busy %.1f%% (at the maximum SM clock)\n", 100 * tot / std::max(avail, 1.0));
             }
             fprintf(stderr, "  prune item selection %.1f%% of warp cycles, %llu passes (%.2f per visit)\n",

@@ -4,9 +4,13 @@
 // (query mode 1, distributed_memory/query.hpp:82-91, over batchLocalQuery,
 // distributed_memory/query_funcs.hpp:23-30).  Here requests of any size
 // arrive at any time:
-//   * admission: a request is admitted once its pairs fit in the in-flight
-//     budget (max_inflight_pairs device slots) and a request entry is free;
-//     a request larger than the budget is rejected with CHL_ERR_OOM;
+//   * admission by memory: every admitted pair holds 12 bytes of staging
+//     (8 for the pair, 4 for its answer) until it is answered; a request is
+//     admitted once its pairs fit in the budget (max_inflight_pairs) and a
+//     request entry is free, and a request larger than the budget is
+//     rejected with CHL_ERR_OOM.  The budget is released when the request's
+//     answers are complete, whether or not its client has collected them;
+//     an answered request keeps only its entry until chl_server_wait;
 //   * batching: the server thread packs the pending pairs of many requests
 //     (splitting large ones) into one launch of up to max_batch_pairs;
 //   * overlap: kPipes batches are in flight at once, each on its own stream
@@ -73,9 +77,11 @@ struct chl_server {
     std::condition_variable cv_work, cv_done, cv_space;
     std::deque<Request *> pending;
     std::unordered_map<uint64_t, Request *> table;
-    size_t inflight_pairs = 0;
+    size_t inflight_pairs = 0;      // admitted pairs not yet answered
     uint64_t next_id = 1;
     bool stop = false;
+    int blocked = 0;                // callers inside submit / wait
+    std::condition_variable cv_quit;
     Pipe pipes[kPipes];
     uint64_t launch_seq = 0;
     std::thread worker;
@@ -94,11 +100,13 @@ void finish_pipe(chl_server *s, Pipe &p) {
         if (pc.r->done == pc.r->k) {
             pc.r->complete = true;
             pc.r->t1 = Clock::now();
+            s->inflight_pairs -= pc.r->k;   // its staging is free again
         }
     }
     p.pieces.clear();
     p.busy = false;
     s->cv_done.notify_all();
+    s->cv_space.notify_all();
 }
 
 void server_loop(chl_server *s) {
@@ -110,7 +118,12 @@ void server_loop(chl_server *s) {
         std::unique_lock<std::mutex> lk(s->mu);
         bool any_busy = false;
         for (Pipe &p : s->pipes) any_busy |= p.busy;
-        if (s->stop && s->pending.empty() && !any_busy) break;
+        if (s->stop) {
+            // requests not yet on the device are dropped (their callers were
+            // told so by chl_server_free); batches in flight are retired
+            s->pending.clear();
+            if (!any_busy) break;
+        }
         if (s->pending.empty()) {
             if (any_busy) {
                 lk.unlock();
@@ -225,13 +238,19 @@ extern "C" int chl_server_submit(chl_server *s, const uint32_t *pairs, size_t k,
     r->pairs.assign(pairs, pairs + 2 * k);
     r->out.assign(k, 0);
     std::unique_lock<std::mutex> lk(s->mu);
+    if (s->stop) {
+        delete r;
+        return CHL_ERR_INVALID;
+    }
+    ++s->blocked;
     s->cv_space.wait(lk, [&] {
         return s->stop || (s->inflight_pairs + k <= s->opts.max_inflight_pairs &&
                            s->table.size() < s->opts.max_requests);
     });
+    if (--s->blocked == 0 && s->stop) s->cv_quit.notify_all();
     if (s->stop) {
         delete r;
-        return CHL_ERR_INVALID;
+        return CHL_ERR_INVALID;   // the server is being freed
     }
     r->id = s->next_id++;
     r->t0 = Clock::now();
@@ -253,19 +272,24 @@ extern "C" int chl_server_wait(chl_server *s, uint64_t req_id, int32_t *out, dou
                                double *latency_ms) {
     if (!s) return CHL_ERR_INVALID;
     std::unique_lock<std::mutex> lk(s->mu);
+    if (s->stop) return CHL_ERR_INVALID;
     auto it = s->table.find(req_id);
     if (it == s->table.end()) return CHL_ERR_INVALID;
     Request *r = it->second;
-    auto ready = [&] { return r->complete || s->error != CHL_OK; };
+    auto ready = [&] { return s->stop || r->complete || s->error != CHL_OK; };
+    ++s->blocked;
+    bool timed_out = false;
     if (timeout_ms < 0) {
         s->cv_done.wait(lk, ready);
-    } else if (!s->cv_done.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms), ready)) {
-        return CHL_ERR_TIMEOUT;
+    } else {
+        timed_out = !s->cv_done.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms), ready);
     }
+    if (--s->blocked == 0 && s->stop) s->cv_quit.notify_all();
+    if (s->stop) return CHL_ERR_INVALID;   // the server is being freed: r may be gone
+    if (timed_out) return CHL_ERR_TIMEOUT;
     if (!r->complete) return s->error;
     if (out && r->k) std::memcpy(out, r->out.data(), r->k * 4);
     if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t1 - r->t0).count();
-    s->inflight_pairs -= r->k;
     s->table.erase(it);
     delete r;
     s->cv_space.notify_all();
@@ -284,11 +308,15 @@ extern "C" int chl_server_stats(chl_server *s, uint64_t *launches, uint64_t *pai
 extern "C" void chl_server_free(chl_server *s) {
     if (!s) return;
     {
-        std::lock_guard<std::mutex> g(s->mu);
+        // fail every caller blocked in submit or wait, and wait until they
+        // have left (after that, nothing of this server is touched by them)
+        std::unique_lock<std::mutex> lk(s->mu);
         s->stop = true;
+        s->cv_work.notify_all();
+        s->cv_space.notify_all();
+        s->cv_done.notify_all();
+        s->cv_quit.wait(lk, [&] { return s->blocked == 0; });
     }
-    s->cv_work.notify_all();
-    s->cv_space.notify_all();
     if (s->worker.joinable()) s->worker.join();
     for (Pipe &p : s->pipes) {
         if (p.st) cudaStreamSynchronize(p.st);

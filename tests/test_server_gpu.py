@@ -1,5 +1,6 @@
 """Continuous-batching server: each answer is the same alone and in the mix."""
 import threading
+import time
 
 import numpy as np
 import pytest
@@ -67,3 +68,70 @@ def test_wait_timeout_and_unknown_id(P, labels):
         srv.wait(12345, 1)
     assert e.value.status == P.CHL_ERR_INVALID
     srv.close()
+
+
+def test_unclaimed_requests_do_not_starve_admission(P, labels):
+    """A request's pairs leave the admission budget once answered, even if
+    its client never waits for it, so later submits are admitted."""
+    L, n = labels
+    srv = P.Server(L, max_inflight_pairs=1000, max_requests=64, max_batch_pairs=256)
+    ids = []
+    for i in range(5):
+        got = []
+        t = threading.Thread(target=lambda: got.append(srv.submit(P.generate_query(800, n, seed=i))))
+        t.start()
+        t.join(timeout=60)
+        assert got, "submit starved by requests nobody waited for"
+        ids.append(got[0])
+    # the answers are kept for a late wait
+    for i, rid in enumerate(ids):
+        out, _ = srv.wait(rid, 800)
+        assert np.array_equal(out, P.query(L, P.generate_query(800, n, seed=i)))
+    srv.close()
+
+
+def test_free_fails_a_blocked_submit(P, labels):
+    L, n = labels
+    srv = P.Server(L, max_inflight_pairs=1 << 16, max_requests=1, max_batch_pairs=256)
+    srv.submit(P.generate_query(10, n, seed=1))   # holds the only request entry
+    res = []
+
+    def blocked():
+        try:
+            srv.submit(P.generate_query(10, n, seed=2))
+            res.append("admitted")
+        except P.CHLError as e:
+            res.append(e.status)
+
+    t = threading.Thread(target=blocked)
+    t.start()
+    time.sleep(0.5)
+    assert not res, "the second submit should wait for a free entry"
+    srv.close()
+    t.join(timeout=60)
+    assert res == [P.CHL_ERR_INVALID]
+
+
+def test_free_with_a_waiter(P, labels):
+    """A waiter either gets its (correct) answers or CHL_ERR_INVALID when the
+    server is freed under it; it never hangs."""
+    L, n = labels
+    for trial in range(4):
+        srv = P.Server(L, max_inflight_pairs=1 << 21, max_batch_pairs=1 << 14)
+        q = P.generate_query(1 << 20, n, seed=trial)
+        rid = srv.submit(q)
+        res = []
+
+        def waiter():
+            try:
+                out, _ = srv.wait(rid, len(q))
+                res.append(bool(np.array_equal(out, P.query(L, q))))
+            except P.CHLError as e:
+                res.append(e.status)
+
+        t = threading.Thread(target=waiter)
+        t.start()
+        srv.close()
+        t.join(timeout=60)
+        assert not t.is_alive()
+        assert res[0] in (True, P.CHL_ERR_INVALID)
