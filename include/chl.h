@@ -196,7 +196,9 @@ typedef struct chl_build_opts {
                              (the first) are searched label-correcting in
                              distance windows of about this many vertices:
                              0 auto (1024), 1 off (batched settle rounds)   */
-    uint32_t reserved[2];
+    uint32_t window_warps; /* warps building one such tree: 0 auto (4), 1, 2,
+                             4 or 8                                         */
+    uint32_t reserved[1];
 } chl_build_opts;
 
 /* Fill opts with the defaults (hybrid, sf auto, ps 1024, autotune on,

@@ -51,7 +51,7 @@ class BuildOpts(C.Structure):
                 ("first_superstep", C.c_uint32), ("growth", C.c_double),
                 ("max_warps", C.c_uint32), ("root_limit", C.c_uint32),
                 ("superstep_extend", C.c_int32), ("label_cap", C.c_uint32), ("queue_split", C.c_int32),
-                ("window_target", C.c_uint32), ("reserved", C.c_uint32 * 2)]
+                ("window_target", C.c_uint32), ("window_warps", C.c_uint32), ("reserved", C.c_uint32 * 1)]
 
 
 class BuildStats(C.Structure):
@@ -440,7 +440,7 @@ def build(g: Graph, order, mode: int = MODE_HYBRID, sf: float = 0.0, ps: float =
           first_superstep: int = 0, growth: float = 0.0,
           use_graphs: Optional[int] = None, root_limit: int = 0,
           superstep_extend: int = 0, label_cap: int = 0, queue_split: int = 0,
-          window_target: int = 0) -> Labeling:
+          window_target: int = 0, window_warps: int = 0) -> Labeling:
     o = _u32(order)
     opts = BuildOpts()
     lib().chl_build_opts_default(C.byref(opts))
@@ -458,6 +458,7 @@ def build(g: Graph, order, mode: int = MODE_HYBRID, sf: float = 0.0, ps: float =
     opts.superstep_extend = superstep_extend
     opts.label_cap = label_cap
     opts.window_target = window_target
+    opts.window_warps = window_warps
     opts.queue_split = queue_split
     h = C.c_void_p()
     _check(lib().chl_build(g._h, _ptr(o, _U32P), len(o), C.byref(opts), C.byref(h)), "build")

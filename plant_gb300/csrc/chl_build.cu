@@ -101,6 +101,7 @@ struct TreeArgs {
     uint32_t *ws_key;               // per warp slot, n entries each
     uint32_t *ws_vis;
     uint32_t *ws_front;             // per warp slot: queue, next queue, far pile
+    uint32_t *ws_win;               // window kernel: 6 n words per tree (block)
     BuildCtl *ctl;
     uint32_t hash_slots;            // root hash table slots (a power of two)
     uint32_t hash_shift;            // 32 - log2(hash_slots)
@@ -902,22 +903,47 @@ batch_kernel(TreeArgs a) {
 // again on every decrease keeps the flags exact; PLaNT's early exit
 // (distributed_memory/akiba.hpp:95) is tested at window boundaries, where the
 // count of queued not-via keys is exact.  GLL trees (iteration_gll) skip
-// expanding and labelling vertices ranked above the root.  A window takes a
-// few passes over hundreds of vertices where the IN criterion takes one
-// round per few dozen settled vertices.
-constexpr int kWinBatch = 256;   // members relaxed per batch
+// expanding and labelling vertices ranked above the root.
+//
+// A block of TW warps builds one tree: the warps split each pass's members
+// and the pile, and append to the tree's lists through shared counters (the
+// order of members and pile entries never matters).  Per tree, in the
+// window workspace (6 n words): key, touched vertices, members, the key each
+// member was last relaxed with, and the far pile double-buffered for the
+// block-parallel refill.
+constexpr int kWinBatch = 256;   // members relaxed per warp batch
+
+struct WinShared {
+    uint32_t root, nominal;
+    uint32_t nm;        // members of the window
+    uint32_t npile;     // entries of the current pile
+    uint32_t npile2;    // entries written to the other pile by a refill
+    uint32_t nvis;      // touched vertices
+    uint32_t thr;       // window end (exclusive)
+    uint32_t delta;     // window width (0: choose at the first refill)
+    uint32_t lo;        // lower bound of the live far keys
+    uint32_t kmin, kmax;
+    uint32_t changed;
+    uint32_t psel;      // which pile buffer is current
+    int ql;             // queued not-via keys (PLaNT)
+    uint32_t t_size, t_lab;
+    uint32_t err;
+};
 
 __host__ __device__ constexpr size_t window_smem_per_warp() {
     return ((size_t)8 * kWinBatch + (size_t)4 * (4 * kWinBatch + 1) + 8 + (size_t)12 * kEmit + 15) & ~(size_t)15;
 }
+__host__ __device__ constexpr size_t window_smem(int tw) {
+    return ((sizeof(WinShared) + 15) & ~(size_t)15) + (size_t)tw * window_smem_per_warp();
+}
 
-template <bool UNIT, bool PLANT>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+template <bool UNIT, bool PLANT, int TW>
+__global__ void __launch_bounds__(TW * 32)
 window_kernel(TreeArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const uint32_t lane = lane_id(), wib = threadIdx.x >> 5;
-    const uint32_t slot = blockIdx.x * kWarpsPerBlock + wib;
-    unsigned char *base = smem + wib * window_smem_per_warp();
+    WinShared &sh = *(WinShared *)smem;
+    const uint32_t tid = threadIdx.x, lane = lane_id(), wib = tid >> 5;
+    unsigned char *base = smem + ((sizeof(WinShared) + 15) & ~(size_t)15) + wib * window_smem_per_warp();
     uint64_t *s_ba = (uint64_t *)base;                 // arc begin of batch vertex
     uint32_t *s_bv = (uint32_t *)(s_ba + kWinBatch);   // batch vertex
     uint32_t *s_bk = s_bv + kWinBatch;                 // batch key
@@ -926,11 +952,11 @@ window_kernel(TreeArgs a) {
     uint64_t *s_ek = (uint64_t *)(((uintptr_t)(s_tl + kWinBatch) + 7) & ~(uintptr_t)7);   // staged label keys
     uint32_t *s_ev = (uint32_t *)(s_ek + kEmit);       // staged label distances
 
-    uint32_t *key = a.ws_key + (size_t)slot * a.n;
-    uint32_t *vis = a.ws_vis + (size_t)slot * a.n;
-    uint32_t *memb = a.ws_front + (size_t)slot * 3 * a.n;   // window members
-    uint32_t *mkey = memb + a.n;                              // key a member was last relaxed with
-    uint32_t *pile = mkey + a.n;                              // far vertices (first touch beyond thr)
+    uint32_t *key = a.ws_win + (size_t)blockIdx.x * 6 * a.n;
+    uint32_t *vis = key + a.n;
+    uint32_t *memb = vis + a.n;      // window members
+    uint32_t *mkey = memb + a.n;     // key a member was last relaxed with
+    uint32_t *piles = mkey + a.n;    // two far piles
     unsigned long long c_vis = 0, c_arcs = 0;
 
     uint32_t n_emit = 0;
@@ -953,37 +979,54 @@ window_kernel(TreeArgs a) {
         n_emit = 0;
         __syncwarp();
     };
+    // warp-wide append of the lanes with `take` to a list with a shared
+    // counter; returns this lane's index (only meaningful where take)
+    auto append_at = [&](bool take, uint32_t *counter) -> uint32_t {
+        const uint32_t m = __ballot_sync(kFull, take);
+        uint32_t b = 0;
+        if (m && lane == 0) b = atomicAdd(counter, (uint32_t)__popc(m));
+        b = __shfl_sync(kFull, b, 0);
+        return b + __popc(m & lanemask_lt());
+    };
 
     while (true) {
-        uint32_t r = kInf;
-        bool r_nominal = false;
-        if (lane == 0) r = fetch_root(a, r_nominal);
-        r = __shfl_sync(kFull, r, 0);
-        r_nominal = __shfl_sync(kFull, r_nominal ? 1u : 0u, 0) != 0;
+        if (tid == 0) {
+            bool nom = false;
+            sh.root = fetch_root(a, nom);
+            sh.nominal = nom ? 1u : 0u;
+            sh.t_size = 0;
+            sh.t_lab = 0;
+        }
+        __syncthreads();
+        const uint32_t r = sh.root;
         if (r == kInf) break;
-        uint32_t t_size = 0, t_lab = 0;
         const uint32_t v = a.order[r];
         for (int sd = 0; sd < a.sides; ++sd) {
             const int f = (a.sides == 1) ? 1 : sd;
             const uint64_t *goff = a.g_off[f];
             const uint4 *farc = a.g_farc[f];
             const uint2 *fhead = a.g_fhead[f];
-            if (lane == 0) {
+            if (tid == 0) {
                 __stcg(&key[v], 1u);
                 vis[0] = v;
                 memb[0] = v;
                 mkey[0] = kInf;
+                sh.nm = 1;
+                sh.npile = 0;
+                sh.nvis = 1;
+                sh.thr = 1;          // the first window holds the root alone
+                sh.delta = 0;
+                sh.lo = kInf;
+                sh.psel = 0;
+                sh.ql = 1;
+                sh.err = 0;
             }
-            __syncwarp();
-            uint32_t nvis = 1, nm = 1, npile = 0;
-            uint32_t thr = 1;            // the first window holds the root alone
-            uint32_t pmin = kInf;        // per lane: lower bound of the live far keys
-            uint32_t delta = 0;          // window width (0: choose at the first refill)
-            int ql = 1;                  // queued not-via keys (PLaNT)
+            __syncthreads();
+            uint32_t pmin = kInf;    // per lane: lower bound of far keys set since the last refill
             bool changed = false;
 
-            // Relax the nb vertices of the batch (arcs flattened over the lanes).
-            auto relax = [&](uint32_t nb) {
+            // Relax the warp's nb batch vertices (arcs flattened over the lanes).
+            auto relax = [&](uint32_t nb, uint32_t thr, uint32_t *pile) {
                 uint32_t total = 0, ncomp = 0;
                 for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
                     const uint32_t j = j0 + lane;
@@ -1027,100 +1070,84 @@ window_kernel(TreeArgs a) {
                     cur += (uint32_t)__popc(starts);
                     return own;
                 };
-                constexpr int RC = CHL_RELAX_CHUNKS;
-                for (uint32_t t0 = 0; t0 < total; t0 += 32 * RC) {
-                    uint32_t w[RC], nk[RC], old[RC];
-                    bool upd[RC];
-#pragma unroll
-                    for (int c = 0; c < RC; ++c) {
-                        const uint32_t tc = t0 + 32u * c;
-                        const uint32_t own = tc < total ? owner(tc) : 0u;
-                        const uint32_t t = tc + lane;
-                        w[c] = 0;
-                        nk[c] = 0;
-                        old[c] = kInf;
-                        upd[c] = false;
-                        if (t < total) {
-                            const uint32_t lo = s_tl[own];
-                            const uint64_t e = s_ba[lo] + (t - s_bx[own]);
-                            uint32_t len, rk;
-                            if (UNIT) {
-                                const uint2 hr = fhead[e];
-                                w[c] = hr.x;
-                                rk = hr.y;
-                                len = 1;
-                            } else {
-                                const uint4 hl = farc[e];
-                                w[c] = hl.x;
-                                len = hl.y;
-                                rk = hl.z;
-                            }
-                            const uint32_t kx = s_bk[lo];
-                            const uint32_t nv = (!PLANT || ((kx & 1u) && rk >= r)) ? 1u : 0u;
-                            const uint64_t dd64 = (uint64_t)(kx >> 1) + len;
-                            if (dd64 < 0x7FFFFFFFull) {
-                                nk[c] = (uint32_t)dd64 * 2u + nv;
-                                old[c] = atomicMin(&key[w[c]], nk[c]);
-                                upd[c] = nk[c] < old[c];
-                            } else {
-                                a.ctl->err = 1;   // the reference asserts dd < infty
-                            }
+                int dql = 0;
+                for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+                    const uint32_t own = owner(t0);
+                    const uint32_t t = t0 + lane;
+                    uint32_t w = 0, nk = 0, old = kInf;
+                    bool upd = false;
+                    if (t < total) {
+                        const uint32_t lo = s_tl[own];
+                        const uint64_t e = s_ba[lo] + (t - s_bx[own]);
+                        uint32_t len, rk;
+                        if (UNIT) {
+                            const uint2 hr = fhead[e];
+                            w = hr.x;
+                            rk = hr.y;
+                            len = 1;
+                        } else {
+                            const uint4 hl = farc[e];
+                            w = hl.x;
+                            len = hl.y;
+                            rk = hl.z;
+                        }
+                        const uint32_t kx = s_bk[lo];
+                        const uint32_t nv = (!PLANT || ((kx & 1u) && rk >= r)) ? 1u : 0u;
+                        const uint64_t dd64 = (uint64_t)(kx >> 1) + len;
+                        if (dd64 < 0x7FFFFFFFull) {
+                            nk = (uint32_t)dd64 * 2u + nv;
+                            old = atomicMin(&key[w], nk);
+                            upd = nk < old;
+                        } else {
+                            a.ctl->err = 1;   // the reference asserts dd < infty
                         }
                     }
-#pragma unroll
-                    for (int c = 0; c < RC; ++c) {
-                        const uint32_t dk = nk[c] >> 1;
-                        const bool fresh = upd[c] && old[c] == kInf;
-                        const bool in_win = upd[c] && dk < thr;
-                        if (in_win) changed = true;
-                        // a new member: first touched inside the window, or a
-                        // far vertex whose key drops into it (its far entry
-                        // goes stale)
-                        const bool join = in_win && (old[c] == kInf || (old[c] >> 1) >= thr);
-                        const uint32_t jm = __ballot_sync(kFull, join);
-                        if (join) {
-                            const uint32_t o = nm + __popc(jm & lanemask_lt());
-                            if (o < a.n) {
-                                memb[o] = w[c];
-                                mkey[o] = kInf;
-                            } else {
-                                a.ctl->err = 2;
-                            }
-                        }
-                        nm = min(nm + __popc(jm), a.n);
-                        const uint32_t vm = __ballot_sync(kFull, fresh);
-                        if (fresh) {
-                            const uint32_t o = nvis + __popc(vm & lanemask_lt());
-                            if (o < a.n) vis[o] = w[c];
-                            else a.ctl->err = 2;
-                        }
-                        nvis = min(nvis + __popc(vm), a.n);
-                        if (upd[c] && dk >= thr) pmin = min(pmin, dk);
-                        const bool to_far = fresh && dk >= thr;
-                        const uint32_t pm = __ballot_sync(kFull, to_far);
-                        if (to_far) {
-                            const uint32_t o = npile + __popc(pm & lanemask_lt());
-                            if (o < a.n) pile[o] = w[c];
-                            else a.ctl->err = 2;
-                        }
-                        npile = min(npile + __popc(pm), a.n);
-                        if (PLANT) {
-                            int dq = 0;
-                            if (upd[c]) dq = (int)(nk[c] & 1u) - (old[c] == kInf ? 0 : (int)(old[c] & 1u));
-                            ql += __reduce_add_sync(kFull, dq);
+                    const uint32_t dk = nk >> 1;
+                    const bool fresh = upd && old == kInf;
+                    const bool in_win = upd && dk < thr;
+                    changed |= in_win;
+                    // a new member: first touched inside the window, or a far
+                    // vertex whose key drops into it (its far entry goes stale)
+                    const bool join = in_win && (old == kInf || (old >> 1) >= thr);
+                    const uint32_t jo = append_at(join, &sh.nm);
+                    if (join) {
+                        if (jo < a.n) {
+                            memb[jo] = w;
+                            mkey[jo] = kInf;
+                        } else {
+                            sh.err = 2;
                         }
                     }
+                    const uint32_t vo = append_at(fresh, &sh.nvis);
+                    if (fresh) {
+                        if (vo < a.n) vis[vo] = w;
+                        else sh.err = 2;
+                    }
+                    if (upd && dk >= thr) pmin = min(pmin, dk);
+                    const bool to_far = fresh && dk >= thr;
+                    const uint32_t po = append_at(to_far, &sh.npile);
+                    if (to_far) {
+                        if (po < a.n) pile[po] = w;
+                        else sh.err = 2;
+                    }
+                    if (PLANT && upd) dql += (int)(nk & 1u) - (old == kInf ? 0 : (int)(old & 1u));
+                }
+                if (PLANT) {
+                    dql = __reduce_add_sync(kFull, dql);
+                    if (lane == 0 && dql) atomicAdd(&sh.ql, dql);
                 }
                 __syncwarp();
             };
 
             while (true) {
                 // passes over the window's members until no key below thr drops
-                do {
+                while (true) {
+                    const uint32_t thr = sh.thr;
+                    uint32_t *pile = piles + (size_t)sh.psel * a.n;
+                    const uint32_t pass_n = sh.nm;
                     changed = false;
-                    const uint32_t pass_n = nm;
                     uint32_t nb = 0;
-                    for (uint32_t b0 = 0; b0 < pass_n; b0 += 32) {
+                    for (uint32_t b0 = wib * 32; b0 < pass_n; b0 += 32 * TW) {
                         const uint32_t i = b0 + lane;
                         bool need = false;
                         uint32_t x = 0, k = 0;
@@ -1142,15 +1169,23 @@ window_kernel(TreeArgs a) {
                         nb += __popc(bm);
                         __syncwarp();
                         if (nb > (uint32_t)kWinBatch - 32) {
-                            relax(nb);
+                            relax(nb, thr, pile);
                             nb = 0;
                         }
                     }
-                    if (nb) relax(nb);
-                } while (__any_sync(kFull, changed));
+                    if (nb) relax(nb, thr, pile);
+                    __syncthreads();   // (a) every member counter and key update is done
+                    if (tid == 0) sh.changed = 0;
+                    __syncthreads();
+                    if (__any_sync(kFull, changed) && lane == 0) sh.changed = 1;
+                    __syncthreads();
+                    if (!sh.changed) break;
+                }
                 // the window is final: its labels, from the final keys
+                const uint32_t nm = sh.nm;
                 int nv_final = 0;
-                for (uint32_t b0 = 0; b0 < nm; b0 += 32) {
+                uint32_t lab = 0;
+                for (uint32_t b0 = wib * 32; b0 < nm; b0 += 32 * TW) {
                     const uint32_t i = b0 + lane;
                     bool emit = false;
                     uint32_t x = 0, k = 0;
@@ -1173,90 +1208,146 @@ window_kernel(TreeArgs a) {
                             s_ev[at] = k >> 1;
                         }
                         n_emit += __popc(em);
-                        t_lab += __popc(em);
+                        lab += __popc(em);
                     }
                 }
-                t_size += nm;
-                if (PLANT) {
-                    ql -= __reduce_add_sync(kFull, nv_final);
-                    if (ql == 0) break;   // plant :95 early exit (all queued keys are via)
+                if (PLANT) nv_final = __reduce_add_sync(kFull, nv_final);
+                const uint32_t pmin_w = __reduce_min_sync(kFull, pmin);
+                pmin = kInf;
+                if (lane == 0) {
+                    if (PLANT && nv_final) atomicAdd(&sh.ql, -nv_final);
+                    if (lab) atomicAdd(&sh.t_lab, lab);
+                    if (pmin_w != kInf) atomicMin(&sh.lo, pmin_w);
                 }
-                // next window from the far pile: entries below the old
-                // threshold are stale (they joined a window), entries below
-                // the new one join, the rest stay, compacted in place
-                nm = 0;
-                uint32_t lo = __reduce_min_sync(kFull, pmin);
-                if (delta == 0 && npile > 0) {
+                __syncthreads();   // (b) ql, lo final for this window
+                if (PLANT && sh.ql == 0) break;   // plant :95 early exit (all queued keys are via)
+                __syncthreads();   // every thread has read ql
+                if (tid == 0) {
+                    sh.t_size += nm;
+                    sh.nm = 0;
+                    sh.kmin = kInf;
+                    sh.kmax = 0;
+                }
+                __syncthreads();
+                if (sh.delta == 0) {
+                    // first refill: a width for about near_target vertices,
+                    // taking the far keys as spread evenly over [min, max]
+                    const uint32_t np = sh.npile;
+                    const uint32_t *pile = piles + (size_t)sh.psel * a.n;
                     uint32_t mn = kInf, mx = 0;
-                    for (uint32_t i = lane; i < npile; i += 32) {
+                    for (uint32_t i = tid; i < np; i += 32 * TW) {
                         const uint32_t k = __ldcg(&key[pile[i]]) >> 1;
                         mn = min(mn, k);
                         mx = max(mx, k);
                     }
                     mn = __reduce_min_sync(kFull, mn);
                     mx = __reduce_max_sync(kFull, mx);
-                    lo = mn;
-                    uint64_t d = (uint64_t)(mx - min(mn, mx)) * a.near_target / max(npile, 1u);
-                    if (d < 1) d = 1;
-                    if (d > 0x7FFFFFFFull) d = 0x7FFFFFFFull;
-                    delta = (uint32_t)d;
+                    if (lane == 0) {
+                        atomicMin(&sh.kmin, mn);
+                        atomicMax(&sh.kmax, mx);
+                    }
+                    __syncthreads();
+                    if (tid == 0 && np > 0) {
+                        sh.lo = sh.kmin;
+                        uint64_t d = (uint64_t)(sh.kmax - min(sh.kmin, sh.kmax)) * a.near_target / max(np, 1u);
+                        if (d < 1) d = 1;
+                        if (d > 0x7FFFFFFFull) d = 0x7FFFFFFFull;
+                        sh.delta = (uint32_t)d;
+                    }
+                    __syncthreads();
                 }
-                for (int pass = 0; pass < 4 && nm == 0 && npile > 0; ++pass) {
-                    const uint32_t t_old = thr;
-                    thr = sat_add(lo, delta);
-                    uint32_t keep = 0, moved = 0, kmin = kInf;
-                    for (uint32_t b0 = 0; b0 < npile; b0 += 32) {
+                // next window from the far pile: entries below the old
+                // threshold are stale (they joined a window), entries below
+                // the new one join, the rest move to the other pile buffer
+                for (int pass = 0; pass < 4; ++pass) {
+                    if (sh.nm != 0 || sh.npile == 0) break;
+                    const uint32_t t_old = sh.thr;
+                    const uint32_t thr = sat_add(sh.lo, sh.delta);
+                    const uint32_t np = sh.npile;
+                    const uint32_t *src = piles + (size_t)sh.psel * a.n;
+                    uint32_t *dst = piles + (size_t)(sh.psel ^ 1u) * a.n;
+                    __syncthreads();   // (d) every thread has read the window state
+                    if (tid == 0) {
+                        sh.npile2 = 0;
+                        sh.kmin = kInf;
+                    }
+                    __syncthreads();
+                    uint32_t kmin = kInf;
+                    for (uint32_t b0 = wib * 32; b0 < np; b0 += 32 * TW) {
                         const uint32_t i = b0 + lane;
-                        const bool valid = i < npile;
-                        const uint32_t x = valid ? pile[i] : 0u;
+                        const bool valid = i < np;
+                        const uint32_t x = valid ? src[i] : 0u;
                         const uint32_t k = valid ? (__ldcg(&key[x]) >> 1) : kInf;
                         const bool live = valid && k >= t_old;
                         const bool nr = live && k < thr;
                         const bool kp = live && !nr;
-                        const uint32_t nmk = __ballot_sync(kFull, nr);
-                        const uint32_t kmk = __ballot_sync(kFull, kp);
-                        // every lane has read its entry (ballots above), and a
-                        // kept entry moves only to a lower index
+                        const uint32_t mo = append_at(nr, &sh.nm);
                         if (nr) {
-                            const uint32_t o = moved + __popc(nmk & lanemask_lt());
-                            memb[o] = x;
-                            mkey[o] = kInf;
+                            memb[mo] = x;
+                            mkey[mo] = kInf;
                         }
+                        const uint32_t ko = append_at(kp, &sh.npile2);
                         if (kp) {
-                            pile[keep + __popc(kmk & lanemask_lt())] = x;
+                            dst[ko] = x;
                             kmin = min(kmin, k);
                         }
-                        moved += __popc(nmk);
-                        keep += __popc(kmk);
                     }
-                    __syncwarp();
-                    npile = keep;
-                    nm = moved;
-                    lo = __reduce_min_sync(kFull, kmin);
-                    pmin = lane == 0 ? lo : kInf;
-                    if (moved < a.near_target / 4) delta = delta < 0x40000000u ? 2u * delta : 0x7FFFFFFFu;
-                    else if (moved > 4 * a.near_target) delta = max(delta / 2, 1u);
+                    kmin = __reduce_min_sync(kFull, kmin);
+                    if (lane == 0 && kmin != kInf) atomicMin(&sh.kmin, kmin);
+                    __syncthreads();   // (e) the refill pass is complete
+                    if (tid == 0) {
+                        sh.thr = thr;
+                        sh.psel ^= 1u;
+                        sh.npile = sh.npile2;
+                        sh.lo = sh.kmin;
+                        const uint32_t moved = sh.nm;
+                        if (moved < a.near_target / 4) sh.delta = sh.delta < 0x40000000u ? 2u * sh.delta : 0x7FFFFFFFu;
+                        else if (moved > 4 * a.near_target) sh.delta = max(sh.delta / 2, 1u);
+                    }
+                    __syncthreads();
                 }
-                if (nm == 0) {
-                    if (npile > 0) a.ctl->err = 2;   // not reached: lo is exact from the second pass on
+                if (sh.nm == 0) {
+                    if (sh.npile > 0 && tid == 0) a.ctl->err = 2;   // not reached: lo is exact from the second pass on
                     break;
                 }
             }
-            c_vis += t_size;
-            for (uint32_t k = lane; k < nvis; k += 32) __stcg(&key[vis[k]], kInf);
-            __syncwarp();
+            __syncthreads();
+            if (sh.err && tid == 0) a.ctl->err = 2;
+            const uint32_t nvis = min(sh.nvis, a.n);
+            for (uint32_t k = tid; k < nvis; k += 32 * TW) __stcg(&key[vis[k]], kInf);
+            if (tid == 0) sh.t_size += sh.nm;   // the last window's members, when the early exit ended the tree
+            __syncthreads();
         }
         flush_labels();
-        if (lane == 0) {
-            a.tree_size[r - a.r0] = t_size;
-            a.tree_labels[r - a.r0] = t_lab;
-            finish_root(a, r_nominal);
+        if (tid == 0) {
+            c_vis += sh.t_size;
+            a.tree_size[r - a.r0] = sh.t_size;
+            a.tree_labels[r - a.r0] = sh.t_lab;
+            finish_root(a, sh.nominal != 0);
         }
+        __syncthreads();
     }
     if (lane == 0) {
         atomicAdd(&a.ctl->visits, c_vis);
         atomicAdd(&a.ctl->arcs, c_arcs);
     }
+}
+
+using TreeKernel = void (*)(TreeArgs);
+
+template <bool UNIT, bool PLANT>
+TreeKernel window_kernel_tw(uint32_t tw) {
+    switch (tw) {
+    case 1: return window_kernel<UNIT, PLANT, 1>;
+    case 2: return window_kernel<UNIT, PLANT, 2>;
+    case 8: return window_kernel<UNIT, PLANT, 8>;
+    default: return window_kernel<UNIT, PLANT, 4>;
+    }
+}
+
+TreeKernel window_kernel_for(bool unit, bool plant, uint32_t tw) {
+    if (unit) return plant ? window_kernel_tw<true, true>(tw) : window_kernel_tw<true, false>(tw);
+    return plant ? window_kernel_tw<false, true>(tw) : window_kernel_tw<false, false>(tw);
 }
 
 __global__ void fat_arcs(uint64_t m, const uint2 *arc, const uint32_t *rank, uint4 *out) {
@@ -1607,14 +1698,16 @@ struct Build {
     uint32_t *keep = nullptr;
     uint64_t *kpre = nullptr;
     uint32_t *tsize = nullptr, *tlab = nullptr;
-    uint32_t *ws_key = nullptr, *ws_vis = nullptr, *ws_front = nullptr;
+    uint32_t *ws_all = nullptr;   // tree workspace (both kernels' layouts)
+    uint32_t *ws_key = nullptr, *ws_vis = nullptr, *ws_front = nullptr;   // batch_kernel views
+    uint32_t win_trees = 0, win_tw = 4;   // window_kernel: trees (blocks) and warps per tree
+    int ws_layout = 0;   // 1: batch_kernel keys all INF, 2: window_kernel keys all INF
     BuildCtl *ctl = nullptr;
     void *tmp = nullptr;
     size_t tmp_bytes = 0;
     cudaStream_t st = nullptr;
     uint32_t warps = 0;   // warps the schedule is sized for
     uint32_t slots = 0;   // warp slots launched by batch_kernel
-    uint32_t slots_win = 0;   // warp slots launched by window_kernel (workspace: the larger)
     uint32_t hash_max = 2048;                // largest root hash table (slots)
     uint4 *farc[2] = {nullptr, nullptr};     // (head, length, rank[head], 0) per arc
     uint2 *fhead[2] = {nullptr, nullptr};    // (head, rank[head]) per arc, unit lengths
@@ -1646,9 +1739,7 @@ struct Build {
         cudaFree(kpre);
         cudaFree(tsize);
         cudaFree(tlab);
-        cudaFree(ws_key);
-        cudaFree(ws_vis);
-        cudaFree(ws_front);
+        cudaFree(ws_all);
         cudaFree(ctl);
         cudaFree(tmp);
         if (st) cudaStreamDestroy(st);
@@ -1810,20 +1901,33 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     // when no root is left for the superstep, and every refusal of a root is
     // final for it.  The grid and the workspace cover those alone (b.warps
     // still sets the first superstep's size).
-    int nbo = 0, nbw = 0;
+    int nbo = 0;
     CHL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &nbo, unit ? batch_kernel<true, true> : batch_kernel<false, true>, kWarpsPerBlock * 32, 0));
-    CHL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &nbw, unit ? window_kernel<true, true> : window_kernel<false, true>, kWarpsPerBlock * 32,
-        kWarpsPerBlock * window_smem_per_warp()));
     nbo = std::max(nbo, 1);
-    nbw = std::max(nbw, 1);
     b.slots = std::min(b.warps, (uint32_t)nbo * (uint32_t)sms * kWarpsPerBlock);
-    b.slots_win = std::min(b.warps, (uint32_t)nbw * (uint32_t)sms * kWarpsPerBlock);
-    const size_t slots = std::max(b.slots, b.slots_win);
-    if ((rc = dalloc(&b.ws_key, slots * n)) || (rc = dalloc(&b.ws_vis, slots * n))) return rc;
-    CHL_CUDA(cudaMemsetAsync(b.ws_key, 0xFF, slots * n * 4, b.st));
-    if ((rc = dalloc(&b.ws_front, slots * 3 * (size_t)n))) return rc;   // front, fnext, far pile
+    // window kernel (first superstep): one tree per block of win_tw warps,
+    // as many trees as are resident, 6 n words each
+    b.win_tw = opts.window_warps ? opts.window_warps : 4;
+    if (b.win_tw != 1 && b.win_tw != 2 && b.win_tw != 4 && b.win_tw != 8) {
+        set_error("window_warps must be 0, 1, 2, 4 or 8");
+        return CHL_ERR_INVALID;
+    }
+    {
+        int nbw = 0;
+        CHL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbw, window_kernel_for(unit, true, b.win_tw),
+                                                                 b.win_tw * 32, window_smem(b.win_tw)));
+        const uint64_t fit_trees = std::max<uint64_t>(1, ws_budget / std::max<uint64_t>(24ull * n, 1));
+        b.win_trees = (uint32_t)std::min<uint64_t>((uint64_t)std::max(nbw, 1) * sms, fit_trees);
+    }
+    // one workspace for both layouts: batch_kernel's key, vis and queue
+    // arrays per warp slot (5 n words), window_kernel's 6 n words per tree
+    const size_t ws_words = std::max((size_t)b.slots * 5 * n, (size_t)b.win_trees * 6 * n);
+    if ((rc = dalloc(&b.ws_all, ws_words))) return rc;
+    b.ws_key = b.ws_all;
+    b.ws_vis = b.ws_all + (size_t)b.slots * n;
+    b.ws_front = b.ws_all + (size_t)b.slots * 2 * n;
+    b.ws_layout = 0;   // set before each tree launch
     {
         // root hash slots: at most 2048, and within CHL_SMEM_CAP_KB of shared
         // memory per block (measured on the 1024-square grid: 2048 slots at 2
@@ -1879,7 +1983,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         // beyond that an overflow re-runs the superstep's root range.
         size_t fr = 0, tot = 0;
         CHL_CUDA(cudaMemGetInfo(&fr, &tot));
-        const uint64_t want = (uint64_t)budget_base + (uint64_t)std::max(b.slots, b.slots_win) * b.sides * n;
+        const uint64_t want = (uint64_t)budget_base + (uint64_t)std::max(b.slots, b.win_trees) * b.sides * n;
         const uint64_t fit = (uint64_t)(fr / 4 / 36);
         if ((rc = grow_new(b, std::min(want, fit)))) return rc;
     }
@@ -1974,24 +2078,34 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             }
             void (*kern)(TreeArgs);
             size_t smem_launch = smem;
-            int grid = blocks;
-            if (committed == 0 && win_target > 1) {
+            int grid = blocks, block = kWarpsPerBlock * 32;
+            const bool windowed = committed == 0 && win_target > 1;
+            if (windowed) {
                 // no committed labels: no tree can be pruned, so the trees
                 // are searched label-correcting in windows (window_kernel)
                 ta.near_target = win_target;
-                grid = (int)(b.slots_win / kWarpsPerBlock);
-                smem_launch = kWarpsPerBlock * window_smem_per_warp();
-                if (unit) kern = plant_now ? window_kernel<true, true> : window_kernel<true, false>;
-                else kern = plant_now ? window_kernel<false, true> : window_kernel<false, false>;
+                ta.ws_win = b.ws_all;
+                grid = (int)b.win_trees;
+                block = (int)b.win_tw * 32;
+                smem_launch = window_smem(b.win_tw);
+                kern = window_kernel_for(unit, plant_now, b.win_tw);
             } else if (unit) {
                 kern = plant_now ? batch_kernel<true, true> : batch_kernel<true, false>;
             } else {
                 kern = plant_now ? batch_kernel<false, true> : batch_kernel<false, false>;
             }
+            // the two layouts share the workspace: every key the next kernel
+            // reads is INF (each tree resets its own keys when it ends)
+            const int layout = windowed ? 2 : 1;
+            if (b.ws_layout != layout) {
+                const size_t words = windowed ? (size_t)b.win_trees * 6 * n : (size_t)b.slots * 5 * n;
+                CHL_CUDA(cudaMemsetAsync(b.ws_all, 0xFF, words * 4, b.st));
+                b.ws_layout = layout;
+            }
             CHL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_launch));
             CHL_CUDA(cudaEventRecord(ev_a, b.st));
-            kern<<<grid, kWarpsPerBlock * 32, smem_launch, b.st>>>(ta);
-            step_slots = (uint32_t)grid * kWarpsPerBlock;
+            kern<<<grid, block, smem_launch, b.st>>>(ta);
+            step_slots = (uint32_t)grid * (uint32_t)block / 32;
             CHL_CUDA(cudaGetLastError());
             CHL_CUDA(cudaEventRecord(ev_b, b.st));
             ++launches;

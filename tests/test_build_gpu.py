@@ -29,12 +29,17 @@ def same_labels(L, ref, n):
 
 @pytest.mark.parametrize("case", CASES)
 @pytest.mark.parametrize("mode", list(MODES))
-@pytest.mark.parametrize("sched", ["default", "small"])
+@pytest.mark.parametrize("sched", ["default", "small", "rounds", "win1", "win8"])
 def test_golden_label_files(P, case, mode, sched, tmp_path):
     c = label_case(case)
     g = P.Graph.read(c["gr"])
     order = P.Order.read(c["order"])
-    kw = {"first_superstep": 7, "growth": 0.3} if sched == "small" else {}
+    kw = {"small": {"first_superstep": 7, "growth": 0.3},
+          # first superstep by settle rounds instead of label-correcting windows
+          "rounds": {"window_target": 1},
+          # windows of about 2 vertices, one warp per tree; 8 warps per tree
+          "win1": {"window_target": 2, "window_warps": 1, "first_superstep": 40},
+          "win8": {"window_warps": 8, "window_target": 8}}.get(sched, {})
     L = P.build(g, order, mode=MODES[mode], **kw)
     out = str(tmp_path / "gpu.labels")
     L.write(out)
@@ -71,6 +76,9 @@ def test_queue_split_matches_oracle(P, O, split, kind):
     for mode in (MODES["hybrid"], MODES["gll"]):
         L = P.build(g, order, mode=mode, queue_split=split)
         assert same_labels(L, ref, g.get_n()), (split, mode)
+        # the first superstep's windows sized like the split
+        L = P.build(g, order, mode=mode, window_target=split, first_superstep=split * 4)
+        assert same_labels(L, ref, g.get_n()), ("window", split, mode)
 
 
 @pytest.mark.parametrize("mode", list(MODES))
@@ -186,7 +194,11 @@ def test_build_is_deterministic(P):
                # far entries, threshold doubling and halving), and off
                {"queue_split": 1}, {"queue_split": 2}, {"queue_split": 8}, {"queue_split": 8, "mode": 1},
                {"queue_split": 33, "first_superstep": 1, "growth": 0.05}, {"queue_split": 200},
-               {"queue_split": 8, "mode": 2}, {"queue_split": 8, "max_warps": 4}):
+               {"queue_split": 8, "mode": 2}, {"queue_split": 8, "max_warps": 4},
+               # first-superstep windows: off, tiny, large; 1, 2 and 8 warps per tree
+               {"window_target": 1}, {"window_target": 2}, {"window_target": 3, "mode": 1},
+               {"window_target": 100000}, {"window_warps": 1}, {"window_warps": 2, "window_target": 16},
+               {"window_warps": 8, "mode": 1}, {"window_warps": 8, "first_superstep": 5000, "window_target": 5}):
         b = P.build(g, order, sf=0.2, **kw).export()
         for x, y in zip(a, b):
             assert np.array_equal(x, y), kw
