@@ -125,8 +125,8 @@ static void init_arcs(chl_graph *g, std::vector<TmpArc> &a) {
     graph_fill_stats(g);
 }
 
-// add_tmp_arc (shared_memory/graph.hpp:156-162).  u and v arrive already
-// converted to the unsigned Vertex type, as in the reference.
+// add_tmp_arc (shared_memory/graph.hpp:156-162): the arc and its mirrored
+// reverse record, after a bounds check of the (already 32-bit) endpoints.
 static bool add_tmp_arc(chl_graph *g, long long n, std::vector<TmpArc> &tmp,
                         uint32_t u, uint32_t v, int32_t w, bool undirected) {
     if ((long long)u >= n || (long long)v >= n) return false;
@@ -136,178 +136,294 @@ static bool add_tmp_arc(chl_graph *g, long long n, std::vector<TmpArc> &tmp,
     return true;
 }
 
-static bool read_dimacs(FILE *file, bool undirected, chl_graph *g,
-                        std::vector<TmpArc> &tmp, long long &n) {
-    char buf[512];
-    long long u, v, w, m;
-    bool inited = false;
-    while (fgets(buf, sizeof(buf), file) != NULL) {
-        size_t L = strlen(buf);
-        if (L == 0 || buf[L - 1] != '\n') {
-            if (buf[0] != 'c') return false;
-            while (!feof(file) && fgetc(file) != '\n') {}
-        } else if (buf[0] == 'p') {
-            if (inited) return false;
-            inited = true;
-            if (sscanf(buf, "p sp %lld %lld", &n, &m) != 2) return false;
-        } else if (buf[0] == 'a') {
-            if (sscanf(buf, "a %lld %lld %lld", &u, &v, &w) != 3) return false;
-            if (!add_tmp_arc(g, n, tmp, (uint32_t)(u - 1), (uint32_t)(v - 1),
-                             (int32_t)w, undirected))
-                return false;
-        } else if (buf[0] == 'c') {
-            continue;
-        } else {
+// ---------------------------------------------------------------- text input
+//
+// The reference reads its formats with stdio: fgets into a 512-byte buffer
+// examined with strlen and sscanf (DIMACS, SNAP, edge lists), or fgetc
+// (METIS).  Here the file is a byte span and Text hands out exactly what
+// those calls would see, so the accept / reject decision and every value
+// match the reference byte for byte, including long lines (fgets returns
+// them in 511-byte pieces), NUL bytes (strlen stops there) and a last line
+// without a newline (fgets stops at the end of the input and sets feof).
+struct Text {
+    const unsigned char *p, *e;
+    bool at_eof = false;   // a read has tried to go past the last byte (feof)
+
+    // fgets(buf, 512): up to 511 bytes, through the first newline.  `vis` is
+    // strlen(buf); false when nothing is left.
+    struct Piece {
+        const char *s;
+        size_t vis;
+    };
+    bool piece(Piece &pc) {
+        if (p >= e) {
+            at_eof = true;
             return false;
         }
+        const unsigned char *q = p;
+        size_t k = 0;
+        bool nl = false;
+        while (k < 511 && q < e) {
+            ++k;
+            if (*q++ == '\n') {
+                nl = true;
+                break;
+            }
+        }
+        if (!nl && k < 511) at_eof = true;   // stopped by the end of the input
+        pc.s = (const char *)p;
+        pc.vis = 0;
+        while (pc.vis < k && pc.s[pc.vis] != '\0') ++pc.vis;
+        p = q;
+        return true;
     }
-    return true;
-}
-
-// character sources of the METIS reader: the file, or a buffer (whose end
-// reads as EOF)
-struct FileChars {
-    FILE *f;
-    int get() { return fgetc(f); }
-};
-struct BufChars {
-    const char *p, *e;
-    bool hit_end;
+    // fgetc: a byte, or EOF
     int get() {
-        if (p < e) return (int)(unsigned char)*p++;
-        hit_end = true;
-        return EOF;
+        if (p >= e) {
+            at_eof = true;
+            return EOF;
+        }
+        return *p++;
+    }
+    // fgetc until a newline (consumed) or the end
+    void rest_of_line() {
+        for (int c = get(); c != '\n' && c != EOF; c = get()) {}
     }
 };
 
-template <class Chars>
-static bool metis_parse(Chars &src, bool undirected, chl_graph *g, std::vector<TmpArc> &tmp, long long &n) {
-    int c, i = 0, fmt = 0, ncon = 0, skip = 0;
-    long long elem = 0;
-    uint32_t v = 0, head = 0xFFFFFFFFu;
-    // The reference never clears its `newline` flag, so a '%' anywhere
-    // starts a comment that runs to the end of the line.
-    const bool newline = true;
-    bool inelem = false;
-    (void)ncon;
-    do {
-        c = src.get();
-        if (newline && c == '%') {
-            while (c != '\n' && c != EOF) c = src.get();
-        } else if (c != EOF && isdigit(c)) {
-            inelem = true;
-            elem = elem * 10 + c - '0';
-        } else if (c == EOF || isspace(c)) {
-            if (inelem) {
-                if (v == 0) {
-                    if (i == 0) {
-                        n = elem;
-                    } else if (i == 1) {
-                        /* m */
-                    } else if (i == 2) {
-                        if ((elem % 10 > 1) || ((elem / 10) % 10 > 1) || elem > 111)
-                            return false;
-                        fmt = (int)elem;
-                        skip = (fmt >= 100) + (fmt % 100 >= 10);
-                    } else if (i == 3) {
-                        if (fmt % 100 < 10) return false;
-                        ncon = (int)elem;
-                        skip = (fmt >= 100) + ncon;
-                    } else {
-                        return false;
-                    }
-                } else if (i >= skip) {
-                    if (fmt % 10 == 1) {
-                        if ((i - skip) % 2 == 0) {
-                            head = (uint32_t)(elem - 1);
-                        } else if (!add_tmp_arc(g, n, tmp, v - 1, head,
-                                                (int32_t)elem, undirected)) {
-                            return false;
-                        }
-                    } else if (!add_tmp_arc(g, n, tmp, v - 1, (uint32_t)(elem - 1),
-                                            1, undirected)) {
-                        return false;
-                    }
-                }
-                ++i;
-                elem = 0;
-                inelem = false;
+static inline bool ends_line(const Text::Piece &pc) { return pc.vis > 0 && pc.s[pc.vis - 1] == '\n'; }
+
+// sscanf on s[0, len) with a format of literal bytes, ' ' (any run of white
+// space, possibly empty) and 'D' (a %lld conversion: white space, optional
+// sign, at least one digit; out-of-range values saturate as strtoll's do).
+// Returns the number of conversions before the first mismatch.
+static int scan_fmt(const char *s, size_t len, const char *fmt, long long *out) {
+    size_t k = 0;
+    int got = 0;
+    auto space = [&](size_t at) { return at < len && isspace((unsigned char)s[at]); };
+    for (const char *f = fmt; *f; ++f) {
+        if (*f == ' ') {
+            while (space(k)) ++k;
+        } else if (*f == 'D') {
+            while (space(k)) ++k;
+            bool neg = false;
+            if (k < len && (s[k] == '+' || s[k] == '-')) neg = s[k++] == '-';
+            const size_t d0 = k;
+            unsigned long long mag = 0;
+            bool over = false;
+            const unsigned long long lim = neg ? 9223372036854775808ull : 9223372036854775807ull;
+            for (; k < len && s[k] >= '0' && s[k] <= '9'; ++k) {
+                const unsigned dig = (unsigned)(s[k] - '0');
+                if (!over && mag <= (lim - dig) / 10) mag = mag * 10 + dig;
+                else over = true;
             }
-            if (c == '\n' || (!newline && c == EOF)) {
-                if (v > 0 && (i < skip || (fmt % 10 == 1 && (i - skip) % 2 == 1)))
-                    return false;
-                ++v;
-                i = 0;
-            }
+            if (k == d0) return got;
+            if (over) mag = lim;
+            out[got++] = neg ? (long long)(0ull - mag) : (long long)mag;
         } else {
+            if (k >= len || s[k] != *f) return got;
+            ++k;
+        }
+    }
+    return got;
+}
+
+// DIMACS (shared_memory/graph.hpp:168-189): `p sp n m` once, `a u v w` with
+// 1-based ids, `c` comments; a piece that does not end its line (long line,
+// or the last line without a newline) is allowed only as a comment, whose
+// remainder is skipped.
+static bool parse_dimacs(Text &t, bool undirected, chl_graph *g, std::vector<TmpArc> &tmp, long long &n) {
+    bool have_p = false;
+    Text::Piece pc;
+    long long v[3];
+    while (t.piece(pc)) {
+        const char c0 = pc.vis ? pc.s[0] : '\0';
+        if (!ends_line(pc)) {
+            if (c0 != 'c') return false;
+            if (!t.at_eof) t.rest_of_line();
+            continue;
+        }
+        switch (c0) {
+        case 'c':
+            break;
+        case 'p':
+            if (have_p || scan_fmt(pc.s, pc.vis, "p sp D D", v) != 2) return false;
+            have_p = true;
+            n = v[0];
+            break;
+        case 'a':
+            if (scan_fmt(pc.s, pc.vis, "a D D D", v) != 3 ||
+                !add_tmp_arc(g, n, tmp, (uint32_t)(v[0] - 1), (uint32_t)(v[1] - 1), (int32_t)v[2], undirected))
+                return false;
+            break;
+        default:
             return false;
         }
-    } while (c != EOF);
+    }
     return true;
 }
 
-static bool read_metis(FILE *file, bool undirected, chl_graph *g,
-                       std::vector<TmpArc> &tmp, long long &n) {
-    FileChars src{file};
-    return metis_parse(src, undirected, g, tmp, n);
+// SNAP (shared_memory/graph.hpp:262-282): `#` lines are comments (their
+// remainder skipped), one of them may be the `# Nodes: n Edges: m` header;
+// every other line holds `u v` (0-based, length 1) and must end with a
+// newline unless it is the last.
+static bool parse_snap(Text &t, bool undirected, chl_graph *g, std::vector<TmpArc> &tmp, long long &n) {
+    bool have_header = false;
+    Text::Piece pc;
+    long long v[2];
+    while (t.piece(pc)) {
+        if (pc.vis && pc.s[0] == '#') {
+            // sscanf stores each conversion as it succeeds: a comment that
+            // matches only up to the vertex count still sets n
+            const int got = scan_fmt(pc.s, pc.vis, "# Nodes: D Edges: D", v);
+            if (got >= 1) n = v[0];
+            if (got == 2) {
+                if (have_header) return false;
+                have_header = true;
+            }
+            if (!ends_line(pc)) t.rest_of_line();
+            continue;
+        }
+        if (!ends_line(pc) && !t.at_eof) return false;
+        if (scan_fmt(pc.s, pc.vis, "D D", v) != 2 ||
+            !add_tmp_arc(g, n, tmp, (uint32_t)v[0], (uint32_t)v[1], 1, undirected))
+            return false;
+    }
+    return true;
 }
 
-// true when the METIS reader returns false before it has read past
-// buf[0, len): it reads characters in order and never revisits a verdict, so
-// it rejects any file that starts with these bytes at the same character
-// (false: no verdict from this prefix)
+// Edge list (shared_memory/graph.hpp:284-308): `u v w` per line (0-based),
+// n = the number of distinct ids.  The reference indexes its arrays by the
+// raw ids, so ids outside [0, n) are undefined behaviour there; they are
+// rejected here.
+static bool parse_edgelist(Text &t, bool undirected, chl_graph *g, std::vector<TmpArc> &tmp, long long &n) {
+    std::set<long long> ids;
+    Text::Piece pc;
+    long long v[3];
+    while (t.piece(pc)) {
+        if (!ends_line(pc) && !t.at_eof) return false;
+        if (scan_fmt(pc.s, pc.vis, "D D D", v) != 3) return false;
+        tmp.push_back(TmpArc{(uint32_t)v[0], (uint32_t)v[1], (int32_t)v[2], 1, (uint8_t)undirected});
+        tmp.push_back(TmpArc{(uint32_t)v[1], (uint32_t)v[0], (int32_t)v[2], (uint8_t)undirected, 1});
+        g->m += 1 + (undirected ? 1 : 0);
+        ids.insert(v[0]);
+        ids.insert(v[1]);
+    }
+    n = (long long)ids.size();
+    for (const TmpArc &a : tmp)
+        if ((long long)a.u >= n || (long long)a.head >= n) return false;
+    return true;
+}
+
+// METIS (shared_memory/graph.hpp:211-256), in two stages.  The lexer turns
+// bytes into numbers and line ends: digits accumulate into a number (with
+// wrap-around, as the reference's long long does), white space ends it, a
+// newline also ends the line, '%' starts a comment that swallows everything
+// through the next newline -- that newline ends no line, and a number may go
+// on after it -- and any other byte rejects the file.  The end of the input
+// ends a pending number but no line, except inside a comment, where the
+// pending number is dropped.
+// The interpreter reads line 0 as the header `n m [fmt [ncon]]` (fmt's
+// digits each 0 or 1, fmt <= 111; ncon only when fmt's tens digit is 1) and
+// line v > 0 as the arcs of vertex v - 1 after `skip` leading numbers (vertex
+// size and weights): heads (1-based), each followed by a length when fmt's
+// ones digit is 1.  A line short of its leading numbers, or with a head but
+// no length, rejects the file.
+struct MetisInterp {
+    bool undirected;
+    chl_graph *g;
+    std::vector<TmpArc> &tmp;
+    long long &n;
+    uint32_t line = 0;
+    int idx = 0;          // numbers seen on this line
+    long long fmt = 0;
+    int skip = 0;
+    uint32_t head = 0xFFFFFFFFu;
+
+    bool number(long long x) {
+        if (line == 0) {
+            switch (idx) {
+            case 0:
+                n = x;
+                break;
+            case 1:
+                break;   // the arc count is not used
+            case 2:
+                if (x % 10 > 1 || (x / 10) % 10 > 1 || x > 111) return false;
+                fmt = x;
+                skip = (fmt >= 100) + (fmt % 100 >= 10);
+                break;
+            case 3:
+                if (fmt % 100 < 10) return false;
+                skip = (int)((fmt >= 100) + x);
+                break;
+            default:
+                return false;
+            }
+        } else if (idx >= skip) {
+            const bool weighted = fmt % 10 == 1;
+            if (weighted && (idx - skip) % 2 == 0) {
+                head = (uint32_t)(x - 1);
+            } else if (!add_tmp_arc(g, n, tmp, line - 1, weighted ? head : (uint32_t)(x - 1),
+                                    weighted ? (int32_t)x : 1, undirected)) {
+                return false;
+            }
+        }
+        ++idx;
+        return true;
+    }
+    bool end_line() {
+        if (line > 0 && (idx < skip || (fmt % 10 == 1 && (idx - skip) % 2 == 1))) return false;
+        ++line;
+        idx = 0;
+        return true;
+    }
+};
+
+// Runs the METIS lexer over t; true if the file is accepted.  *stopped_early
+// (may be NULL) tells whether a rejection came before the end of the input.
+static bool parse_metis(Text &t, MetisInterp &in, bool *stopped_early) {
+    unsigned long long acc = 0;
+    bool pending = false;
+    if (stopped_early) *stopped_early = false;
+    auto reject = [&]() {
+        if (stopped_early) *stopped_early = !t.at_eof;
+        return false;
+    };
+    while (true) {
+        const int c = t.get();
+        if (c == '%') {
+            int d;
+            do d = t.get(); while (d != '\n' && d != EOF);
+            if (d == EOF) return true;   // a pending number is dropped
+            continue;
+        }
+        if (c >= '0' && c <= '9') {
+            acc = acc * 10 + (unsigned)(c - '0');
+            pending = true;
+            continue;
+        }
+        if (c != EOF && !isspace(c)) return reject();
+        if (pending) {
+            if (!in.number((long long)acc)) return reject();
+            acc = 0;
+            pending = false;
+        }
+        if (c == EOF) return true;
+        if (c == '\n' && !in.end_line()) return reject();
+    }
+}
+
+// true when the METIS reader rejects a file that starts with buf[0, len)
+// before reading past it (its verdict is then final for the whole file)
 bool metis_rejects_prefix(const char *buf, size_t len) {
     chl_graph g;
     std::vector<TmpArc> tmp;
     long long n = 0;
-    BufChars src{buf, buf + len, false};
-    return !metis_parse(src, false, &g, tmp, n) && !src.hit_end;
-}
-
-static bool read_snap(FILE *file, bool undirected, chl_graph *g,
-                      std::vector<TmpArc> &tmp, long long &n) {
-    char buf[512];
-    long long u, v, m;
-    bool inited = false;
-    while (fgets(buf, sizeof(buf), file)) {
-        size_t L = strlen(buf);
-        if (buf[0] == '#') {
-            if (sscanf(buf, "# Nodes: %lld Edges: %lld", &n, &m) == 2) {
-                if (inited) return false;
-                inited = true;
-            }
-            for (int ch = L ? buf[L - 1] : EOF; ch != '\n' && ch != EOF; ch = fgetc(file)) {}
-        } else {
-            if ((L == 0 || buf[L - 1] != '\n') && !feof(file)) return false;
-            if (sscanf(buf, "%lld %lld", &u, &v) != 2) return false;
-            if (!add_tmp_arc(g, n, tmp, (uint32_t)u, (uint32_t)v, 1, undirected))
-                return false;
-        }
-    }
-    return true;
-}
-
-// The reference counts distinct ids as n and indexes per-vertex arrays by
-// the raw ids; ids outside [0, n) are undefined behaviour there and are
-// rejected here.
-static bool read_edgelist(FILE *file, bool undirected, chl_graph *g,
-                          std::vector<TmpArc> &tmp, long long &n) {
-    char buf[512];
-    long long u, v, w;
-    std::set<long long> nodes;
-    while (fgets(buf, sizeof(buf), file)) {
-        size_t L = strlen(buf);
-        if ((L == 0 || buf[L - 1] != '\n') && !feof(file)) return false;
-        if (sscanf(buf, "%lld %lld %lld", &u, &v, &w) != 3) return false;
-        tmp.push_back(TmpArc{(uint32_t)u, (uint32_t)v, (int32_t)w, 1, (uint8_t)undirected});
-        tmp.push_back(TmpArc{(uint32_t)v, (uint32_t)u, (int32_t)w, (uint8_t)undirected, 1});
-        g->m += 1 + (undirected ? 1 : 0);
-        if (nodes.insert(u).second) n++;
-        if (nodes.insert(v).second) n++;
-    }
-    for (const TmpArc &t : tmp)
-        if ((long long)t.u >= n || (long long)t.head >= n) return false;
-    return true;
+    Text t{(const unsigned char *)buf, (const unsigned char *)buf + len};
+    MetisInterp in{false, &g, tmp, n};
+    bool early = false;
+    return !parse_metis(t, in, &early) && early;
 }
 
 static int finish(chl_graph *g, long long n, std::vector<TmpArc> &tmp) {
@@ -367,24 +483,44 @@ using namespace chl;
 
 extern "C" int chl_graph_load(const char *path, int undirected, chl_graph **out) {
     if (!path || !out) return CHL_ERR_INVALID;
-    FILE *file = fopen(path, "r");
+    FILE *file = fopen(path, "rb");
     if (!file) {
         set_error(std::string("cannot open graph file ") + path);
         return CHL_ERR_IO;
     }
-    typedef bool (*parser_t)(FILE *, bool, chl_graph *, std::vector<TmpArc> &, long long &);
-    const parser_t parsers[4] = {read_dimacs, read_metis, read_snap, read_edgelist};
-    for (int p = 0; p < 4; ++p) {
-        chl_graph *g = new (std::nothrow) chl_graph();
-        if (!g) {
-            fclose(file);
-            return CHL_ERR_OOM;
+    std::vector<unsigned char> bytes;
+    {
+        unsigned char chunk[1 << 16];
+        size_t k;
+        while ((k = fread(chunk, 1, sizeof(chunk), file)) > 0) bytes.insert(bytes.end(), chunk, chunk + k);
+        const bool bad = ferror(file) != 0;
+        fclose(file);
+        if (bad) {
+            set_error(std::string("cannot read graph file ") + path);
+            return CHL_ERR_IO;
         }
+    }
+    // hl::Graph::read (shared_memory/graph.hpp:327-335): each reader in turn
+    // from the start of the file, the first that accepts it wins
+    const unsigned char *b = bytes.data(), *e = bytes.data() + bytes.size();
+    for (int fmt = 0; fmt < 4; ++fmt) {
+        chl_graph *g = new (std::nothrow) chl_graph();
+        if (!g) return CHL_ERR_OOM;
         std::vector<TmpArc> tmp;
         long long n = 0;
-        bool ok = parsers[p](file, undirected != 0, g, tmp, n);
+        Text t{b, e};
+        bool ok;
+        if (fmt == 0) {
+            ok = parse_dimacs(t, undirected != 0, g, tmp, n);
+        } else if (fmt == 1) {
+            MetisInterp in{undirected != 0, g, tmp, n};
+            ok = parse_metis(t, in, nullptr);
+        } else if (fmt == 2) {
+            ok = parse_snap(t, undirected != 0, g, tmp, n);
+        } else {
+            ok = parse_edgelist(t, undirected != 0, g, tmp, n);
+        }
         if (ok) {
-            fclose(file);
             int st = finish(g, n, tmp);
             if (st != CHL_OK) {
                 delete g;
@@ -394,9 +530,7 @@ extern "C" int chl_graph_load(const char *path, int undirected, chl_graph **out)
             return CHL_OK;
         }
         delete g;
-        rewind(file);
     }
-    fclose(file);
     set_error(std::string("no parser accepts graph file ") + path);
     return CHL_ERR_FORMAT;
 }

@@ -154,12 +154,17 @@ __device__ __forceinline__ bool match_lit(const char *&p, const char *e, const c
 }
 
 // sscanf(line, "# Nodes: %lld Edges: %lld") == 2, with p just after the '#'
-// (a blank of the format matches any run of white space, none included)
+// (a blank of the format matches any run of white space, none included).
+// A line that converts the vertex count but not the edge count still sets
+// n in the reference (sscanf stores each conversion as it succeeds), which
+// changes n between arcs: such files are left to the host (*unsup).
 __device__ __forceinline__ bool snap_header(const char *p, const char *e, long long &n, long long &m, bool &unsup) {
     skip_space(p, e);
     if (!match_lit(p, e, "Nodes:") || !scan_ll(p, e, n, unsup)) return false;
     skip_space(p, e);
-    return match_lit(p, e, "Edges:") && scan_ll(p, e, m, unsup);
+    const bool full = match_lit(p, e, "Edges:") && scan_ll(p, e, m, unsup);
+    if (!full) unsup = true;
+    return full;
 }
 
 // One line per thread.  DIMACS: `p` fills the header fields; SNAP: the

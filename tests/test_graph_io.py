@@ -99,3 +99,128 @@ def test_graph_from_csr_rejects_bad_input(P):
         P.Graph.from_csr(2, np.array([0, 1, 2], np.uint64), [1, 5], [1, 1])   # head out of range
     with pytest.raises(P.CHLError):
         P.Graph.from_csr(2, np.array([0, 1], np.uint64), [1], [1])           # off too short
+
+
+def _fuzz_files(seed, count):
+    """Seeded small graph files near the parsers' edge cases: every format,
+    comments, blank and long lines, signs, huge numbers, NUL bytes, stray
+    characters, missing final newlines, '%' comments inside METIS lines."""
+    rng = np.random.default_rng(seed)
+
+    def num():
+        r = rng.random()
+        if r < 0.7:
+            return str(int(rng.integers(0, 8)))
+        if r < 0.8:
+            return str(int(rng.integers(-3, 0)))
+        if r < 0.9:
+            return "+" + str(int(rng.integers(0, 8)))
+        return "".join(rng.choice(list("0123456789"), int(rng.integers(17, 22))))
+
+    def small():
+        return str(int(rng.integers(0, 9)))
+
+    def ws():
+        return rng.choice([" ", "  ", "\t", " \t "])
+
+    files = []
+    for k in range(count):
+        kind = k % 4
+        lines = []
+        nl = int(rng.integers(1, 9))
+        if kind == 0:   # DIMACS
+            lines.append("p sp " + small() + ws() + num())
+            for _ in range(nl):
+                c = rng.random()
+                if c < 0.6:
+                    lines.append("a" + ws() + num() + ws() + num() + ws() + num())
+                elif c < 0.75:
+                    lines.append("c " + "x" * int(rng.choice([3, 505, 510, 511, 600])))
+                elif c < 0.85:
+                    lines.append("psp" + small() + " " + num())
+                else:
+                    lines.append(rng.choice(["", "a 1 2", "x 1 2 3", "a 1 2 3 4", "p sp 3 4"]))
+        elif kind == 1:   # METIS
+            hdr = [small(), num()]
+            if rng.random() < 0.7:
+                hdr.append(str(rng.choice([0, 1, 10, 11, 100, 101, 110, 111, 2, 12])))
+                if rng.random() < 0.3:
+                    hdr.append(num())
+            lines.append(" ".join(hdr))
+            for _ in range(nl):
+                toks = [num() for _ in range(int(rng.integers(0, 6)))]
+                s = " ".join(t.lstrip("+-") for t in toks)
+                if rng.random() < 0.2:
+                    s += "%c" + rng.choice(["", " 12", "x"])
+                if rng.random() < 0.1:
+                    s = "% comment " + s
+                lines.append(s)
+        elif kind == 2:   # SNAP
+            if rng.random() < 0.8:
+                lines.append("# Nodes: " + small() + " Edges: " + num())
+            for _ in range(nl):
+                c = rng.random()
+                if c < 0.7:
+                    lines.append(num() + rng.choice(["\t", " "]) + num())
+                elif c < 0.85:
+                    lines.append("#" + "y" * int(rng.choice([1, 509, 511, 520])))
+                else:
+                    lines.append(rng.choice(["", "1", "# Nodes: 2 Edges: 1", "1 2 3"]))
+        else:   # edge list
+            for j in range(nl):
+                c = rng.random()
+                if c < 0.8:
+                    # a first number read as a METIS vertex count stays small
+                    lines.append((small() if j == 0 else num()) + " " + num() + " " + num())
+                else:
+                    lines.append(rng.choice(["", "1 2", "z", "1 2 3 4", "9" * 600]))
+        text = "\n".join(lines)
+        if rng.random() < 0.8:
+            text += "\n"
+        data = text.encode()
+        if rng.random() < 0.05:
+            p = int(rng.integers(0, max(1, len(data))))
+            data = data[:p] + b"\0" + data[p:]
+        files.append(data)
+    return files
+
+
+def _edgelist_ids_out_of_range(data):
+    """True for a file the reference reads as an edge list with an id outside
+    [0, number of distinct ids): undefined behaviour there (it indexes its
+    arrays by the raw ids), rejected by the package (a documented deviation)."""
+    ids = []
+    for line in data.split(b"\n"):
+        t = line.split()
+        if not line.strip():
+            continue
+        try:
+            ids += [int(t[0]) & 0xFFFFFFFF, int(t[1]) & 0xFFFFFFFF]
+        except (ValueError, IndexError):
+            return False
+    return bool(ids) and max(ids) >= len(set(ids))
+
+
+def test_parsers_match_reference_harness_on_fuzz(P, O, tmp_path):
+    """Where oracle/_ref/graphdump (hl::Graph::read compiled from the
+    reference) was built: 400 seeded edge-case files read both ways."""
+    import subprocess
+    exe = O.ref_bin("graphdump")
+    if exe is None:
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+    bad = []
+    for i, data in enumerate(_fuzz_files(2024, 400)):
+        path = str(tmp_path / f"f{i}.txt")
+        with open(path, "wb") as f:
+            f.write(data)
+        for und in (0, 1):
+            r = subprocess.run([exe, path, str(und)], capture_output=True, timeout=60)
+            if r.returncode != 0:
+                continue   # the reference itself fails on this file (e.g. allocation)
+            exp = r.stdout.decode()
+            got = product_dump(P, path, und)
+            if got == "FAIL\n" and exp != "FAIL\n" and _edgelist_ids_out_of_range(data):
+                continue
+            if got != exp:
+                bad.append((i, und))
+    assert not bad, bad[:10]
