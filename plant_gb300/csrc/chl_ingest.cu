@@ -61,6 +61,7 @@ constexpr int kLineMax = 511;   // fgets buffer of 512 bytes
 constexpr int kFmtDimacs = 0;
 constexpr int kFmtSnap = 1;
 constexpr int kFmtEdgelist = 2;
+constexpr int kFmtMetis = 3;
 
 // flags in the status word
 constexpr unsigned kFailFormat = 1u;    // not a file of the format by the reference's rules
@@ -291,6 +292,87 @@ __global__ void parse_lines(const char *buf, uint64_t S, const uint64_t *nl, uin
     }
 }
 
+// ---- METIS (shared_memory/graph.hpp:211-256) on the device
+// The reference reads METIS byte by byte: digits make numbers, white space
+// ends them, a newline ends a line, and '%' swallows everything through the
+// next newline, which then ends no line.  A physical line whose first
+// non-blank byte is '%' is therefore no line at all; every other physical
+// line is one METIS line.  A '%' after a number on a line joins that line
+// with the next (and may join two numbers): such files go to the host.
+
+// 1 for a physical line that is a METIS line, 0 for a comment line
+__global__ void metis_line_flags(const char *buf, uint64_t S, const uint64_t *nl, uint64_t nnl, uint64_t lines,
+                                 uint32_t *flag) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < lines; k += stride) {
+        const uint64_t start = k == 0 ? 0 : nl[k - 1] + 1;
+        const uint64_t end = k < nnl ? nl[k] : S;
+        uint64_t q = start;
+        while (q < end && is_space(buf[q])) ++q;
+        flag[k] = (q < end && buf[q] == '%') ? 0u : 1u;
+    }
+}
+
+// One METIS line per thread.  idx[k]: its line number (exclusive scan of the
+// flags; line 0, the header, was read on the host).  Vertex idx[k] - 1 gets
+// an arc per head after the first `skip` numbers, with the following number
+// as its length when `weighted`.  A line that ends with a newline must hold
+// all its leading numbers and no head without a length.
+__global__ void metis_parse_lines(const char *buf, uint64_t S, const uint64_t *nl, uint64_t nnl, uint64_t lines,
+                                  const uint32_t *flag, const uint64_t *idx, int skip, int weighted, ParseOut *po,
+                                  int64_t *au, int64_t *av, int64_t *aw) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < lines; k += stride) {
+        if (!flag[k] || idx[k] == 0) continue;
+        const uint64_t start = k == 0 ? 0 : nl[k - 1] + 1;
+        const bool has_nl = k < nnl;
+        const uint64_t end = has_nl ? nl[k] : S;
+        const long long line = (long long)idx[k];
+        int i = 0, digits = 0;
+        long long x = 0, head = 0;
+        bool bad = false;
+        for (uint64_t q = start; q <= end; ++q) {
+            const char c = q < end ? buf[q] : ' ';
+            if (c >= '0' && c <= '9') {
+                if (++digits > 18) {
+                    atomicOr(&po->status, kUnsupported);
+                    bad = true;
+                    break;
+                }
+                x = x * 10 + (c - '0');
+                continue;
+            }
+            if (c == '%') {
+                atomicOr(&po->status, kUnsupported);   // a comment after numbers joins lines
+                bad = true;
+                break;
+            }
+            if (!is_space(c)) {
+                atomicOr(&po->status, kFailFormat);
+                bad = true;
+                break;
+            }
+            if (digits) {
+                if (i >= skip) {
+                    if (weighted && ((i - skip) & 1) == 0) {
+                        head = x;
+                    } else {
+                        const unsigned long long slot = atomicAdd(&po->arcs, 1ull);
+                        au[slot] = line;                 // vertex line - 1
+                        av[slot] = weighted ? head : x;  // head + 1
+                        aw[slot] = weighted ? x : 1;
+                    }
+                }
+                ++i;
+                digits = 0;
+                x = 0;
+            }
+        }
+        if (!bad && has_nl && (i < skip || (weighted && ((i - skip) & 1))))
+            atomicOr(&po->status, kFailFormat);
+    }
+}
+
 // edge-list ids as order-preserving unsigned keys (sign bit flipped)
 __global__ void id_keys(uint64_t arcs, const int64_t *au, const int64_t *av, uint64_t *key, uint32_t *val) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -503,6 +585,62 @@ int read_file(const char *path, std::vector<char> &buf) {
     return CHL_OK;
 }
 
+// The METIS header: the first physical line whose first non-blank byte is
+// not '%' (comment lines before it are swallowed), read with the reference's
+// rules: `n m [fmt [ncon]]`, fmt's digits each 0 or 1 and fmt <= 111, ncon
+// only when fmt's tens digit is 1.  Returns 1 with n, skip and weighted set,
+// 0 when the host must decide (a rejected header, a comment after a number,
+// more than 18 digits).
+int metis_header(const std::vector<char> &file, long long &n, int &skip, int &weighted) {
+    size_t q = 0;
+    const size_t S = file.size();
+    auto space = [&](char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r'; };
+    while (true) {   // skip comment lines
+        size_t a = q;
+        while (a < S && space(file[a]) && file[a] != '\n') ++a;
+        if (a < S && file[a] == '%') {
+            while (a < S && file[a] != '\n') ++a;
+            q = a + 1;
+            continue;
+        }
+        break;
+    }
+    long long tok[4] = {0, 0, 0, 0};
+    int cnt = 0, digits = 0;
+    long long x = 0;
+    for (; q <= S; ++q) {
+        const char c = q < S ? file[q] : ' ';
+        if (c >= '0' && c <= '9') {
+            if (++digits > 18) return 0;
+            x = x * 10 + (c - '0');
+            continue;
+        }
+        if (!space(c)) return 0;
+        if (digits) {
+            if (cnt >= 4) return 0;
+            tok[cnt++] = x;
+            digits = 0;
+            x = 0;
+        }
+        if (c == '\n' || q == S) break;
+    }
+    if (cnt == 0) return 0;
+    n = tok[0];
+    long long fmt = 0;
+    skip = 0;
+    if (cnt >= 3) {
+        fmt = tok[2];
+        if (fmt % 10 > 1 || (fmt / 10) % 10 > 1 || fmt > 111) return 0;
+        skip = (fmt >= 100) + (fmt % 100 >= 10);
+    }
+    if (cnt == 4) {
+        if (fmt % 100 < 10) return 0;
+        skip = (int)((fmt >= 100) + tok[3]);
+    }
+    weighted = fmt % 10 == 1;
+    return 1;
+}
+
 // 1: the file is of format fmt by the reference's rules and the graph was
 // built; 0: defer to the host parsers; < 0: -status of an error
 int ingest_text(const std::vector<char> &file, int fmt, bool undirected, chl_graph *g) {
@@ -537,7 +675,25 @@ int ingest_text(const std::vector<char> &file, int fmt, bool undirected, chl_gra
     CHL_CUDA_NEG(cudaMemcpy(d_po, &h, sizeof(h), cudaMemcpyHostToDevice));
     int64_t *au, *av, *aw;
     if ((rc = pool.get(&au, lines)) || (rc = pool.get(&av, lines)) || (rc = pool.get(&aw, lines))) return -rc;
-    if (lines) {
+    long long metis_n = 0;
+    if (fmt == kFmtMetis) {
+        int skip = 0, weighted = 0;
+        if (!metis_header(file, metis_n, skip, weighted)) return 0;
+        uint32_t *d_flag;
+        uint64_t *d_idx;
+        if ((rc = pool.get(&d_flag, lines + 1)) || (rc = pool.get(&d_idx, lines + 2))) return -rc;
+        void *ltmp;
+        const size_t ltmp_bytes = scan_tmp_bytes(std::max<uint64_t>(lines, 1));
+        if ((rc = pool.get((char **)&ltmp, ltmp_bytes))) return -rc;
+        if (lines) {
+            metis_line_flags<<<device_sms() * 8, 256>>>(d_buf, S, d_nl, nnl, lines, d_flag);
+            CHL_CUDA_NEG(cudaGetLastError());
+            if ((rc = scan_u32_excl(d_flag, d_idx, lines, nullptr, ltmp, ltmp_bytes, 0))) return -rc;
+            metis_parse_lines<<<device_sms() * 8, 256>>>(d_buf, S, d_nl, nnl, lines, d_flag, d_idx, skip, weighted,
+                                                         d_po, au, av, aw);
+            CHL_CUDA_NEG(cudaGetLastError());
+        }
+    } else if (lines) {
         parse_lines<<<device_sms() * 8, 256>>>(d_buf, S, d_nl, nnl, lines, fmt, d_po, au, av, aw);
         CHL_CUDA_NEG(cudaGetLastError());
     }
@@ -566,6 +722,8 @@ int ingest_text(const std::vector<char> &file, int fmt, bool undirected, chl_gra
             CHL_CUDA_NEG(cudaMemcpy(&nd, d_dist, 8, cudaMemcpyDeviceToHost));
             n = (long long)nd;
         }
+    } else if (fmt == kFmtMetis) {
+        n = metis_n;
     } else {
         if (h.p_count > 1) return 0;                   // a second header
         n = h.p_count ? h.n : 0;                       // arcs before the header see n = 0
@@ -586,7 +744,8 @@ int ingest_text(const std::vector<char> &file, int fmt, bool undirected, chl_gra
     const int grid = device_sms() * 8;
     CHL_CUDA_NEG(cudaMemset(d_status, 0, 4));
     if (arcs)
-        make_records<<<grid, 256>>>(arcs, au, av, aw, n, fmt == kFmtDimacs ? 1 : 0, undirected ? 1 : 0, ru, rh,
+        make_records<<<grid, 256>>>(arcs, au, av, aw, n, (fmt == kFmtDimacs || fmt == kFmtMetis) ? 1 : 0,
+                                    undirected ? 1 : 0, ru, rh,
                                     rl, rf, d_status);
     unsigned st = 0;
     CHL_CUDA_NEG(cudaMemcpy(&st, d_status, 4, cudaMemcpyDeviceToHost));
@@ -691,6 +850,7 @@ extern "C" int chl_graph_load_gpu(const char *path, int undirected, chl_graph **
     if (first == '#') fmt = kFmtSnap;
     else if (file.empty() || file[0] == 'p' || file[0] == 'a' || file[0] == 'c') fmt = kFmtDimacs;
     else if (metis_rejects_prefix(file.data(), std::min<size_t>(file.size(), (size_t)1 << 16))) fmt = kFmtEdgelist;
+    else fmt = kFmtMetis;   // files METIS rejects later are left to the host
     const int r = fmt < 0 ? 0 : ingest_text(file, fmt, undirected != 0, g);
     if (r == 1) {
         if (parsed_on_gpu) *parsed_on_gpu = 1;

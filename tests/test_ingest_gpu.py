@@ -1,4 +1,4 @@
-"""GPU DIMACS, SNAP and edge-list ingestion against the host parsers (which
+"""GPU DIMACS, METIS, SNAP and edge-list ingestion against the host parsers (which
 follow the reference's Graph::read and are pinned to it by test_graph_io.py).
 
 Every file must give the same outcome both ways: the same CSRs in both
@@ -159,7 +159,7 @@ def test_random_snap_files(P, tmp_path):
 
 def test_edgelist_quirks(P, tmp_path):
     # a file DIMACS and SNAP reject on its first line is an edge list when the
-    # host's METIS reader rejects a prefix of it; METIS files stay on the host
+    # host's METIS reader rejects a prefix of it
     cases = {
         "plain": ("0 1 5\n1 2 3\n2 0 4\n", True),
         "unit_weights": ("0 1 1\n1 2 1\n2 0 1\n", True),
@@ -171,9 +171,6 @@ def test_edgelist_quirks(P, tmp_path):
         "loops_and_dups": ("0 0 3\n0 1 5\n0 1 2\n1 0 7\n", True),
         "weight_10": ("0 1 10\n1 0 11\n", True),
         "negative_weight": ("0 1 -4\n1 0 2\n", True),
-        "metis_empty": ("0 5 1\n", False),
-        "metis_two_numbers": ("0 1\n", False),
-        "metis_graph": ("3 2\n2\n1 3\n2\n", False),
         "negative_id": ("-1 0 3\n0 1 2\n", False),
         "blank_line": ("0 1 5\n\n1 0 2\n", False),
         "long_line": ("0 1 " + " " * 600 + "5\n", False),
@@ -202,3 +199,42 @@ def test_random_edgelist_files(P, tmp_path):
         for und in (False, True):
             r = same(P, p, und, expect_gpu=True)
             assert r[0] == "ok" and r[1][0] == n
+
+
+def test_metis_on_gpu(P, tmp_path):
+    """METIS files are read on the GPU (comment lines included); a comment
+    after a number, which joins two lines in the reference's reader, and
+    files whose header the reference rejects are left to the host."""
+    cases = {
+        "empty_weighted": ("0 5 1\n", True),
+        "two_numbers": ("0 1\n", True),
+        "plain": ("3 2\n2\n1 3\n2\n", True),
+        "comments": ("% a METIS file\n%\n3 2\n  % indented comment\n2\n1 3\n% last\n2\n", True),
+        "arc_lengths": ("3 3 1\n2 7 3 4\n1 7\n1 4\n", True),
+        "vertex_sizes": ("3 2 100\n5 2\n6 1 3\n7 2\n", True),
+        "vertex_weights_ncon": ("3 2 11 2\n1 1 2 5\n1 1 1 5 3 6\n1 1 2 6\n", True),
+        "all_fields": ("3 2 111 1\n9 1 2 5\n9 1 1 5 3 6\n9 1 2 6\n", True),
+        "no_final_newline": ("3 2\n2\n1 3\n2", True),
+        "crlf_tabs": ("3 2\r\n2\r\n1\t3\r\n2\r\n", True),
+        "blank_lines": ("4 1\n2\n1\n\n\n", True),
+        "long_line": ("3 3\n2 3" + " " * 900 + "\n1 3\n1 2\n", True),
+        "comment_after_number": ("3 2\n2 % x\n1 3\n2\n", False),
+        "bad_fmt": ("3 2 2\n2\n1 3\n2\n", False),
+        "missing_length": ("3 3 1\n2\n1 7\n1 4\n", False),
+        "too_many_lines": ("2 1\n2\n1\n1\n", False),
+        "stray_byte": ("3 2\n2\n1 x\n2\n", False),
+    }
+    for name, (text, on_gpu) in cases.items():
+        p = write(tmp_path, name + ".graph", text)
+        for und in (False, True):
+            same(P, p, und, expect_gpu=on_gpu)
+
+
+def test_fuzz_files_agree(P, tmp_path):
+    """The 400 seeded edge-case files of the parser fuzz (every format): the
+    GPU path and the host parsers give the same graph or the same error."""
+    from test_graph_io import _fuzz_files
+    for i, data in enumerate(_fuzz_files(2024, 400)):
+        p = write(tmp_path, f"z{i}.txt", data)
+        for und in (False, True):
+            same(P, p, und)
