@@ -356,6 +356,9 @@ int chl_server_submit(chl_server *s, const uint32_t *pairs, size_t k,
  * CHL_ERR_INVALID if the server is freed while the caller waits. */
 int chl_server_wait(chl_server *s, uint64_t req_id, int32_t *out,
                     double timeout_ms, double *latency_ms);
+/* Callers currently blocked in chl_server_submit (waiting for admission)
+ * or chl_server_wait (no counterpart in the reference; for monitoring). */
+int chl_server_blocked(chl_server *s, uint32_t *callers);
 /* Totals since creation: launches, pairs answered, requests completed. */
 int chl_server_stats(chl_server *s, uint64_t *launches, uint64_t *pairs,
                      uint64_t *requests);

@@ -136,6 +136,7 @@ SIGNATURES = {
     "chl_server_submit": (C.c_int, [_P, _U32P, C.c_size_t, _U64P]),
     "chl_server_wait": (C.c_int, [_P, C.c_uint64, _I32P, C.c_double, C.POINTER(C.c_double)]),
     "chl_server_stats": (C.c_int, [_P, _U64P, _U64P, _U64P]),
+    "chl_server_blocked": (C.c_int, [_P, _U32P]),
     "chl_server_free": (None, [_P]),
     "chl_gnn_create": (C.c_int, [C.c_uint32, C.c_uint64, C.POINTER(_P)]),
     "chl_gnn_param_count": (C.c_size_t, [_P]),
@@ -535,15 +536,23 @@ class Server:
         _check(lib().chl_server_wait(self._h, rid, _ptr(out, _I32P), timeout_ms, C.byref(lat)), "wait")
         return out, lat.value
 
+    def blocked(self) -> int:
+        """Callers blocked in submit (admission) or wait."""
+        x = C.c_uint32()
+        _check(lib().chl_server_blocked(self._h, C.byref(x)), "server blocked")
+        return x.value
+
     def stats(self):
         a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
         _check(lib().chl_server_stats(self._h, C.byref(a), C.byref(b), C.byref(c)), "stats")
         return {"launches": a.value, "pairs": b.value, "requests": c.value}
 
     def close(self):
-        if self._h:
-            lib().chl_server_free(self._h)
-            self._h = None
+        # the handle is dropped before it is freed: no method call starts on
+        # a server that is being freed
+        h, self._h = self._h, None
+        if h:
+            lib().chl_server_free(h)
 
     def __del__(self):
         try:

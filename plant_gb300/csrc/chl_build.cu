@@ -897,8 +897,9 @@ batch_kernel(TreeArgs a) {
 // below thr.  Then every key below thr is final -- it is the minimum over all
 // paths, and every other queued key is at least thr -- so the window's labels
 // are emitted from the final keys, and the next window, [thr, lo + delta),
-// is taken from the far pile (lo its smallest live key; delta adapts so that
-// a window holds about near_target vertices).  Keys carry PLaNT's via flag
+// is taken from the far pile (lo its smallest live key; delta starts at the
+// spread of the root's neighbours' distances and is halved or doubled after
+// each window so that a window holds about near_target vertices).  Keys carry PLaNT's via flag
 // (distance * 2 + not-via), and a flag change is a key decrease, so relaxing
 // again on every decrease keeps the flags exact; PLaNT's early exit
 // (distributed_memory/akiba.hpp:95) is tested at window boundaries, where the
@@ -1227,11 +1228,16 @@ window_kernel(TreeArgs a) {
                     sh.nm = 0;
                     sh.kmin = kInf;
                     sh.kmax = 0;
+                    // the width follows the size of the window just finished
+                    if (sh.delta) {
+                        if (nm > 2 * a.near_target) sh.delta = max(sh.delta / 2, 1u);
+                        else if (nm < a.near_target / 2) sh.delta = sh.delta < 0x40000000u ? 2u * sh.delta : 0x7FFFFFFFu;
+                    }
                 }
                 __syncthreads();
                 if (sh.delta == 0) {
-                    // first refill: a width for about near_target vertices,
-                    // taking the far keys as spread evenly over [min, max]
+                    // first refill: the spread of the root's neighbours'
+                    // distances (then adapted window by window)
                     const uint32_t np = sh.npile;
                     const uint32_t *pile = piles + (size_t)sh.psel * a.n;
                     uint32_t mn = kInf, mx = 0;
@@ -1249,10 +1255,7 @@ window_kernel(TreeArgs a) {
                     __syncthreads();
                     if (tid == 0 && np > 0) {
                         sh.lo = sh.kmin;
-                        uint64_t d = (uint64_t)(sh.kmax - min(sh.kmin, sh.kmax)) * a.near_target / max(np, 1u);
-                        if (d < 1) d = 1;
-                        if (d > 0x7FFFFFFFull) d = 0x7FFFFFFFull;
-                        sh.delta = (uint32_t)d;
+                        sh.delta = max(sh.kmax - min(sh.kmin, sh.kmax), 1u);
                     }
                     __syncthreads();
                 }
@@ -1300,9 +1303,6 @@ window_kernel(TreeArgs a) {
                         sh.psel ^= 1u;
                         sh.npile = sh.npile2;
                         sh.lo = sh.kmin;
-                        const uint32_t moved = sh.nm;
-                        if (moved < a.near_target / 4) sh.delta = sh.delta < 0x40000000u ? 2u * sh.delta : 0x7FFFFFFFu;
-                        else if (moved > 4 * a.near_target) sh.delta = max(sh.delta / 2, 1u);
                     }
                     __syncthreads();
                 }

@@ -296,6 +296,13 @@ extern "C" int chl_server_wait(chl_server *s, uint64_t req_id, int32_t *out, dou
     return CHL_OK;
 }
 
+extern "C" int chl_server_blocked(chl_server *s, uint32_t *callers) {
+    if (!s || !callers) return CHL_ERR_INVALID;
+    std::lock_guard<std::mutex> g(s->mu);
+    *callers = (uint32_t)s->blocked;
+    return CHL_OK;
+}
+
 extern "C" int chl_server_stats(chl_server *s, uint64_t *launches, uint64_t *pairs, uint64_t *requests) {
     if (!s) return CHL_ERR_INVALID;
     std::lock_guard<std::mutex> g(s->mu);
