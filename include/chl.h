@@ -195,7 +195,7 @@ typedef struct chl_build_opts {
     uint32_t window_target; /* trees of a superstep with no committed labels
                              (the first) are searched label-correcting in
                              distance windows of about this many vertices:
-                             0 auto (1024), 1 off (batched settle rounds)   */
+                             0 auto (off), 1 off (batched settle rounds)    */
     uint32_t window_warps; /* warps building one such tree: 0 auto (4), 1, 2,
                              4 or 8                                         */
     uint32_t reserved[1];

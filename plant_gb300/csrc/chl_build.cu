@@ -2004,7 +2004,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     // superstep early.
     // label-correcting windows of the first superstep's trees: about this
     // many vertices per window (1: IN-criterion rounds instead)
-    const uint32_t win_target = opts.window_target ? opts.window_target : 1024u;
+    const uint32_t win_target = opts.window_target ? opts.window_target : 1u;
     const uint32_t first = opts.first_superstep ? opts.first_superstep : auto_first;
     const double growth = opts.growth > 0 ? opts.growth : auto_growth;
     while (r0 < n && (opts.root_limit == 0 || r0 < opts.root_limit)) {
