@@ -169,7 +169,11 @@ typedef struct chl_build_opts {
     double sf;            /* superstep label budget factor (hhl -s), 0 = auto
                              (32 on heavy-tailed graphs, 1024 otherwise)  */
     double ps;            /* phase switch ratio tree/label (hhl -ps)          */
-    int32_t autotune;     /* 1: pick superstep growth from graph statistics   */
+    int32_t autotune;     /* 1: schedule options left at 0 come from the
+                             tuned-schedule table for the graph's class
+                             (chl_graph_class; $CHL_SCHEDULES or
+                             tuned_schedules.txt beside the library), the
+                             rest from graph statistics                    */
     int32_t use_graphs;   /* 1: capture the per-superstep kernel chain in a
                              CUDA graph                                       */
     int32_t verbose;      /* 1: print the reference's summary line            */
@@ -229,6 +233,11 @@ typedef struct chl_build_stats {
  * device memory. */
 int chl_build(const chl_graph *g, const uint32_t *order, uint32_t n,
               const chl_build_opts *opts, chl_labels **out);
+/* The graph's class in the tuned-schedule table (no reference counterpart):
+ * "sym|dir-n2^<log2 n>-deg<mean out-degree>-skewheavy|flat", the key under
+ * which plant_gb300/autotune.py stores the schedule it measured fastest for
+ * graphs of that kind, and which chl_build with opts->autotune reads. */
+int chl_graph_class(const chl_graph *g, char *buf, size_t cap);
 /* Statistics of the build that produced `l`. */
 int chl_build_get_stats(const chl_labels *l, chl_build_stats *stats);
 

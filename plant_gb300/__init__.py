@@ -110,6 +110,7 @@ SIGNATURES = {
     "chl_order_betweenness": (C.c_int, [_P, C.c_uint32, C.c_uint64, _U32P]),
     "chl_build_opts_default": (None, [C.POINTER(BuildOpts)]),
     "chl_build": (C.c_int, [_P, _U32P, C.c_uint32, C.POINTER(BuildOpts), C.POINTER(_P)]),
+    "chl_graph_class": (C.c_int, [_P, C.c_char_p, C.c_size_t]),
     "chl_build_get_stats": (C.c_int, [_P, C.POINTER(BuildStats)]),
     "chl_labels_write": (C.c_int, [_P, C.c_char_p]),
     "chl_labels_read": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
@@ -260,6 +261,12 @@ class Graph:
 
     def out_arcs(self) -> int:
         return lib().chl_graph_out_arcs(self._h)
+
+    def graph_class(self) -> str:
+        """Class of the graph in the tuned-schedule table (chl_graph_class)."""
+        buf = C.create_string_buffer(128)
+        _check(lib().chl_graph_class(self._h, buf, len(buf)), "graph class")
+        return buf.value.decode()
 
     def symmetric(self) -> bool:
         return bool(lib().chl_graph_symmetric(self._h))

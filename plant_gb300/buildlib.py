@@ -29,6 +29,7 @@ SOURCES = [
     "chl_gnn.cu",
     "chl_labelio.cu",
     "chl_ingest.cu",
+    "chl_tune.cpp",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

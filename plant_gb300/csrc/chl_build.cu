@@ -1797,6 +1797,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     chl_build_opts opts;
     if (opts_in) opts = *opts_in;
     else chl_build_opts_default(&opts);
+    if (g && opts.autotune) apply_tuned_schedule(g, opts);
     if (!g || !order_h || !out || n != g->n) {
         set_error("order size must equal the number of graph vertices");
         return CHL_ERR_INVALID;

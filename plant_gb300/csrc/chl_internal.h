@@ -134,6 +134,10 @@ int write_labels_text_device(const chl_labels *l, const char *path);
 void graph_release_device(chl_graph *g);
 int build_labels(const chl_graph *g, const uint32_t *order, uint32_t n,
                  const chl_build_opts *opts, chl_labels **out);
+// graph class of the tuned-schedule table (chl_tune.cpp)
+std::string graph_class(const chl_graph *g);
+// fill the options left at 0 from the tuned-schedule table; true if found
+bool apply_tuned_schedule(const chl_graph *g, chl_build_opts &opts);
 // build a graph from unique undirected edges (u < v), symmetric CSR
 int graph_from_undirected_unique(uint32_t n, std::vector<uint64_t> &edges_uv,
                                  std::vector<int32_t> &w, chl_graph **out);

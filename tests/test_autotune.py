@@ -17,7 +17,8 @@ def test_search_and_cache(P, tmp_path, monkeypatch):
     from plant_gb300 import autotune as A
     calls = []
 
-    def fake_build(g, order, root_limit=0, first_superstep=0, growth=0.0, sf=0.0, queue_split=0, **kw):
+    def fake_build(g, order, root_limit=0, first_superstep=0, growth=0.0, sf=0.0, queue_split=0, window_target=1,
+                   window_warps=4, **kw):
         calls.append((root_limit, first_superstep, growth, sf, queue_split))
         # minimum at first=1024, growth=2.0, sf=128, queue_split=512
         ms = (100 + abs(first_superstep - 1024) / 10 + abs(growth - 2.0) * 7 + abs(sf - 128) / 50
@@ -29,10 +30,11 @@ def test_search_and_cache(P, tmp_path, monkeypatch):
     order = np.arange(g.get_n(), dtype=np.uint32)
     cache = str(tmp_path / "tune.json")
     cfg = A.tune(g, order, fraction=0.1, min_roots=10, cache=cache)
-    assert cfg == {"first_superstep": 1024, "growth": 2.0, "sf": 128.0, "queue_split": 512}
+    assert cfg == {"first_superstep": 1024, "growth": 2.0, "sf": 128.0, "queue_split": 512, "window_target": 1,
+                   "window_warps": 4}
     assert all(c[0] == max(10, int(0.1 * g.get_n())) for c in calls)
     n_calls = len(calls)
-    assert n_calls <= len(A.FIRST) + len(A.GROWTH) + len(A.SF) + len(A.QSPLIT)
+    assert n_calls <= sum(len(v) for _, v in A.KNOBS)
     data = json.load(open(cache))
     assert A.graph_key(g) in data and data[A.graph_key(g)]["config"] == cfg
     # cached: no further builds
@@ -59,3 +61,42 @@ def test_tuned_build_is_exact(P, tmp_path):
     L = A.tuned_build(g, order, cache=str(tmp_path / "t.json"))
     for x, y in zip(L.export(), ref):
         assert np.array_equal(x, y)
+
+
+def test_table_round_trip(P, tmp_path):
+    """write_table writes the text table the library reads; a class's line
+    is replaced, other lines are kept."""
+    from plant_gb300 import autotune as A
+    path = str(tmp_path / "sched.txt")
+    g = P.Graph.grid(40, 40, seed=2)
+    key = g.graph_class()
+    assert key == A.graph_key(g) and key.startswith("sym-n2^11-deg")
+    A.write_table(path, entries={key: {"first_superstep": 7, "growth": 0.5, "sf": 2.0, "queue_split": 1,
+                                       "window_target": 1, "window_warps": 4}, "dir-n2^3-deg1-skewflat": {
+        "first_superstep": 1, "growth": 1.0, "sf": 1.0, "queue_split": 0, "window_target": 256, "window_warps": 8}})
+    A.write_table(path, entries={key: {"first_superstep": 9, "growth": 0.25, "sf": 4.0, "queue_split": 0,
+                                       "window_target": 1, "window_warps": 4}})
+    lines = [x.split() for x in open(path) if x.strip() and not x.startswith("#")]
+    assert sorted(x[0] for x in lines) == sorted([key, "dir-n2^3-deg1-skewflat"])
+    assert [x for x in lines if x[0] == key][0][1:] == ["9", "0.25", "4.0", "0", "1", "4"]
+
+
+@pytest.mark.gpu
+def test_build_reads_the_table(P, tmp_path, monkeypatch):
+    """With autotune set, options left at 0 come from the table for the
+    graph's class (CHL_SCHEDULES), and the labels stay exact."""
+    from plant_gb300 import autotune as A
+    g = P.Graph.grid(50, 50, seed=6)
+    order = P.Order.degree(g, seed=2)
+    ref = P.build(g, order, autotune=0)
+    path = str(tmp_path / "sched.txt")
+    A.write_table(path, entries={g.graph_class(): {"first_superstep": 1, "growth": 0.01, "sf": 0.5,
+                                                   "queue_split": 1, "window_target": 1, "window_warps": 4}})
+    monkeypatch.setenv("CHL_SCHEDULES", path)
+    L = P.build(g, order)
+    assert L.stats()["supersteps"] > 3 * ref.stats()["supersteps"]
+    for x, y in zip(L.export(), ref.export()):
+        assert np.array_equal(x, y)
+    # explicit options win over the table
+    L2 = P.build(g, order, first_superstep=100000)
+    assert L2.stats()["supersteps"] == 1
