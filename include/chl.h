@@ -168,7 +168,9 @@ typedef struct chl_build_opts {
     int32_t mode;         /* chl_build_mode                                  */
     double sf;            /* superstep label budget factor (hhl -s), 0 = auto
                              (32 on heavy-tailed graphs, 1024 otherwise)  */
-    double ps;            /* phase switch ratio tree/label (hhl -ps)          */
+    double ps;            /* phase switch ratio tree/label (hhl -ps), 0 =
+                             auto: 1024 (the reference's default) on road-
+                             like graphs, 8 on heavy-tailed ones          */
     int32_t autotune;     /* 1: schedule options left at 0 come from the
                              tuned-schedule table for the graph's class
                              (chl_graph_class; $CHL_SCHEDULES or
@@ -199,13 +201,14 @@ typedef struct chl_build_opts {
     uint32_t window_target; /* trees of a superstep with no committed labels
                              (the first) are searched label-correcting in
                              distance windows of about this many vertices:
-                             0 auto (off), 1 off (batched settle rounds)    */
-    uint32_t window_warps; /* warps building one such tree: 0 auto (4), 1, 2,
-                             4 or 8                                         */
+                             0 auto (1024 on heavy-tailed graphs, off on
+                             road-like ones), 1 off (batched settle rounds) */
+    uint32_t window_warps; /* warps building one such tree: 0 auto (8 on
+                             heavy-tailed graphs, else 4), 1, 2, 4 or 8     */
     uint32_t reserved[1];
 } chl_build_opts;
 
-/* Fill opts with the defaults (hybrid, sf auto, ps 1024, autotune on,
+/* Fill opts with the defaults (hybrid, sf auto, ps auto, autotune on,
  * commit chain captured in a CUDA graph). */
 void chl_build_opts_default(chl_build_opts *opts);
 

@@ -443,7 +443,7 @@ class Labeling:
             self._h = None
 
 
-def build(g: Graph, order, mode: int = MODE_HYBRID, sf: float = 0.0, ps: float = 1024.0,
+def build(g: Graph, order, mode: int = MODE_HYBRID, sf: float = 0.0, ps: float = 0.0,
           verbose: int = 0, max_warps: int = 0, autotune: int = 1,
           first_superstep: int = 0, growth: float = 0.0,
           use_graphs: Optional[int] = None, root_limit: int = 0,

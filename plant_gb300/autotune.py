@@ -1,10 +1,10 @@
 """Schedule autotuner for the label build.
 
-The build's speed depends on six schedule knobs: the roots in the first
+The build's speed depends on seven schedule knobs: the roots in the first
 superstep, the superstep growth factor, the label budget per superstep, the
-queue size at which a tree's queue is split into near and far parts, and the
+queue size at which a tree's queue is split into near and far parts, the
 window size and warps per tree of the first superstep's label-correcting
-trees.  The labels never depend on them (canonical labels are unique for an
+trees, and the PLaNT-to-GLL phase switch ratio.  The labels never depend on them (canonical labels are unique for an
 order), and the labels of the hubs of rank < R are final once the roots below
 R are processed, so every candidate is timed on the same exact work: a prefix
 build of the roots of rank < R (``root_limit``; the whole build when
@@ -38,10 +38,11 @@ FIRST = (0, 256, 1024, 4096)      # 0: the built-in choice from graph statistics
 GROWTH = (0.0, 0.5, 1.0, 2.0)     # 0.0: built-in
 SF = (0.0, 32.0, 128.0, 1024.0)   # label budget per superstep (x n); 0.0: built-in
 QSPLIT = (0, 1, 512, 4096)        # near/far queue split size; 0: built-in, 1: off
-WTARGET = (1, 256, 1024, 4096)    # first-superstep window size; 1: settle rounds
-WWARPS = (4, 8)                   # warps per first-superstep tree
+WTARGET = (0, 1, 256, 1024, 4096) # first-superstep window size; 0: built-in, 1: settle rounds
+WWARPS = (0, 4, 8)                # warps per first-superstep tree; 0: built-in
+PS = (0.0, 8.0, 64.0, 1024.0)     # hybrid phase switch ratio; 0.0: built-in
 KNOBS = (("first_superstep", FIRST), ("growth", GROWTH), ("sf", SF), ("queue_split", QSPLIT),
-         ("window_target", WTARGET), ("window_warps", WWARPS))
+         ("window_target", WTARGET), ("window_warps", WWARPS), ("ps", PS))
 SHIPPED = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuned_schedules.txt")
 
 
@@ -91,7 +92,8 @@ def tune(g: Graph, order, fraction: float = 0.02, min_roots: int = 4096, repeats
                 log(f"autotune {key} {cfg}: {best:.1f} ms for roots < {R}")
         return timings[k]
 
-    cfg = {"first_superstep": 0, "growth": 0.0, "sf": 0.0, "queue_split": 0, "window_target": 1, "window_warps": 4}
+    cfg = {"first_superstep": 0, "growth": 0.0, "sf": 0.0, "queue_split": 0, "window_target": 0, "window_warps": 0,
+           "ps": 0.0}
     t0 = time.perf_counter()
     for knob, values in KNOBS:
         best_v = min(values, key=lambda v: cost({**cfg, knob: v}))
@@ -113,9 +115,10 @@ def tuned_build(g: Graph, order, cache: str | None = DEFAULT_CACHE, log=None, **
 
 def table_line(key: str, cfg: dict) -> str:
     """One line of the library's tuned-schedule table."""
-    return "{} {} {} {} {} {} {}".format(key, int(cfg["first_superstep"]), float(cfg["growth"]), float(cfg["sf"]),
-                                         int(cfg["queue_split"]), int(cfg.get("window_target", 1)),
-                                         int(cfg.get("window_warps", 4)))
+    return "{} {} {} {} {} {} {} {}".format(key, int(cfg["first_superstep"]), float(cfg["growth"]),
+                                            float(cfg["sf"]), int(cfg["queue_split"]),
+                                            int(cfg.get("window_target", 0)), int(cfg.get("window_warps", 0)),
+                                            float(cfg.get("ps", 0.0)))
 
 
 def write_table(path: str = SHIPPED, cache: str | None = DEFAULT_CACHE, entries: dict | None = None) -> None:
@@ -131,7 +134,7 @@ def write_table(path: str = SHIPPED, cache: str | None = DEFAULT_CACHE, entries:
                 if k is None or k not in new:
                     lines.append(line.rstrip("\n"))
     except OSError:
-        lines = ["# graph-class first_superstep growth sf queue_split window_target window_warps",
+        lines = ["# graph-class first_superstep growth sf queue_split window_target window_warps ps",
                  "# written by plant_gb300/autotune.py (write_table); read by chl_build when autotune is set"]
     lines += [table_line(k, c) for k, c in sorted(new.items())]
     tmp = path + ".tmp"

@@ -1862,6 +1862,16 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     if ((rc = grow_new(b, opts.label_cap ? (uint64_t)opts.label_cap : std::max<uint64_t>(4ull * n, 1u << 20))))
         return rc;
 
+    // heavy-tailed degree distribution: the largest out-degree above 32
+    // times the mean (scale-free graphs); bounded-degree (road-like)
+    // otherwise.  Several schedule defaults below depend on it.
+    bool heavy_tail = false;
+    {
+        uint64_t maxdeg = 0;
+        for (uint32_t v = 0; v < n; ++v) maxdeg = std::max<uint64_t>(maxdeg, g->off[1][v + 1] - g->off[1][v]);
+        const double avgdeg = n ? (double)g->off[1][n] / n : 0.0;
+        heavy_tail = maxdeg > 32.0 * std::max(1.0, avgdeg);
+    }
     // workspace: one slot per resident warp
     const int sms = device_sms();
     const bool unit = g->unit;
@@ -1907,9 +1917,10 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         &nbo, unit ? batch_kernel<true, true> : batch_kernel<false, true>, kWarpsPerBlock * 32, 0));
     nbo = std::max(nbo, 1);
     b.slots = std::min(b.warps, (uint32_t)nbo * (uint32_t)sms * kWarpsPerBlock);
-    // window kernel (first superstep): one tree per block of win_tw warps,
-    // as many trees as are resident, 6 n words each
-    b.win_tw = opts.window_warps ? opts.window_warps : 4;
+    // window kernel (first superstep): one tree per block of win_tw warps
+    // (auto: 8 on heavy-tailed graphs, 4 otherwise), as many trees as are
+    // resident, 6 n words each
+    b.win_tw = opts.window_warps ? opts.window_warps : (heavy_tail ? 8 : 4);
     if (b.win_tw != 1 && b.win_tw != 2 && b.win_tw != 4 && b.win_tw != 8) {
         set_error("window_warps must be 0, 1, 2, 4 or 8");
         return CHL_ERR_INVALID;
@@ -1946,21 +1957,11 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     // 512/1024-square grids): heavy-tailed degree distributions start with
     // 1024 roots and double, so the hubs commit before the bulk of the trees
     // while the early supersteps still fill the GPU; bounded-degree
-    // (road-like) graphs start with one root per resident warp and grow by
-    // half of the committed prefix.
-    uint32_t auto_first;
-    double auto_growth;
-    bool heavy_tail = false;
-    {
-        uint64_t arcs_out = g->off[1][n];
-        uint64_t maxdeg = 0;
-        for (uint32_t v = 0; v < n; ++v) maxdeg = std::max<uint64_t>(maxdeg, g->off[1][v + 1] - g->off[1][v]);
-        const double avgdeg = n ? (double)arcs_out / n : 0.0;
-        const bool heavy = maxdeg > 32.0 * std::max(1.0, avgdeg);
-        auto_first = heavy ? 1024u : std::max<uint32_t>(64u, b.warps);
-        auto_growth = heavy ? 2.0 : 0.5;
-        heavy_tail = heavy;
-    }
+    // (road-like) graphs start with two roots per warp of the schedule (the
+    // 1024-square grid: 1.15x faster than one) and grow by half of the
+    // committed prefix.
+    const uint32_t auto_first = heavy_tail ? 1024u : std::max<uint32_t>(64u, 2 * b.warps);
+    const double auto_growth = heavy_tail ? 2.0 : 0.5;
     // superstep loop
     // label budget per superstep (the reference's sf * N); auto: 32 on
     // heavy-tailed graphs, 1024 on road-like ones.  On road-like graphs a
@@ -2004,8 +2005,16 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     // The label budget sf * n (the reference's label_limit) also ends a
     // superstep early.
     // label-correcting windows of the first superstep's trees: about this
-    // many vertices per window (1: IN-criterion rounds instead)
-    const uint32_t win_target = opts.window_target ? opts.window_target : 1u;
+    // many vertices per window (1: IN-criterion rounds instead).  Auto: on
+    // heavy-tailed graphs, whose first trees are huge BFS-like searches
+    // (RMAT scale 20: 1.4x faster builds with 8 warps per tree); off on
+    // road-like ones, where the windows' coarser PLaNT exit overstates the
+    // tree/label ratio and moves the hybrid switch
+    const uint32_t win_target = opts.window_target ? opts.window_target : (heavy_tail ? 1024u : 1u);
+    // phase switch ratio (the reference's -ps, default 1024): auto 8 on
+    // heavy-tailed graphs (RMAT scale 20: pruned GLL supersteps after the
+    // first are faster than PLaNT trees there)
+    const double ps = opts.ps > 0 ? opts.ps : (heavy_tail ? 8.0 : 1024.0);
     const uint32_t first = opts.first_superstep ? opts.first_superstep : auto_first;
     const double growth = opts.growth > 0 ? opts.growth : auto_growth;
     while (r0 < n && (opts.root_limit == 0 || r0 < opts.root_limit)) {
@@ -2017,6 +2026,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         if (opts.root_limit) r_end = std::min<uint32_t>(r_end, opts.root_limit);
         BuildCtl hc;
         bool rerun = false;
+        uint32_t step_reruns = 0;
         // root hash table: a power of two at least twice the longest committed
         // list, within the occupancy-preserving size (entries beyond half the
         // table are searched in the global list)
@@ -2125,6 +2135,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
                 return CHL_ERR_INVALID;
             }
             if (hc.overflow || hc.nlab > b.new_cap) {
+                ++step_reruns;
                 // re-run the same root range with room for every label
                 if ((rc = grow_new(b, hc.nlab + hc.nlab / 4 + 1024))) return rc;
                 r_end = r1;
@@ -2151,7 +2162,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             CHL_CUDA(cudaStreamSynchronize(b.st));
             double ratio;
             std::memcpy(&ratio, &bits, 8);
-            if (ratio > opts.ps) {
+            if (ratio > ps) {
                 do_plant = false;
                 switch_open = false;
             }
@@ -2301,12 +2312,12 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
                     (double)tstat[1] / std::max<uint32_t>(1, r1 - r_begin));
         if (opts.verbose >= 2)
             fprintf(stderr,
-                    "superstep %u: roots [%u,%u) %s tree_ms %.2f labels %llu visits %llu reads %llu arcs %llu "
-                    "committed %llu max_list %u\n",
+                    "superstep %u: roots [%u,%u) %s tree_ms %.2f commit_ms %.2f labels %llu visits %llu reads %llu "
+                    "arcs %llu committed %llu max_list %u label_cap %llu reruns %u\n",
                     supersteps, r_begin, r1, plant_now ? "plant" : "gll",
-                    step_tree_ms, (unsigned long long)M, (unsigned long long)hc.visits,
+                    step_tree_ms, ms1, (unsigned long long)M, (unsigned long long)hc.visits,
                     (unsigned long long)hc.label_reads, (unsigned long long)hc.arcs, (unsigned long long)committed,
-                    max_list);
+                    max_list, (unsigned long long)b.new_cap, step_reruns);
     }
     CHL_CUDA(cudaEventRecord(ev1, b.st));
     CHL_CUDA(cudaStreamSynchronize(b.st));
@@ -2357,7 +2368,7 @@ extern "C" void chl_build_opts_default(chl_build_opts *o) {
     std::memset(o, 0, sizeof(*o));
     o->mode = CHL_MODE_HYBRID;
     o->sf = 0.0;
-    o->ps = 1024.0;
+    o->ps = 0.0;
     o->autotune = 1;
     o->use_graphs = 1;
     o->verbose = 0;

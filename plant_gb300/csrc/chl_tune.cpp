@@ -3,7 +3,7 @@
 //
 // plant_gb300/autotune.py times candidate schedules on the GPU and writes the
 // winners as a table, one graph class per line:
-//     <class> first_superstep growth sf queue_split window_target window_warps
+//     <class> first_superstep growth sf queue_split window_target window_warps ps
 // A build with opts.autotune set takes, for every schedule option it leaves
 // at 0 (auto), the value of its graph's class from that table: the file named
 // by $CHL_SCHEDULES, else tuned_schedules.txt next to this library.  The
@@ -58,9 +58,10 @@ bool apply_tuned_schedule(const chl_graph *g, chl_build_opts &o) {
     while (!found && fgets(line, sizeof(line), f)) {
         if (line[0] == '#') continue;
         unsigned first = 0, wt = 0, ww = 0;
-        double growth = 0, sf = 0;
+        double growth = 0, sf = 0, ps = 0;
         int qs = 0;
-        if (sscanf(line, "%127s %u %lf %lf %d %u %u", name, &first, &growth, &sf, &qs, &wt, &ww) != 7) continue;
+        if (sscanf(line, "%127s %u %lf %lf %d %u %u %lf", name, &first, &growth, &sf, &qs, &wt, &ww, &ps) != 8)
+            continue;
         if (cls != name) continue;
         found = true;
         if (!o.first_superstep) o.first_superstep = first;
@@ -69,6 +70,7 @@ bool apply_tuned_schedule(const chl_graph *g, chl_build_opts &o) {
         if (!o.queue_split) o.queue_split = qs;
         if (!o.window_target) o.window_target = wt;
         if (!o.window_warps) o.window_warps = ww;
+        if (o.ps <= 0) o.ps = ps;
     }
     fclose(f);
     return found;

@@ -17,8 +17,8 @@ def test_search_and_cache(P, tmp_path, monkeypatch):
     from plant_gb300 import autotune as A
     calls = []
 
-    def fake_build(g, order, root_limit=0, first_superstep=0, growth=0.0, sf=0.0, queue_split=0, window_target=1,
-                   window_warps=4, **kw):
+    def fake_build(g, order, root_limit=0, first_superstep=0, growth=0.0, sf=0.0, queue_split=0, window_target=0,
+                   window_warps=0, ps=0.0, **kw):
         calls.append((root_limit, first_superstep, growth, sf, queue_split))
         # minimum at first=1024, growth=2.0, sf=128, queue_split=512
         ms = (100 + abs(first_superstep - 1024) / 10 + abs(growth - 2.0) * 7 + abs(sf - 128) / 50
@@ -30,8 +30,8 @@ def test_search_and_cache(P, tmp_path, monkeypatch):
     order = np.arange(g.get_n(), dtype=np.uint32)
     cache = str(tmp_path / "tune.json")
     cfg = A.tune(g, order, fraction=0.1, min_roots=10, cache=cache)
-    assert cfg == {"first_superstep": 1024, "growth": 2.0, "sf": 128.0, "queue_split": 512, "window_target": 1,
-                   "window_warps": 4}
+    assert cfg == {"first_superstep": 1024, "growth": 2.0, "sf": 128.0, "queue_split": 512, "window_target": 0,
+                   "window_warps": 0, "ps": 0.0}
     assert all(c[0] == max(10, int(0.1 * g.get_n())) for c in calls)
     n_calls = len(calls)
     assert n_calls <= sum(len(v) for _, v in A.KNOBS)
@@ -78,7 +78,7 @@ def test_table_round_trip(P, tmp_path):
                                        "window_target": 1, "window_warps": 4}})
     lines = [x.split() for x in open(path) if x.strip() and not x.startswith("#")]
     assert sorted(x[0] for x in lines) == sorted([key, "dir-n2^3-deg1-skewflat"])
-    assert [x for x in lines if x[0] == key][0][1:] == ["9", "0.25", "4.0", "0", "1", "4"]
+    assert [x for x in lines if x[0] == key][0][1:] == ["9", "0.25", "4.0", "0", "1", "4", "0.0"]
 
 
 @pytest.mark.gpu
