@@ -342,6 +342,24 @@ def build_work_bytes(L, g):
     return tot
 
 
+def schedule_used(g):
+    """The tuned-schedule table line chl_build applies to g (autotune on), or
+    the built-in defaults when the table has no line for g's class."""
+    cls = g.graph_class()
+    path = os.environ.get("CHL_SCHEDULES") or os.path.join(ROOT, "plant_gb300", "tuned_schedules.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                t = line.split()
+                if t and not line.startswith("#") and t[0] == cls:
+                    keys = ("first_superstep", "growth", "sf", "queue_split", "window_target", "window_warps", "ps")
+                    return {"class": cls, "source": os.path.basename(path),
+                            "table": dict(zip(keys, (float(x) for x in t[1:])))}
+    except OSError:
+        pass
+    return {"class": cls, "source": "built-in defaults"}
+
+
 def reference_digests():
     """Digests of the reference's own labels on the benchmark workloads
     (tests/golden/scale_digests.json, written by
@@ -375,7 +393,7 @@ def rmat_leg(P, args, serve_seconds):
     n = g.get_n()
     g.to_device()
     out = {"workload": "rmat20 ef16 (0.57,0.19,0.19,0.05), degree order, full build", "vertices": n,
-           "arcs": int(g.out_arcs())}
+           "arcs": int(g.out_arcs()), "schedule": schedule_used(g)}
     for name, mode in (("hybrid", P.MODE_HYBRID), ("gll", P.MODE_GLL)):
         P.build(g, order, mode=mode)
         st = []
@@ -619,6 +637,7 @@ def run_ours(args, ws, rank):
                   "hot_achieved_gbs": qh_bytes / (qh_ms / 1e3) / 1e9},
     }
     line["parity"] = parity(L, reference_key(args))
+    line["schedule"] = schedule_used(g)
     if rank == 0 and args.workload == "grid" and not args.no_rmat:
         line["rmat20"] = rmat_leg(P, args, args.serve_seconds)
     if rank == 0 and not args.no_cpu:

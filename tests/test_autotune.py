@@ -98,5 +98,19 @@ def test_build_reads_the_table(P, tmp_path, monkeypatch):
     for x, y in zip(L.export(), ref.export()):
         assert np.array_equal(x, y)
     # explicit options win over the table
-    L2 = P.build(g, order, first_superstep=100000)
+    L2 = P.build(g, order, first_superstep=100000, sf=1e6)
     assert L2.stats()["supersteps"] == 1
+
+
+def test_shipped_table_is_well_formed():
+    """The table shipped beside the library: one line per graph class with
+    the seven schedule values chl_build reads."""
+    import os
+    import re
+    from plant_gb300 import autotune as A
+    rows = [x.split() for x in open(A.SHIPPED) if x.strip() and not x.startswith("#")]
+    assert rows
+    for r in rows:
+        assert re.fullmatch(r"(sym|dir)-n2\^\d+-deg\d+-skew(heavy|flat)", r[0]) and len(r) == 8
+        float(r[2]), float(r[3]), float(r[7])
+        assert all(x.isdigit() for x in (r[1], r[4], r[5], r[6]))
