@@ -526,7 +526,8 @@ def run_reference(args, ws, rank):
                                         f"{len(ends)}) of the GLL restatement (run_paraPLL, sf 32) replayed from "
                                         "their committed state; Horvitz-Thompson estimate of the whole build")},
             "full_build": {"seconds": full_secs, "labels": labels, "labels_per_s": labels / full_secs,
-                           "supersteps": int(len(ends)), "estimate_over_full": float(np.mean(ests)) / full_secs},
+                           "supersteps": int(len(ends)), "estimate_over_full": float(np.mean(ests)) / full_secs,
+                           "step_estimates_over_full": [round(x / full_secs, 3) for x in ests]},
             "setup_s": {"workload": round(t_gen, 1), "full_build": round(full_secs, 1)},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

