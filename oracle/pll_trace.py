@@ -10,8 +10,9 @@ workload and committed as profiles/pll_trace_<workload>.json, which bench.py
 reads.
 
 Test infrastructure: this runs the oracle (single-threaded C), never the GPU
-engine.  The graph and the order are bench.py's own workload (the order from
-the oracle's degree / betweenness restatement, identical to the GPU's).
+engine.  The graph and the order are bench.py's own workload, built by the
+oracle's restatements of the package's seeded generators and of the degree /
+betweenness orders (identical graphs and orders, checked by digest).
 
     python oracle/pll_trace.py                           # 1024x1024 grid
     python oracle/pll_trace.py --workload rmat --scale 20
@@ -43,16 +44,14 @@ def main():
     args = ap.parse_args()
 
     import bench
-    import plant_gb300 as P
     from oracle import oracle as O
 
-    g, order = bench.make_workload(P, args, cpu_order=True)
-    off, head, ln = g.csr(True)
-    og = O.OGraph.from_csr(g.get_n(), off, head, ln)
+    og, order = bench.oracle_workload(O, args)
+    _, head, _ = og.csr(True)
     t0 = time.time()
     tr = O.pll_trace(og, order)
     secs = time.time() - t0
-    out = {"workload": bench.workload_name(args), "vertices": g.get_n(), "graph_arcs": int(len(head)),
+    out = {"workload": bench.workload_name(args), "vertices": og.n, "graph_arcs": int(len(head)),
            "trace_seconds": round(secs, 1), **tr,
            "command": "python oracle/pll_trace.py " + " ".join(sys.argv[1:])}
     path = args.out or os.path.join(ROOT, "profiles", "pll_trace_" + bench.workload_slug(args) + ".json")

@@ -151,7 +151,7 @@ constexpr int kBatch = CHL_KBATCH;   // settled vertices buffered per warp (<= 2
 constexpr int kEmit = 64;   // labels staged per warp before an append
 
 __host__ __device__ constexpr size_t batch_smem_per_warp(uint32_t hash_slots) {
-    return ((size_t)8 * kBatch + (size_t)8 * hash_slots + (size_t)4 * (7 * kBatch + 1 + 32) + 8 +
+    return ((size_t)8 * kBatch + (size_t)8 * hash_slots + (size_t)4 * (8 * kBatch + 1) + 8 +
             (size_t)12 * kEmit + 15) &
            ~(size_t)15;
 }
@@ -249,8 +249,8 @@ batch_kernel(TreeArgs a) {
     uint32_t *s_tl = s_bx + kBatch + 1;                // batch indices still to test
     uint32_t *s_bl = s_tl + kBatch;                    // label list length
     uint32_t *s_nch = s_bl + kBatch;                   // label list chunks
-    uint32_t *s_as = s_nch + kBatch;                   // items of the step (up to 32)
-    uint64_t *s_ek = (uint64_t *)(((uintptr_t)(s_as + 32) + 7) & ~(uintptr_t)7);   // staged label keys
+    uint32_t *s_as = s_nch + kBatch;                   // next chunk to test, per batch vertex
+    uint64_t *s_ek = (uint64_t *)(((uintptr_t)(s_as + kBatch) + 7) & ~(uintptr_t)7);   // staged label keys
     uint32_t *s_ev = (uint32_t *)(s_ek + kEmit);       // staged label distances
 
     uint32_t *key = a.ws_key + (size_t)slot * a.n;
@@ -428,99 +428,86 @@ batch_kernel(TreeArgs a) {
                 long long tc1 = phase_clock();
                 cyc[1] += tc1 - tc0;
                 if (R > 0) {
-                    // Prune tests flattened to (vertex, 16-entry chunk) items,
-                    // chunk-major (chunk 0 of every vertex, then chunk 1, ...),
-                    // one item per lane and step: a round costs about (total
-                    // chunks) / 32 steps instead of the longest list's chunks,
-                    // and an item of a vertex that already has a witness, or
-                    // whose list has passed d(r, u), is skipped.
-                    uint32_t ntest = 0, maxnch = 0;
+                    // Prune tests as (vertex, 16-entry chunk) items, one per
+                    // lane and step.  The vertices still under test wait in a
+                    // circular queue (s_tl, kBatch entries): a step takes up
+                    // to 32 from its front -- with fewer than 32, each gets
+                    // several consecutive chunks -- and puts back at the end
+                    // those with no witness yet whose list has not passed
+                    // d(r, u).  Each vertex gets about one chunk per trip
+                    // through the queue (chunk-major order), and no step
+                    // looks at a vertex that is already decided.
+                    uint32_t nq = 0;
                     for (uint32_t j0 = 0; j0 < nb; j0 += 32) {
                         const uint32_t j = j0 + lane;
                         const bool t = j < nb && s_bp[j] == 0;
                         const uint32_t m = __ballot_sync(kFull, t);
-                        uint32_t nch = 0;
                         if (t) {
-                            s_tl[ntest + __popc(m & lanemask_lt())] = j;
+                            s_tl[nq + __popc(m & lanemask_lt())] = j;
                             const uint32_t xu = lidx(s_bv[j], 1 - f, a.sides);
                             const uint64_t lb = a.l_off[xu], le = a.l_off[xu + 1];
                             s_ba[j] = lb;
                             s_bl[j] = (uint32_t)(le - lb);
-                            nch = (uint32_t)((le - (lb & ~1ull) + 15) >> 4);
-                            s_nch[j] = nch;
+                            s_nch[j] = (uint32_t)((le - (lb & ~1ull) + 15) >> 4);
+                            s_as[j] = 0;   // next chunk to test
                         }
-                        maxnch = max(maxnch, __reduce_max_sync(kFull, nch));
-                        ntest += __popc(m);
+                        nq += __popc(m);
                     }
                     __syncwarp();
-                    const uint32_t nitems = ntest * maxnch;
-                    // i / ntest as a multiply by ceil(2^32 / ntest): exact for
-                    // i < ntest * maxnch when maxnch * ntest^2 < 2^32
-                    const uint64_t inv = ((1ull << 32) + ntest - 1) / max(ntest, 1u);
-                    const bool mul_div = (uint64_t)maxnch * ntest * ntest < (1ull << 32);
-                    uint32_t cursor = 0, nread = 0;
-                    while (true) {
-                        // the next (up to) 32 live items, in item order
-                        uint32_t got = 0;
+                    uint32_t qh = 0, nread = 0;
+                    while (nq > 0) {
                         const long long tsel = phase_clock();
-                        while (got < 32 && cursor < nitems) {
-                            if (kPhaseTiming) cyc[9]++;
-                            const uint32_t i = cursor + lane;
-                            bool live = false;
-                            uint32_t item = 0;
-                            if (i < nitems) {
-                                const uint32_t c = mul_div ? (uint32_t)(((uint64_t)i * inv) >> 32) : i / ntest;
-                                const uint32_t j = s_tl[i - c * ntest];
-                                live = s_bp[j] == 0 && c < s_nch[j];
-                                item = (c << 8) | j;
-                            }
-                            const uint32_t lm = __ballot_sync(kFull, live);
-                            const uint32_t nl = (uint32_t)__popc(lm);
-                            const uint32_t take = min(32u - got, nl);
-                            const uint32_t rk = __popc(lm & lanemask_lt());
-                            if (live && rk < take) s_as[got + rk] = item;
-                            if (take < nl) {
-                                // continue just after the last item taken
-                                const uint32_t lastm = __ballot_sync(kFull, live && rk + 1 == take);
-                                cursor += (uint32_t)__ffs(lastm);
-                            } else {
-                                cursor += 32;
-                            }
-                            got += take;
-                        }
-                        __syncwarp();
+                        if (kPhaseTiming) cyc[9]++;
+                        const uint32_t t = min(nq, 32u);
+                        // lane -> (vertex of the queue front, chunk)
+                        const uint32_t vi = lane % t;
+                        const uint32_t lj = s_tl[(qh + vi) % (uint32_t)kBatch];
+                        const uint32_t c = s_as[lj] + lane / t;
+                        const bool act = c < s_nch[lj];
                         cyc[8] += phase_clock() - tsel;
-                        if (got == 0) break;
                         // one 16-entry item per lane (8 loads of one 128-byte
                         // line in flight per lane)
                         bool hit = false, exhausted = false;
-                        uint32_t lj = 0;
-                        if (lane < got) {
-                            const uint32_t item = s_as[lane];
-                            lj = item & 0xFFu;
-                            const uint32_t c = item >> 8;
+                        if (act) {
                             const uint64_t glb = s_ba[lj];
                             const uint64_t gle = glb + s_bl[lj];
                             const uint32_t gdj = s_bk[lj] >> 1;
                             const uint64_t e0 = (glb & ~1ull) + 16ull * c;
                             // entries [lo, hi) of the 16 belong to the list: lo
-                            // is 1 only in chunk 0 of an odd start, and a live
-                            // item has e0 < gle
+                            // is 1 only in chunk 0 of an odd start, and an
+                            // active item has e0 < gle
                             const uint32_t lo = (uint32_t)(glb - min(glb, e0));
                             const uint64_t span = gle - e0;
                             const uint32_t hi = span < 16 ? (uint32_t)span : 16u;
                             const uint32_t vm = ((1u << hi) - 1u) & ~((1u << lo) - 1u);
                             uint4 q[8];
 #pragma unroll
-                            for (int t = 0; t < 8; ++t) {
-                                q[t] = make_uint4(0, 0, 0, 0);
-                                if ((vm >> (2 * t)) & 3u) q[t] = *(const uint4 *)(lscan + e0 + 2 * t);
+                            for (int u = 0; u < 8; ++u) {
+                                q[u] = make_uint4(0, 0, 0, 0);
+                                if ((vm >> (2 * u)) & 3u) q[u] = *(const uint4 *)(lscan + e0 + 2 * u);
                             }
                             hit = test16d(q, vm, gdj, exhausted);
                             nread += 16;
                         }
                         if (hit) s_bp[lj] = 1;
                         else if (exhausted) atomicOr(&s_bp[lj], 2u);
+                        __syncwarp();
+                        // the front t vertices leave the queue; those still
+                        // undecided with chunks left go back at the end
+                        bool back = false;
+                        uint32_t bj = 0;
+                        if (lane < t) {
+                            bj = lj;   // vi == lane here
+                            const uint32_t taken = 32u / t + (lane < 32u % t ? 1u : 0u);
+                            const uint32_t nc = s_as[bj] + taken;
+                            s_as[bj] = nc;
+                            back = s_bp[bj] == 0 && nc < s_nch[bj];
+                        }
+                        const uint32_t bm = __ballot_sync(kFull, back);
+                        qh = (qh + t) % (uint32_t)kBatch;
+                        nq -= t;
+                        if (back) s_tl[(qh + nq + __popc(bm & lanemask_lt())) % (uint32_t)kBatch] = bj;
+                        nq += __popc(bm);
                         __syncwarp();
                     }
                     c_reads += nread;
