@@ -68,6 +68,8 @@ struct BuildCtl {
     unsigned long long n_keep;      // labels surviving the clean pass
     unsigned int overflow;
     unsigned int err;               // 1: distance overflow, 2: workspace bound
+    unsigned int max_dist;          // largest distance of a label emitted this superstep
+    unsigned int reserved_;
     unsigned long long max_ratio_num;  // (tree, labels) of the worst root
     unsigned long long max_ratio_den;
     unsigned long long running;     // trees of the nominal root range in progress
@@ -270,6 +272,7 @@ batch_kernel(TreeArgs a) {
     // label arrays kEmit at a time (one atomic per flush instead of one
     // per settle round)
     uint32_t n_emit = 0;
+    uint32_t d_hi = 0;   // largest distance this lane has written
     auto flush_labels = [&]() {
         __syncwarp();
         if (n_emit) {
@@ -278,6 +281,7 @@ batch_kernel(TreeArgs a) {
             b = __shfl_sync(kFull, b, 0);
             for (uint32_t k = lane; k < n_emit; k += 32) {
                 const unsigned long long p = b + k;
+                d_hi = max(d_hi, s_ev[k]);
                 if (p < a.out_cap) {
                     a.out_key[p] = s_ek[k];
                     a.out_val[p] = s_ev[k];
@@ -856,9 +860,11 @@ batch_kernel(TreeArgs a) {
             finish_root(a, r_nominal);
         }
     }
+    d_hi = __reduce_max_sync(kFull, d_hi);
     if (lane == 0) {
         atomicAdd(&a.ctl->visits, c_vis);
         atomicAdd(&a.ctl->arcs, c_arcs);
+        if (d_hi) atomicMax(&a.ctl->max_dist, d_hi);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) c_reads += __shfl_xor_sync(kFull, c_reads, o);
@@ -914,6 +920,7 @@ struct WinShared {
     uint32_t changed;
     uint32_t psel;      // which pile buffer is current
     int ql;             // queued not-via keys (PLaNT)
+    uint32_t dnv;       // largest distance of a not-via member so far (PLaNT)
     uint32_t t_size, t_lab;
     uint32_t err;
 };
@@ -948,6 +955,7 @@ window_kernel(TreeArgs a) {
     unsigned long long c_vis = 0, c_arcs = 0;
 
     uint32_t n_emit = 0;
+    uint32_t d_hi = 0;   // largest distance this lane has written
     auto flush_labels = [&]() {
         __syncwarp();
         if (n_emit) {
@@ -956,6 +964,7 @@ window_kernel(TreeArgs a) {
             b = __shfl_sync(kFull, b, 0);
             for (uint32_t k = lane; k < n_emit; k += 32) {
                 const unsigned long long p = b + k;
+                d_hi = max(d_hi, s_ev[k]);
                 if (p < a.out_cap) {
                     a.out_key[p] = s_ek[k];
                     a.out_val[p] = s_ev[k];
@@ -1007,6 +1016,7 @@ window_kernel(TreeArgs a) {
                 sh.lo = kInf;
                 sh.psel = 0;
                 sh.ql = 1;
+                sh.dnv = 0;
                 sh.err = 0;
             }
             __syncthreads();
@@ -1172,7 +1182,7 @@ window_kernel(TreeArgs a) {
                 // the window is final: its labels, from the final keys
                 const uint32_t nm = sh.nm;
                 int nv_final = 0;
-                uint32_t lab = 0;
+                uint32_t lab = 0, dnv = 0;
                 for (uint32_t b0 = wib * 32; b0 < nm; b0 += 32 * TW) {
                     const uint32_t i = b0 + lane;
                     bool emit = false;
@@ -1183,6 +1193,7 @@ window_kernel(TreeArgs a) {
                         if (PLANT) {
                             nv_final += (int)(k & 1u);
                             emit = (k & 1u) != 0;
+                            if (emit) dnv = max(dnv, k >> 1);
                         } else {
                             emit = __ldg(&a.rank[x]) >= r;   // iteration_gll :92
                         }
@@ -1199,11 +1210,15 @@ window_kernel(TreeArgs a) {
                         lab += __popc(em);
                     }
                 }
-                if (PLANT) nv_final = __reduce_add_sync(kFull, nv_final);
+                if (PLANT) {
+                    nv_final = __reduce_add_sync(kFull, nv_final);
+                    dnv = __reduce_max_sync(kFull, dnv);
+                }
                 const uint32_t pmin_w = __reduce_min_sync(kFull, pmin);
                 pmin = kInf;
                 if (lane == 0) {
                     if (PLANT && nv_final) atomicAdd(&sh.ql, -nv_final);
+                    if (PLANT && dnv) atomicMax(&sh.dnv, dnv);
                     if (lab) atomicAdd(&sh.t_lab, lab);
                     if (pmin_w != kInf) atomicMin(&sh.lo, pmin_w);
                 }
@@ -1300,9 +1315,20 @@ window_kernel(TreeArgs a) {
             }
             __syncthreads();
             if (sh.err && tid == 0) a.ctl->err = 2;
+            if (PLANT && sh.nm) {
+                // the early exit ended the tree inside this window: count its
+                // members no farther than the last not-via vertex, the ones
+                // the reference's Dijkstra pops before it stops
+                // (distributed_memory/akiba.hpp:69-95)
+                const uint32_t nm = min(sh.nm, a.n), dl = sh.dnv;
+                uint32_t c = 0;
+                for (uint32_t i = tid; i < nm; i += 32 * TW) c += (__ldcg(&key[memb[i]]) >> 1) <= dl ? 1u : 0u;
+                c = __reduce_add_sync(kFull, c);
+                if (lane == 0 && c) atomicAdd(&sh.t_size, c);
+            }
+            __syncthreads();
             const uint32_t nvis = min(sh.nvis, a.n);
             for (uint32_t k = tid; k < nvis; k += 32 * TW) __stcg(&key[vis[k]], kInf);
-            if (tid == 0) sh.t_size += sh.nm;   // the last window's members, when the early exit ended the tree
             __syncthreads();
         }
         flush_labels();
@@ -1314,9 +1340,11 @@ window_kernel(TreeArgs a) {
         }
         __syncthreads();
     }
+    d_hi = __reduce_max_sync(kFull, d_hi);
     if (lane == 0) {
         atomicAdd(&a.ctl->visits, c_vis);
         atomicAdd(&a.ctl->arcs, c_arcs);
+        if (d_hi) atomicMax(&a.ctl->max_dist, d_hi);
     }
 }
 
@@ -1473,26 +1501,29 @@ __device__ __forceinline__ bool ent_less(uint2 a, uint2 b) { return a.y < b.y ||
 
 // new labels sorted by (list, hub) -> keys (list << 32 | dist), values hub
 __global__ void dist_keys(const uint64_t *keys, const uint32_t *vals, const unsigned long long *d_n,
-                          unsigned long long cap, int hub_bits, uint32_t r0, uint64_t *k2, uint32_t *v2) {
+                          unsigned long long cap, int hub_bits, int dist_bits, uint32_t r0, uint64_t *k2,
+                          uint32_t *v2) {
     unsigned long long n = *d_n;
     if (n > cap) n = cap;
     const uint64_t mask = (1ull << hub_bits) - 1;
     for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
         const uint64_t k = keys[i];
-        k2[i] = ((k >> hub_bits) << 32) | vals[i];
+        k2[i] = ((k >> hub_bits) << dist_bits) | vals[i];
         v2[i] = r0 + (uint32_t)(k & mask);
     }
 }
 
 // Merge, per list, the committed distance-ordered entries with the new ones
-// (sorted by (list, dist) in k2/v2, the list's run at [pre[x], pre[x+1])).
+// (sorted by (list, dist) in k2/v2, the distance in k2's low dist_bits bits,
+// the list's run at [pre[x], pre[x+1])).
 // One warp per list; every entry's final slot is its rank in the other run
 // (binary search) plus its own index.  Ties in distance order by hub.
 __global__ void merge_dist_lists(const uint64_t *old_off, const uint2 *old_ent, const uint64_t *new_off,
                                  const uint64_t *pre, const uint64_t *k2, const uint32_t *v2, uint2 *out,
-                                 uint32_t nl) {
+                                 uint32_t nl, int dist_bits) {
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    const uint64_t dmask = (1ull << dist_bits) - 1;
     for (uint32_t x = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); x < nl; x += warps) {
         const uint64_t ob = old_off[x], oe = old_off[x + 1], nb = new_off[x];
         const uint64_t pb = pre[x], pe = pre[x + 1];
@@ -1502,14 +1533,14 @@ __global__ void merge_dist_lists(const uint64_t *old_off, const uint2 *old_ent, 
             uint64_t lo = 0, hi = nn;   // new entries before e
             while (lo < hi) {
                 const uint64_t mid = (lo + hi) >> 1;
-                const uint2 m = make_uint2(v2[pb + mid], (uint32_t)k2[pb + mid]);
+                const uint2 m = make_uint2(v2[pb + mid], (uint32_t)(k2[pb + mid] & dmask));
                 if (ent_less(m, e)) lo = mid + 1;
                 else hi = mid;
             }
             out[nb + i + lo] = e;
         }
         for (uint64_t t = lane_id(); t < nn; t += 32) {
-            const uint2 e = make_uint2(v2[pb + t], (uint32_t)k2[pb + t]);
+            const uint2 e = make_uint2(v2[pb + t], (uint32_t)(k2[pb + t] & dmask));
             uint64_t lo = 0, hi = no;   // old entries before e
             while (lo < hi) {
                 const uint64_t mid = (lo + hi) >> 1;
@@ -1913,9 +1944,15 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         return CHL_ERR_INVALID;
     }
     {
+        // the occupancy query counts a block's dynamic shared memory only up
+        // to the kernel's current limit (48 KB by default): raise it first
+        const int wsm = (int)window_smem(b.win_tw);
+        for (int p = 0; p < 2; ++p)
+            CHL_CUDA(cudaFuncSetAttribute(window_kernel_for(unit, p != 0, b.win_tw),
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, wsm));
         int nbw = 0;
         CHL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbw, window_kernel_for(unit, true, b.win_tw),
-                                                                 b.win_tw * 32, window_smem(b.win_tw)));
+                                                                 b.win_tw * 32, wsm));
         const uint64_t fit_trees = std::max<uint64_t>(1, ws_budget / std::max<uint64_t>(24ull * n, 1));
         b.win_trees = (uint32_t)std::min<uint64_t>((uint64_t)std::max(nbw, 1) * sms, fit_trees);
     }
@@ -1940,15 +1977,6 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         b.hash_max = t;
     }
 
-    // Schedule defaults from graph statistics (measured on RMAT scale 18 and
-    // 512/1024-square grids): heavy-tailed degree distributions start with
-    // 1024 roots and double, so the hubs commit before the bulk of the trees
-    // while the early supersteps still fill the GPU; bounded-degree
-    // (road-like) graphs start with two roots per warp of the schedule (the
-    // 1024-square grid: 1.15x faster than one) and grow by half of the
-    // committed prefix.
-    const uint32_t auto_first = heavy_tail ? 1024u : std::max<uint32_t>(64u, 2 * b.warps);
-    const double auto_growth = heavy_tail ? 2.0 : 0.5;
     // superstep loop
     // label budget per superstep (the reference's sf * N); auto: 32 on
     // heavy-tailed graphs, 1024 on road-like ones.  On road-like graphs a
@@ -1995,9 +2023,20 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
     // many vertices per window (1: IN-criterion rounds instead).  Auto: on
     // heavy-tailed graphs, whose first trees are huge BFS-like searches
     // (RMAT scale 20: 1.4x faster builds with 8 warps per tree); off on
-    // road-like ones, where the windows' coarser PLaNT exit overstates the
-    // tree/label ratio and moves the hybrid switch
+    // road-like ones (the 1024-square grid: 3.81-4.1 s with windows of
+    // 256-4096 vertices against 3.83 s without)
     const uint32_t win_target = opts.window_target ? opts.window_target : (heavy_tail ? 1024u : 1u);
+    // Schedule defaults from graph statistics (measured on RMAT scale 18/20
+    // and 512/1024-square grids): heavy-tailed degree distributions start
+    // with one root per resident window tree (RMAT scale 20: 608 roots,
+    // 2.15 s against 2.28 s with 256 and 2.34 s with 1024) and double, so the
+    // hubs commit before the bulk of the trees while the early supersteps
+    // still fill the GPU; bounded-degree (road-like) graphs start with two
+    // roots per warp of the schedule (the 1024-square grid: 1.15x faster than
+    // one) and grow by half of the committed prefix.
+    const uint32_t auto_first = heavy_tail ? (win_target > 1 ? std::max<uint32_t>(64u, b.win_trees) : 1024u)
+                                           : std::max<uint32_t>(64u, 2 * b.warps);
+    const double auto_growth = heavy_tail ? 2.0 : 0.5;
     // phase switch ratio (the reference's -ps, default 1024): auto 8 on
     // heavy-tailed graphs (RMAT scale 20: pruned GLL supersteps after the
     // first are faster than PLaNT trees there)
@@ -2162,6 +2201,8 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         if ((rc = ensure_ent(&b.ent_b, &b.ent_cap_b, committed + M))) return rc;
         if ((rc = ensure_ent(&b.dent_b, &b.dent_cap_b, committed + M))) return rc;
         const bool clean_now = !plant_now && M > 0;
+        // bits of the distance part of the (list, distance) sort key
+        const int dist_bits = bits_for((uint64_t)hc.max_dist + 1);
         auto chain = [&]() -> int {
             int rc2;
             // --- sort the new labels by (list, hub)
@@ -2202,14 +2243,15 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             {
                 // the same labels by (list, distance, hub), merged into the
                 // distance-ordered copy (the sort is stable: equal distances
-                // keep hub order)
-                dist_keys<<<cgrid, 256, 0, b.st>>>(sk, sv, d_count, b.new_cap, b.hub_bits, r0, ak, av);
+                // keep hub order); the key holds the distance in the bits the
+                // superstep's largest distance needs
+                dist_keys<<<cgrid, 256, 0, b.st>>>(sk, sv, d_count, b.new_cap, b.hub_bits, dist_bits, r0, ak, av);
                 int par2 = 0;
                 if ((rc2 = radix_sort_pairs(ak, av, sk, sv, (const uint64_t *)d_count, b.new_cap,
-                                            b.key_bits - b.hub_bits + 32, b.tmp, b.tmp_bytes, b.st, &par2)))
+                                            b.key_bits - b.hub_bits + dist_bits, b.tmp, b.tmp_bytes, b.st, &par2)))
                     return rc2;
                 merge_dist_lists<<<cgrid, 256, 0, b.st>>>(b.off_a, b.dent_a, b.off_b, b.pre, par2 ? sk : ak,
-                                                          par2 ? sv : av, b.dent_b, b.nl);
+                                                          par2 ? sv : av, b.dent_b, b.nl, dist_bits);
             }
             // longest committed list, for the next superstep's root staging
             CHL_CUDA(cudaMemsetAsync(&b.ctl->max_ratio_den, 0, 8, b.st));
@@ -2218,7 +2260,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             return CHL_OK;
         };
         kernels += 3 * ((b.key_bits + 7) / 8) + (clean_now ? 9 : 0) + 8 +
-                   2 + 3 * ((b.key_bits - b.hub_bits + 32 + 7) / 8);
+                   2 + 3 * ((b.key_bits - b.hub_bits + dist_bits + 7) / 8);
         CHL_CUDA(cudaEventRecord(ev_a, b.st));
         if (opts.use_graphs) {
             CHL_CUDA(cudaStreamBeginCapture(b.st, cudaStreamCaptureModeThreadLocal));

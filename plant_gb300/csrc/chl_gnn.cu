@@ -127,13 +127,18 @@ __device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
 
 // Y[n x 64] = A[n x K] B[K x 64] (+ bias, relu) where A's columns are the
 // concatenation of two [n x 64] BF16 arrays A0 | A1 (K = 128) or one (K = 64).
-// Each warp computes 16 rows; B is staged in shared memory as BF16.
+// Each warp computes 16 rows at a time.  B is staged in shared memory as
+// BF16, transposed (column-major, rows padded to K + 8 elements so the eight
+// columns a fragment load touches fall in distinct banks); A fragments are
+// read straight from global memory as BF16 pairs.
 // mode 0: Y = relu(AB + bias) -> BF16 out_bf;  mode 1: Y = AB -> FP32 out_f.
 template <int K>
-__global__ void gemm_rows(uint32_t n, const __nv_bfloat16 *A0, const __nv_bfloat16 *A1, const float *B,
-                          const float *bias, int mode, __nv_bfloat16 *out_bf, float *out_f, int ldo) {
-    __shared__ __nv_bfloat16 sB[K * H];
-    for (int i = threadIdx.x; i < K * H; i += blockDim.x) sB[i] = __float2bfloat16_rn(B[i]);
+__global__ void __launch_bounds__(128) gemm_rows(uint32_t n, const __nv_bfloat16 *A0, const __nv_bfloat16 *A1,
+                                                 const float *B, const float *bias, int mode,
+                                                 __nv_bfloat16 *out_bf, float *out_f, int ldo) {
+    constexpr int KP = K + 8;
+    __shared__ __align__(16) __nv_bfloat16 sBt[H * KP];
+    for (int i = threadIdx.x; i < K * H; i += blockDim.x) sBt[(i % H) * KP + i / H] = __float2bfloat16_rn(B[i]);
     __syncthreads();
     const uint32_t lane = lane_id(), gid = lane >> 2, tig = lane & 3;
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
@@ -145,27 +150,29 @@ __global__ void gemm_rows(uint32_t n, const __nv_bfloat16 *A0, const __nv_bfloat
         for (int j = 0; j < 8; ++j)
 #pragma unroll
             for (int q = 0; q < 4; ++q) acc[j][q] = 0.f;
+        // two BF16 at (row, col), col even: one 4-byte load (0 past the end)
+        auto ld2 = [&](const __nv_bfloat16 *src, uint32_t row, int col) -> uint32_t {
+            return row < n ? __ldg((const unsigned int *)(src + (size_t)row * H + col)) : 0u;
+        };
+        uint32_t af[K / 16][4];
 #pragma unroll
         for (int ks = 0; ks < K / 16; ++ks) {
             const __nv_bfloat16 *src = (ks * 16 < H) ? A0 : A1;
-            const int kc = (ks * 16) % H;
-            const __nv_bfloat16 z = __float2bfloat16_rn(0.f);
-            auto ld = [&](uint32_t row, int col) -> __nv_bfloat16 {
-                return row < n ? src[(size_t)row * H + col] : z;
-            };
-            uint32_t a[4];
-            a[0] = pack2(ld(r0, kc + 2 * tig), ld(r0, kc + 2 * tig + 1));
-            a[1] = pack2(ld(r1, kc + 2 * tig), ld(r1, kc + 2 * tig + 1));
-            a[2] = pack2(ld(r0, kc + 2 * tig + 8), ld(r0, kc + 2 * tig + 9));
-            a[3] = pack2(ld(r1, kc + 2 * tig + 8), ld(r1, kc + 2 * tig + 9));
+            const int kc = (ks * 16) % H + 2 * (int)tig;
+            af[ks][0] = ld2(src, r0, kc);
+            af[ks][1] = ld2(src, r1, kc);
+            af[ks][2] = ld2(src, r0, kc + 8);
+            af[ks][3] = ld2(src, r1, kc + 8);
+        }
+#pragma unroll
+        for (int ks = 0; ks < K / 16; ++ks) {
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                const int col = j * 8 + gid;
-                const int k0 = ks * 16 + 2 * tig;
+                const __nv_bfloat16 *bc = sBt + (j * 8 + gid) * KP + ks * 16 + 2 * tig;
                 uint32_t b[2];
-                b[0] = pack2(sB[(k0)*H + col], sB[(k0 + 1) * H + col]);
-                b[1] = pack2(sB[(k0 + 8) * H + col], sB[(k0 + 9) * H + col]);
-                mma_bf16(acc[j], a, b);
+                b[0] = *(const uint32_t *)bc;
+                b[1] = *(const uint32_t *)(bc + 8);
+                mma_bf16(acc[j], af[ks], b);
             }
         }
 #pragma unroll
@@ -184,12 +191,26 @@ __global__ void gemm_rows(uint32_t n, const __nv_bfloat16 *A0, const __nv_bfloat
                     o.y = __float2bfloat16_rn(y1);
                     *(__nv_bfloat162 *)(out_bf + (size_t)row * H + c) = o;
                 } else {
-                    out_f[(size_t)row * ldo + c] = y0;
-                    out_f[(size_t)row * ldo + c + 1] = y1;
+                    *(float2 *)(out_f + (size_t)row * ldo + c) = make_float2(y0, y1);
                 }
             }
         }
     }
+}
+
+// blocks of gemm_rows<K> that fill the GPU (resident blocks per SM x SMs)
+template <int K>
+int gemm_grid(int sms) {
+    static int per_sm = 0;
+    if (!per_sm) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, gemm_rows<K>, 128, 0) != cudaSuccess || b < 1) {
+            (void)cudaGetLastError();
+            b = 4;
+        }
+        per_sm = b;
+    }
+    return per_sm * sms;
 }
 
 // s = h w_out + b_out; loss terms; ds = 2 (s - y) / n
@@ -464,7 +485,7 @@ int forward(chl_gnn *M, const GraphDev &G, uint64_t seed) {
         const __nv_bfloat16 *hp = hb + (size_t)(l - 1) * n * H;
         __nv_bfloat16 *ml = mb + (size_t)l * n * H;
         aggregate_mean<<<sms * 8, 256>>>(n, G.off_out.as<uint64_t>(), G.head_out.as<uint32_t>(), hp, ml);
-        gemm_rows<K2><<<sms * 4, 128>>>(n, hp, ml, W, W + (size_t)K2 * H, 0, hb + (size_t)l * n * H, nullptr, 0);
+        gemm_rows<K2><<<gemm_grid<K2>(sms), 128>>>(n, hp, ml, W, W + (size_t)K2 * H, 0, hb + (size_t)l * n * H, nullptr, 0);
     }
     const float *wout = P + kP0 + (size_t)M->layers * kPL;
     head_fwd_bwd<<<sms * 8, 256>>>(n, hb + (size_t)M->layers * n * H, wout, wout + H, nullptr, M->s.as<float>(),
@@ -502,8 +523,8 @@ int backward(chl_gnn *M, const GraphDev &G, double *loss) {
         grad_w_mma<<<gblocks, 256>>>(n, hp, ml, mb, M->dz.as<float>(), gW, gW + (size_t)K2 * H);
         // dA = dz W^T as two K = 64 GEMMs into the two column halves of dA
         transpose_w<<<16, 256>>>(W, M->wt.as<float>(), M->wt.as<float>() + H * H);
-        gemm_rows<H><<<sms * 4, 128>>>(n, mb, mb, M->wt.as<float>(), nullptr, 1, nullptr, M->dA.as<float>(), K2);
-        gemm_rows<H><<<sms * 4, 128>>>(n, mb, mb, M->wt.as<float>() + H * H, nullptr, 1, nullptr,
+        gemm_rows<H><<<gemm_grid<H>(sms), 128>>>(n, mb, mb, M->wt.as<float>(), nullptr, 1, nullptr, M->dA.as<float>(), K2);
+        gemm_rows<H><<<gemm_grid<H>(sms), 128>>>(n, mb, mb, M->wt.as<float>() + H * H, nullptr, 1, nullptr,
                                        M->dA.as<float>() + H, K2);
         scatter_mean_bwd<<<sms * 8, 256>>>(n, M->dA.as<float>(), G.off_in.as<uint64_t>(), G.head_in.as<uint32_t>(),
                                            G.off_out.as<uint64_t>(), M->dh.as<float>());

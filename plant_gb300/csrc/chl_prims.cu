@@ -175,51 +175,98 @@ __global__ void radix_hist(const uint64_t *keys, const uint64_t *d_n, uint64_t c
         hist[(uint64_t)i * gridDim.x + blockIdx.x] = h[i];
 }
 
-__global__ void radix_scatter(const uint64_t *kin, const uint32_t *vin, uint64_t *kout,
-                              uint32_t *vout, const uint64_t *d_n, uint64_t cap,
-                              int shift, const uint64_t *offs) {
-    __shared__ uint64_t run[kRadix];
-    __shared__ uint32_t wcnt[kSortWarps][kRadix];
-    __shared__ uint32_t tile_tot[kRadix];
-    for (int i = threadIdx.x; i < kRadix; i += blockDim.x)
-        run[i] = offs[(uint64_t)i * gridDim.x + blockIdx.x];
+// Scatter of one digit pass.  A block walks its range in tiles of kTile
+// items: warp w holds the tile's items [w * kWarpItems, (w + 1) *
+// kWarpItems) in registers, ranks them per digit (match_any per round of 32,
+// a running count per warp and digit), the block places the whole tile in
+// shared memory ordered by (digit, position), and each digit's run is then
+// written to its global slots with consecutive threads on consecutive
+// addresses.  Positions within a digit keep the input order (stable).
+constexpr int kTileItems = 8;
+constexpr int kTile = kSortThreads * kTileItems;   // 2048
+static_assert(kSortThreads == kRadix, "the digit prefix gives each thread one digit");
+constexpr int kWarpItems = 32 * kTileItems;
+
+__global__ void __launch_bounds__(kSortThreads) radix_scatter(const uint64_t *kin, const uint32_t *vin, uint64_t *kout,
+                                                              uint32_t *vout, const uint64_t *d_n, uint64_t cap,
+                                                              int shift, const uint64_t *offs) {
+    __shared__ uint64_t s_k[kTile];
+    __shared__ uint32_t s_v[kTile];
+    __shared__ uint32_t wh[kSortWarps][kRadix];   // per-warp digit counts, then their prefix over warps
+    __shared__ uint32_t t_start[kRadix + 1];      // each digit's first slot in the tile
+    __shared__ uint32_t w_tot[kSortWarps];
+    __shared__ uint64_t run[kRadix];              // each digit's next global slot
+    const uint32_t tid = threadIdx.x, lane = lane_id(), warp = tid >> 5;
+    for (int i = tid; i < kRadix; i += blockDim.x) run[i] = offs[(uint64_t)i * gridDim.x + blockIdx.x];
     uint64_t n = *d_n;
     if (n > cap) n = cap;
     uint64_t b, e;
     block_range(n, b, e);
-    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
-    for (uint64_t base = b; base < e; base += kSortThreads) {
-        for (int i = threadIdx.x; i < kSortWarps * kRadix; i += blockDim.x)
-            (&wcnt[0][0])[i] = 0;
+    for (uint64_t base = b; base < e; base += kTile) {
+        const uint32_t cnt = (uint32_t)((e - base) < (uint64_t)kTile ? (e - base) : (uint64_t)kTile);
+        for (int i = tid; i < kSortWarps * kRadix; i += blockDim.x) (&wh[0][0])[i] = 0;
         __syncthreads();
-        uint64_t i = base + threadIdx.x;
-        bool valid = i < e;
-        uint64_t k = valid ? kin[i] : 0;
-        uint32_t v = valid ? vin[i] : 0;
-        uint32_t dg = valid ? (uint32_t)((k >> shift) & 255) : 256u;
-        uint32_t peers = __match_any_sync(kFull, dg);
-        uint32_t rk = __popc(peers & lanemask_lt());
-        uint32_t leader = __ffs(peers) - 1;
-        if (valid && lane == leader) wcnt[warp][dg] = __popc(peers);
+        uint64_t k[kTileItems];
+        uint32_t v[kTileItems], dg[kTileItems], pos[kTileItems];
+#pragma unroll
+        for (int j = 0; j < kTileItems; ++j) {
+            const uint32_t idx = warp * kWarpItems + j * 32 + lane;
+            const bool valid = idx < cnt;
+            k[j] = valid ? kin[base + idx] : 0;
+            v[j] = valid ? vin[base + idx] : 0;
+            dg[j] = valid ? (uint32_t)((k[j] >> shift) & (kRadix - 1)) : (uint32_t)kRadix;
+        }
+#pragma unroll
+        for (int j = 0; j < kTileItems; ++j) {
+            const uint32_t peers = __match_any_sync(kFull, dg[j]);
+            const uint32_t before = dg[j] < kRadix ? wh[warp][dg[j]] : 0u;
+            __syncwarp();
+            if (dg[j] < kRadix && lane == (uint32_t)(__ffs(peers) - 1)) wh[warp][dg[j]] = before + __popc(peers);
+            __syncwarp();
+            pos[j] = before + __popc(peers & lanemask_lt());
+        }
         __syncthreads();
-        for (int d = threadIdx.x; d < kRadix; d += blockDim.x) {
-            uint32_t acc = 0;
+        // per digit (one per thread): prefix over warps, then over digits
+        uint32_t tot = 0;
+        for (int d = tid; d < kRadix; d += blockDim.x) {
 #pragma unroll
             for (int w = 0; w < kSortWarps; ++w) {
-                uint32_t t = wcnt[w][d];
-                wcnt[w][d] = acc;
-                acc += t;
+                const uint32_t t = wh[w][d];
+                wh[w][d] = tot;
+                tot += t;
             }
-            tile_tot[d] = acc;
+        }
+        uint32_t incl = tot;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(kFull, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        if (lane == 31) w_tot[warp] = incl;
+        __syncthreads();
+        uint32_t wbase = 0;
+        for (uint32_t w = 0; w < warp; ++w) wbase += w_tot[w];
+        if (tid < kRadix) t_start[tid] = wbase + incl - tot;
+        if (tid == 0) t_start[kRadix] = cnt;
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < kTileItems; ++j) {
+            if (dg[j] < kRadix) {
+                const uint32_t p = t_start[dg[j]] + wh[warp][dg[j]] + pos[j];
+                s_k[p] = k[j];
+                s_v[p] = v[j];
+            }
         }
         __syncthreads();
-        if (valid) {
-            uint64_t p = run[dg] + wcnt[warp][dg] + rk;
-            kout[p] = k;
-            vout[p] = v;
+        for (uint32_t i = tid; i < cnt; i += blockDim.x) {
+            const uint64_t kk = s_k[i];
+            const uint32_t d = (uint32_t)((kk >> shift) & (kRadix - 1));
+            const uint64_t gp = run[d] + (i - t_start[d]);
+            kout[gp] = kk;
+            vout[gp] = s_v[i];
         }
         __syncthreads();
-        for (int d = threadIdx.x; d < kRadix; d += blockDim.x) run[d] += tile_tot[d];
+        if (tid < kRadix) run[tid] += t_start[tid + 1] - t_start[tid];
         __syncthreads();
     }
 }
