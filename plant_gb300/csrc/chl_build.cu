@@ -415,7 +415,7 @@ batch_kernel(TreeArgs a) {
                 int nv_batch = 0;
                 for (uint32_t j = lane; j < nb; j += 32) {
                     const uint32_t kx = s_bk[j];
-                    const uint32_t rx = s_bp[j];   // rank stored by the scan
+                    const uint32_t rx = __ldg(&a.rank[s_bv[j]]);   // batch vertices only, not every scanned one
                     uint32_t skip;
                     if (PLANT) {
                         nv_batch += (int)(kx & 1u);
@@ -782,14 +782,13 @@ batch_kernel(TreeArgs a) {
                 }
                 // several 32-entry chunks per step: their loads are issued
                 // together
-                auto classify = [&](bool valid, uint32_t x, uint32_t kx, uint32_t wx, uint32_t rx) {
+                auto classify = [&](bool valid, uint32_t x, uint32_t kx, uint32_t wx) {
                     const bool take = valid && (uint64_t)(kx >> 1) < (uint64_t)dmin + wx;
                     const uint32_t tm = __ballot_sync(kFull, take);
                     if (take) {
                         const uint32_t at = nb + __popc(tm & lanemask_lt());
                         s_bv[at] = x;
                         s_bk[at] = kx;
-                        s_bp[at] = rx;   // rank, turned into the skip flag by settle()
                     }
                     nb += __popc(tm);
                     const bool kp = valid && !take;
@@ -805,7 +804,7 @@ batch_kernel(TreeArgs a) {
                     if (stop) break;
                     const long long ts0 = phase_clock();
                     bool vv[CHL_SCAN_CHUNKS];
-                    uint32_t xx[CHL_SCAN_CHUNKS], kk[CHL_SCAN_CHUNKS], ww[CHL_SCAN_CHUNKS], rr[CHL_SCAN_CHUNKS];
+                    uint32_t xx[CHL_SCAN_CHUNKS], kk[CHL_SCAN_CHUNKS], ww[CHL_SCAN_CHUNKS];
 #pragma unroll
                     for (int c = 0; c < CHL_SCAN_CHUNKS; ++c) {
                         const uint32_t i = b0 + 32 * c + lane;
@@ -816,11 +815,10 @@ batch_kernel(TreeArgs a) {
                     for (int c = 0; c < CHL_SCAN_CHUNKS; ++c) {
                         kk[c] = vv[c] ? __ldcg(&key[xx[c]]) : kInf;
                         ww[c] = vv[c] ? win[xx[c]] : 0u;
-                        rr[c] = vv[c] ? __ldg(&a.rank[xx[c]]) : 0u;
                     }
                     __syncwarp();
 #pragma unroll
-                    for (int c = 0; c < CHL_SCAN_CHUNKS; ++c) classify(vv[c], xx[c], kk[c], ww[c], rr[c]);
+                    for (int c = 0; c < CHL_SCAN_CHUNKS; ++c) classify(vv[c], xx[c], kk[c], ww[c]);
                     __syncwarp();
                     cyc[0] += phase_clock() - ts0;
                 }

@@ -128,9 +128,9 @@ __device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
 // Y[n x 64] = A[n x K] B[K x 64] (+ bias, relu) where A's columns are the
 // concatenation of two [n x 64] BF16 arrays A0 | A1 (K = 128) or one (K = 64).
 // Each warp computes 16 rows at a time.  B is staged in shared memory as
-// BF16, transposed (column-major, rows padded to K + 8 elements so the eight
-// columns a fragment load touches fall in distinct banks); A fragments are
-// read straight from global memory as BF16 pairs.
+// BF16, transposed (column-major, rows padded to K + 8 elements: 16-byte
+// aligned rows whose eight-row groups fall in distinct banks) and read with
+// ldmatrix; A fragments are read straight from global memory as BF16 pairs.
 // mode 0: Y = relu(AB + bias) -> BF16 out_bf;  mode 1: Y = AB -> FP32 out_f.
 template <int K>
 __global__ void __launch_bounds__(128) gemm_rows(uint32_t n, const __nv_bfloat16 *A0, const __nv_bfloat16 *A1,
@@ -167,12 +167,20 @@ __global__ void __launch_bounds__(128) gemm_rows(uint32_t n, const __nv_bfloat16
 #pragma unroll
         for (int ks = 0; ks < K / 16; ++ks) {
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const __nv_bfloat16 *bc = sBt + (j * 8 + gid) * KP + ks * 16 + 2 * tig;
-                uint32_t b[2];
-                b[0] = *(const uint32_t *)bc;
-                b[1] = *(const uint32_t *)(bc + 8);
-                mma_bf16(acc[j], af[ks], b);
+            for (int j = 0; j < 8; j += 2) {
+                // one ldmatrix.x4: the B fragments of column tiles j and j + 1
+                // (8x8 matrices: rows = columns of B, 8 consecutive k each;
+                // lane l addresses row l % 8 of matrix l / 8)
+                const uint32_t mtx = lane >> 3;
+                const __nv_bfloat16 *rowp =
+                    sBt + ((j + (mtx >> 1)) * 8 + (lane & 7)) * KP + ks * 16 + (mtx & 1) * 8;
+                uint32_t b[4];
+                asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                             : "=r"(b[0]), "=r"(b[1]), "=r"(b[2]), "=r"(b[3])
+                             : "r"((uint32_t)__cvta_generic_to_shared(rowp)));
+                const uint32_t b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
+                mma_bf16(acc[j], af[ks], b0);
+                mma_bf16(acc[j + 1], af[ks], b1);
             }
         }
 #pragma unroll
