@@ -30,6 +30,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <type_traits>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -83,9 +84,8 @@ struct TreeArgs {
     uint32_t n;
     int sides;                      // 1: symmetric graph, one label side stored
     const uint64_t *g_off[2];       // [f]: arcs traversed by trees of side f
-    const uint4 *g_farc[2];         // (head, length, rank[head], 0) per arc
+    const uint4 *g_farc[2];         // (head, length, rank[head], win[head]) per arc
     const uint2 *g_fhead[2];        // (head, rank[head]) per arc, unit lengths
-    const uint32_t *win[2];         // [f]: shortest arc into v along direction f
     const uint32_t *order;
     const uint32_t *rank;
     const uint64_t *l_off;          // committed labels, index lidx(v, side)
@@ -100,7 +100,7 @@ struct TreeArgs {
     unsigned long long out_cap;
     uint32_t *tree_size;            // per root (index r - r0), sides summed
     uint32_t *tree_labels;
-    uint32_t *ws_key;               // per warp slot, n entries each
+    uint32_t *ws_key;               // per warp slot, n keys each (64-bit on weighted graphs)
     uint32_t *ws_vis;
     uint32_t *ws_front;             // per warp slot: queue, next queue, far pile
     uint32_t *ws_win;               // window kernel: 6 n words per tree (block)
@@ -255,7 +255,13 @@ batch_kernel(TreeArgs a) {
     uint64_t *s_ek = (uint64_t *)(((uintptr_t)(s_as + kBatch) + 7) & ~(uintptr_t)7);   // staged label keys
     uint32_t *s_ev = (uint32_t *)(s_ek + kEmit);       // staged label distances
 
-    uint32_t *key = a.ws_key + (size_t)slot * a.n;
+    // A vertex's key (distance * 2 + not-via).  On weighted graphs it shares
+    // a 64-bit word with win(v), the shortest arc into v (key in the high
+    // half, so atomicMin orders by key): the frontier scan gets both with
+    // one load.  Unit lengths have win(v) = 1 and 32-bit keys.
+    using KeyW = typename std::conditional<UNIT, uint32_t, unsigned long long>::type;
+    KeyW *key = (KeyW *)a.ws_key + (size_t)slot * a.n;
+    constexpr KeyW kKeyNone = (KeyW)~(KeyW)0;
     uint32_t *vis = a.ws_vis + (size_t)slot * a.n;
     // queue as two arrays: a round reads `front` and writes the vertices it
     // keeps, and those its relaxations add, to `fnext`; then they swap
@@ -308,7 +314,6 @@ batch_kernel(TreeArgs a) {
             const long long tr0 = phase_clock();
             const int f = (a.sides == 1) ? 1 : sd;
             const uint64_t *goff = a.g_off[f];
-            const uint32_t *win = a.win[f];
             const uint4 *farc = a.g_farc[f];
             const uint2 *fhead = a.g_fhead[f];
             // label entries the prune tests scan: the distance-ordered copy
@@ -383,7 +388,7 @@ batch_kernel(TreeArgs a) {
                 return hit;
             };
             if (lane == 0) {
-                __stcg(&key[v], 1u);
+                __stcg(&key[v], UNIT ? (KeyW)1u : (KeyW)((1ull << 32) | 1u));   // win 1 admits the root
                 vis[0] = v;
                 front[0] = v;
             }
@@ -597,7 +602,7 @@ batch_kernel(TreeArgs a) {
                 // atomics of both chunks are issued together
                 constexpr int RC = CHL_RELAX_CHUNKS;
                 for (uint32_t t0 = 0; t0 < total; t0 += 32 * RC) {
-                    uint32_t w[RC], nk[RC], old[RC], kxs[RC], len[RC], rk[RC];
+                    uint32_t w[RC], nk[RC], old[RC], kxs[RC], len[RC], rk[RC], wn[RC];
                     bool act[RC], upd[RC];
 #pragma unroll
                     for (int c = 0; c < RC; ++c) {
@@ -607,6 +612,7 @@ batch_kernel(TreeArgs a) {
                         kxs[c] = 0;
                         len[c] = 0;
                         rk[c] = 0;
+                        wn[c] = 1;
                         act[c] = false;
                         upd[c] = false;
                     }
@@ -628,6 +634,7 @@ batch_kernel(TreeArgs a) {
                                 w[c] = hl.x;
                                 len[c] = hl.y;
                                 rk[c] = hl.z;
+                                wn[c] = hl.w;
                             }
                             kxs[c] = s_bk[lo];
                             act[c] = true;
@@ -643,7 +650,13 @@ batch_kernel(TreeArgs a) {
                         const uint64_t dd64 = (uint64_t)(kxs[c] >> 1) + len[c];
                         if (dd64 < 0x7FFFFFFFull) {
                             nk[c] = (uint32_t)dd64 * 2u + nv[c];
-                            old[c] = atomicMin(&key[w[c]], nk[c]);
+                            if (UNIT) {
+                                old[c] = (uint32_t)atomicMin(&key[w[c]], (KeyW)nk[c]);
+                            } else {
+                                const unsigned long long o64 =
+                                    atomicMin(&key[w[c]], (KeyW)(((unsigned long long)nk[c] << 32) | wn[c]));
+                                old[c] = (uint32_t)(o64 >> 32);
+                            }
                             upd[c] = nk[c] < old[c];
                             if (upd[c]) dnext = min(dnext, nk[c] >> 1);
                         } else {
@@ -709,7 +722,7 @@ batch_kernel(TreeArgs a) {
                     // entries, taking the keys as spread evenly over [min, max]
                     uint32_t mn = kInf, mx = 0;
                     for (uint32_t i = lane; i < npile; i += 32) {
-                        const uint32_t k = __ldcg(&key[pile[i]]) >> 1;
+                        const uint32_t k = (uint32_t)(__ldcg(&key[pile[i]]) >> (UNIT ? 1 : 33));
                         mn = min(mn, k);
                         mx = max(mx, k);
                     }
@@ -731,7 +744,7 @@ batch_kernel(TreeArgs a) {
                         const uint32_t i = b0 + lane;
                         const bool valid = i < npile;
                         const uint32_t x = valid ? pile[i] : 0u;
-                        const uint32_t k = valid ? (__ldcg(&key[x]) >> 1) : kInf;
+                        const uint32_t k = valid ? (uint32_t)(__ldcg(&key[x]) >> (UNIT ? 1 : 33)) : kInf;
                         const bool live = valid && k >= t_old;
                         const bool nr = live && k < thr;
                         const bool kp = live && !nr;
@@ -813,8 +826,11 @@ batch_kernel(TreeArgs a) {
                     }
 #pragma unroll
                     for (int c = 0; c < CHL_SCAN_CHUNKS; ++c) {
-                        kk[c] = vv[c] ? __ldcg(&key[xx[c]]) : kInf;
-                        ww[c] = vv[c] ? win[xx[c]] : 0u;
+                        const KeyW k = vv[c] ? __ldcg(&key[xx[c]]) : kKeyNone;
+                        kk[c] = UNIT ? (uint32_t)k : (uint32_t)((unsigned long long)k >> 32);
+                        // unit lengths: every queued vertex but the root has an
+                        // in-arc of length 1, and 1 also admits the root
+                        ww[c] = UNIT ? 1u : (uint32_t)k;
                     }
                     __syncwarp();
 #pragma unroll
@@ -846,7 +862,7 @@ batch_kernel(TreeArgs a) {
             }
             c_vis += t_size;
             const long long tz0 = phase_clock();
-            for (uint32_t k = lane; k < nvis; k += 32) __stcg(&key[vis[k]], kInf);
+            for (uint32_t k = lane; k < nvis; k += 32) __stcg(&key[vis[k]], kKeyNone);
             for (uint32_t k = lane; k < a.hash_slots; k += 32) s_tab[k] = kSlotEmpty;
             cyc[6] += phase_clock() - tz0;
             __syncwarp();
@@ -1363,10 +1379,10 @@ TreeKernel window_kernel_for(bool unit, bool plant, uint32_t tw) {
     return plant ? window_kernel_tw<false, true>(tw) : window_kernel_tw<false, false>(tw);
 }
 
-__global__ void fat_arcs(uint64_t m, const uint2 *arc, const uint32_t *rank, uint4 *out) {
+__global__ void fat_arcs(uint64_t m, const uint2 *arc, const uint32_t *rank, const uint32_t *win, uint4 *out) {
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
         const uint2 a = arc[e];
-        out[e] = make_uint4(a.x, a.y, rank[a.x], 0u);
+        out[e] = make_uint4(a.x, a.y, rank[a.x], win[a.x]);
     }
 }
 
@@ -1725,7 +1741,7 @@ struct Build {
     uint32_t warps = 0;   // warps the schedule is sized for
     uint32_t slots = 0;   // warp slots launched by batch_kernel
     uint32_t hash_max = 2048;                // largest root hash table (slots)
-    uint4 *farc[2] = {nullptr, nullptr};     // (head, length, rank[head], 0) per arc
+    uint4 *farc[2] = {nullptr, nullptr};     // (head, length, rank[head], win[head]) per arc
     uint2 *fhead[2] = {nullptr, nullptr};    // (head, rank[head]) per arc, unit lengths
     cudaGraphExec_t commit_exec = nullptr;   // captured commit chain
     uint64_t graph_launches = 0;
@@ -1906,7 +1922,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
                 fat_heads<<<grid, 256, 0, b.st>>>(m, b.dg->head[s], b.rank, b.fhead[s]);
             } else {
                 if ((rc = dalloc(&b.farc[s], std::max<uint64_t>(m, 1)))) return rc;
-                fat_arcs<<<grid, 256, 0, b.st>>>(m, b.dg->arc[s], b.rank, b.farc[s]);
+                fat_arcs<<<grid, 256, 0, b.st>>>(m, b.dg->arc[s], b.rank, b.dg->win[s], b.farc[s]);
             }
             CHL_CUDA(cudaGetLastError());
             ++prep_kernels;
@@ -1916,7 +1932,8 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             b.fhead[1] = b.fhead[0];
         }
     }
-    // key, vis and three queue arrays per warp slot
+    // key, vis and three queue arrays per warp slot (the 32-bit-key size
+    // sets the schedule's warp count; the slots below use the real one)
     const size_t per_slot = (size_t)n * 20;
     uint32_t want = (uint32_t)sms * 48;   // 12 blocks of 4 warps per SM at most
     if (opts.max_warps) want = std::min<uint32_t>(want, opts.max_warps);
@@ -1933,6 +1950,12 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         &nbo, unit ? batch_kernel<true, true> : batch_kernel<false, true>, kWarpsPerBlock * 32, 0));
     nbo = std::max(nbo, 1);
     b.slots = std::min(b.warps, (uint32_t)nbo * (uint32_t)sms * kWarpsPerBlock);
+    {
+        // weighted graphs hold 64-bit keys: 24 bytes per vertex and slot
+        const size_t slot_bytes = (size_t)n * (unit ? 20 : 24);
+        const uint32_t fit_slots = (uint32_t)std::max<size_t>(kWarpsPerBlock, ws_budget / std::max<size_t>(slot_bytes, 1));
+        b.slots = std::max<uint32_t>(kWarpsPerBlock, (std::min(b.slots, fit_slots) / kWarpsPerBlock) * kWarpsPerBlock);
+    }
     // window kernel (first superstep): one tree per block of win_tw warps
     // (auto: 8 on heavy-tailed graphs, 4 otherwise), as many trees as are
     // resident, 6 n words each
@@ -1954,13 +1977,15 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
         const uint64_t fit_trees = std::max<uint64_t>(1, ws_budget / std::max<uint64_t>(24ull * n, 1));
         b.win_trees = (uint32_t)std::min<uint64_t>((uint64_t)std::max(nbw, 1) * sms, fit_trees);
     }
-    // one workspace for both layouts: batch_kernel's key, vis and queue
-    // arrays per warp slot (5 n words), window_kernel's 6 n words per tree
-    const size_t ws_words = std::max((size_t)b.slots * 5 * n, (size_t)b.win_trees * 6 * n);
+    // one workspace for both layouts: batch_kernel's key (two words on
+    // weighted graphs), vis and queue arrays per warp slot (5 or 6 n words),
+    // window_kernel's 6 n words per tree
+    const size_t key_words = unit ? 1 : 2;
+    const size_t ws_words = std::max((size_t)b.slots * (4 + key_words) * n, (size_t)b.win_trees * 6 * n);
     if ((rc = dalloc(&b.ws_all, ws_words))) return rc;
     b.ws_key = b.ws_all;
-    b.ws_vis = b.ws_all + (size_t)b.slots * n;
-    b.ws_front = b.ws_all + (size_t)b.slots * 2 * n;
+    b.ws_vis = b.ws_all + (size_t)b.slots * key_words * n;
+    b.ws_front = b.ws_vis + (size_t)b.slots * n;
     b.ws_layout = 0;   // set before each tree launch
     {
         // root hash slots: at most 2048, and within CHL_SMEM_CAP_KB of shared
@@ -2068,7 +2093,6 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
                 ta.g_off[s] = b.dg->off[s];
                 ta.g_farc[s] = b.farc[s];
                 ta.g_fhead[s] = b.fhead[s];
-                ta.win[s] = b.dg->win[s];
             }
             ta.order = b.order;
             ta.rank = b.rank;
@@ -2133,7 +2157,7 @@ int build_labels(const chl_graph *g, const uint32_t *order_h, uint32_t n,
             // reads is INF (each tree resets its own keys when it ends)
             const int layout = windowed ? 2 : 1;
             if (b.ws_layout != layout) {
-                const size_t words = windowed ? (size_t)b.win_trees * 6 * n : (size_t)b.slots * 5 * n;
+                const size_t words = windowed ? (size_t)b.win_trees * 6 * n : (size_t)b.slots * (4 + key_words) * n;
                 CHL_CUDA(cudaMemsetAsync(b.ws_all, 0xFF, words * 4, b.st));
                 b.ws_layout = layout;
             }
