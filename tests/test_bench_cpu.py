@@ -58,12 +58,18 @@ def test_pps_sample_is_unbiased_on_known_sizes():
     import bench
     rng = np.random.default_rng(0)
     sizes = np.array([5.0, 1.0, 0.5, 3.0, 0.1, 2.0, 0.0])
-    est = []
-    for _ in range(4000):
-        plan = bench.pps_sample(sizes, 2.0, rng)
-        assert all(sizes[i] > 0 for i, _ in plan)
-        est.append(sum(sizes[i] / pi for i, pi in plan))
-    assert abs(np.mean(est) / sizes.sum() - 1) < 0.02
+    times = sizes * np.linspace(0.5, 1.5, len(sizes))   # time per unit size drifts over the build
+    for target, strata in ((2.0, 1), (6.0, 3), (100.0, 6)):
+        est = []
+        for _ in range(4000):
+            plan = bench.pps_sample(sizes, target, rng)
+            assert len(plan) <= strata
+            assert all(sizes[i] > 0 for i, _ in plan)
+            est.append(sum(times[i] / pi for i, pi in plan))
+        assert abs(np.mean(est) / times.sum() - 1) < 0.02
+    # every live superstep once when the target affords them all: exact
+    plan = bench.pps_sample(sizes, 100.0, rng)
+    assert sorted(i for i, _ in plan) == [0, 1, 2, 3, 4, 5] and all(pi == 1.0 for _, pi in plan)
 
 
 def test_reference_arm_loads_no_product_code(tmp_path):
