@@ -56,8 +56,11 @@ constexpr bool kPhaseTiming = CHL_PHASE_TIMING != 0;
 #define CHL_BATCH_MIN_BLOCKS 0   // batched settle launch bound (0: compiler's choice;
                                  // 1 measured slower: more registers, fewer warps)
 #endif
+#ifndef CHL_RELAX_PRECHECK
+#define CHL_RELAX_PRECHECK 1   // read a key before its atomicMin; skip the atomic when it cannot lower it
+#endif
 #ifndef CHL_RELAX_CHUNKS
-#define CHL_RELAX_CHUNKS 2   // 32-arc chunks per relax step
+#define CHL_RELAX_CHUNKS 3   // 32-arc chunks per relax step
 #endif
 
 struct BuildCtl {
@@ -598,9 +601,12 @@ batch_kernel(TreeArgs a) {
                     cur += (uint32_t)__popc(starts);
                     return own;
                 };
-                // two 32-arc chunks per step: arc loads, rank loads and
-                // atomics of both chunks are issued together
+                // CHL_RELAX_CHUNKS 32-arc chunks per step: their arc loads and
+                // atomics are issued together (three measured best on the
+                // 1024-square grid and RMAT-20: 3.43 -> 3.31 s and 2.06 ->
+                // 1.90 s against two)
                 constexpr int RC = CHL_RELAX_CHUNKS;
+                int dql = 0;   // this lane's change of the queued not-via count
                 for (uint32_t t0 = 0; t0 < total; t0 += 32 * RC) {
                     uint32_t w[RC], nk[RC], old[RC], kxs[RC], len[RC], rk[RC], wn[RC];
                     bool act[RC], upd[RC];
@@ -641,16 +647,22 @@ batch_kernel(TreeArgs a) {
                         }
                     }
                     uint32_t nv[RC];
+                    KeyW pre[RC];   // the key word before the atomic (keys only decrease)
 #pragma unroll
-                    for (int c = 0; c < RC; ++c)
+                    for (int c = 0; c < RC; ++c) {
                         nv[c] = (!PLANT || ((kxs[c] & 1u) && rk[c] >= r)) ? 1u : 0u;
+                        pre[c] = (CHL_RELAX_PRECHECK && act[c]) ? __ldcg(&key[w[c]]) : kKeyNone;
+                    }
 #pragma unroll
                     for (int c = 0; c < RC; ++c) {
                         if (!act[c]) continue;
                         const uint64_t dd64 = (uint64_t)(kxs[c] >> 1) + len[c];
                         if (dd64 < 0x7FFFFFFFull) {
                             nk[c] = (uint32_t)dd64 * 2u + nv[c];
-                            if (UNIT) {
+                            const uint32_t pk = UNIT ? (uint32_t)pre[c] : (uint32_t)((unsigned long long)pre[c] >> 32);
+                            if (pk <= nk[c]) {
+                                old[c] = pk;   // no decrease: no atomic
+                            } else if (UNIT) {
                                 old[c] = (uint32_t)atomicMin(&key[w[c]], (KeyW)nk[c]);
                             } else {
                                 const unsigned long long o64 =
@@ -695,13 +707,10 @@ batch_kernel(TreeArgs a) {
                             }
                             npile = min(npile + __popc(pm), a.n);
                         }
-                        if (PLANT) {
-                            int dq = 0;
-                            if (upd[c]) dq = (int)(nk[c] & 1u) - (old[c] == kInf ? 0 : (int)(old[c] & 1u));
-                            ql += __reduce_add_sync(kFull, dq);
-                        }
+                        if (PLANT && upd[c]) dql += (int)(nk[c] & 1u) - (old[c] == kInf ? 0 : (int)(old[c] & 1u));
                     }
                 }
+                if (PLANT) ql += __reduce_add_sync(kFull, dql);
                 __syncwarp();
                 nb = 0;
                 if (PLANT && ql == 0) stop = true;   // plant :95 early exit
@@ -1083,66 +1092,94 @@ window_kernel(TreeArgs a) {
                     return own;
                 };
                 int dql = 0;
-                for (uint32_t t0 = 0; t0 < total; t0 += 32) {
-                    const uint32_t own = owner(t0);
-                    const uint32_t t = t0 + lane;
-                    uint32_t w = 0, nk = 0, old = kInf;
-                    bool upd = false;
-                    if (t < total) {
-                        const uint32_t lo = s_tl[own];
-                        const uint64_t e = s_ba[lo] + (t - s_bx[own]);
-                        uint32_t len, rk;
-                        if (UNIT) {
-                            const uint2 hr = fhead[e];
-                            w = hr.x;
-                            rk = hr.y;
-                            len = 1;
-                        } else {
-                            const uint4 hl = farc[e];
-                            w = hl.x;
-                            len = hl.y;
-                            rk = hl.z;
+                // WC 32-arc chunks per step: their arc loads and atomics are
+                // issued together
+                constexpr int WC = CHL_RELAX_CHUNKS;
+                for (uint32_t t0 = 0; t0 < total; t0 += 32 * WC) {
+                    uint32_t w[WC], nk[WC], old[WC], kxs[WC], len[WC], rk[WC];
+                    bool act[WC], upd[WC];
+#pragma unroll
+                    for (int c = 0; c < WC; ++c) {
+                        w[c] = 0;
+                        nk[c] = 0;
+                        old[c] = kInf;
+                        kxs[c] = 0;
+                        len[c] = 0;
+                        rk[c] = 0;
+                        act[c] = false;
+                        upd[c] = false;
+                    }
+#pragma unroll
+                    for (int c = 0; c < WC; ++c) {
+                        const uint32_t tc = t0 + 32u * c;
+                        const uint32_t own = tc < total ? owner(tc) : 0u;
+                        const uint32_t t = tc + lane;
+                        if (t < total) {
+                            const uint32_t lo = s_tl[own];
+                            const uint64_t e = s_ba[lo] + (t - s_bx[own]);
+                            if (UNIT) {
+                                const uint2 hr = fhead[e];
+                                w[c] = hr.x;
+                                rk[c] = hr.y;
+                                len[c] = 1;
+                            } else {
+                                const uint4 hl = farc[e];
+                                w[c] = hl.x;
+                                len[c] = hl.y;
+                                rk[c] = hl.z;
+                            }
+                            kxs[c] = s_bk[lo];
+                            act[c] = true;
                         }
-                        const uint32_t kx = s_bk[lo];
-                        const uint32_t nv = (!PLANT || ((kx & 1u) && rk >= r)) ? 1u : 0u;
-                        const uint64_t dd64 = (uint64_t)(kx >> 1) + len;
+                    }
+                    uint32_t pre[WC];   // the key before the atomic (keys only decrease)
+#pragma unroll
+                    for (int c = 0; c < WC; ++c) pre[c] = (CHL_RELAX_PRECHECK && act[c]) ? __ldcg(&key[w[c]]) : kInf;
+#pragma unroll
+                    for (int c = 0; c < WC; ++c) {
+                        if (!act[c]) continue;
+                        const uint32_t nv = (!PLANT || ((kxs[c] & 1u) && rk[c] >= r)) ? 1u : 0u;
+                        const uint64_t dd64 = (uint64_t)(kxs[c] >> 1) + len[c];
                         if (dd64 < 0x7FFFFFFFull) {
-                            nk = (uint32_t)dd64 * 2u + nv;
-                            old = atomicMin(&key[w], nk);
-                            upd = nk < old;
+                            nk[c] = (uint32_t)dd64 * 2u + nv;
+                            old[c] = pre[c] <= nk[c] ? pre[c] : atomicMin(&key[w[c]], nk[c]);
+                            upd[c] = nk[c] < old[c];
                         } else {
                             a.ctl->err = 1;   // the reference asserts dd < infty
                         }
                     }
-                    const uint32_t dk = nk >> 1;
-                    const bool fresh = upd && old == kInf;
-                    const bool in_win = upd && dk < thr;
-                    changed |= in_win;
-                    // a new member: first touched inside the window, or a far
-                    // vertex whose key drops into it (its far entry goes stale)
-                    const bool join = in_win && (old == kInf || (old >> 1) >= thr);
-                    const uint32_t jo = append_at(join, &sh.nm);
-                    if (join) {
-                        if (jo < a.n) {
-                            memb[jo] = w;
-                            mkey[jo] = kInf;
-                        } else {
-                            sh.err = 2;
+#pragma unroll
+                    for (int c = 0; c < WC; ++c) {
+                        const uint32_t dk = nk[c] >> 1;
+                        const bool fresh = upd[c] && old[c] == kInf;
+                        const bool in_win = upd[c] && dk < thr;
+                        changed |= in_win;
+                        // a new member: first touched inside the window, or a far
+                        // vertex whose key drops into it (its far entry goes stale)
+                        const bool join = in_win && (old[c] == kInf || (old[c] >> 1) >= thr);
+                        const uint32_t jo = append_at(join, &sh.nm);
+                        if (join) {
+                            if (jo < a.n) {
+                                memb[jo] = w[c];
+                                mkey[jo] = kInf;
+                            } else {
+                                sh.err = 2;
+                            }
                         }
+                        const uint32_t vo = append_at(fresh, &sh.nvis);
+                        if (fresh) {
+                            if (vo < a.n) vis[vo] = w[c];
+                            else sh.err = 2;
+                        }
+                        if (upd[c] && dk >= thr) pmin = min(pmin, dk);
+                        const bool to_far = fresh && dk >= thr;
+                        const uint32_t po = append_at(to_far, &sh.npile);
+                        if (to_far) {
+                            if (po < a.n) pile[po] = w[c];
+                            else sh.err = 2;
+                        }
+                        if (PLANT && upd[c]) dql += (int)(nk[c] & 1u) - (old[c] == kInf ? 0 : (int)(old[c] & 1u));
                     }
-                    const uint32_t vo = append_at(fresh, &sh.nvis);
-                    if (fresh) {
-                        if (vo < a.n) vis[vo] = w;
-                        else sh.err = 2;
-                    }
-                    if (upd && dk >= thr) pmin = min(pmin, dk);
-                    const bool to_far = fresh && dk >= thr;
-                    const uint32_t po = append_at(to_far, &sh.npile);
-                    if (to_far) {
-                        if (po < a.n) pile[po] = w;
-                        else sh.err = 2;
-                    }
-                    if (PLANT && upd) dql += (int)(nk & 1u) - (old == kInf ? 0 : (int)(old & 1u));
                 }
                 if (PLANT) {
                     dql = __reduce_add_sync(kFull, dql);
