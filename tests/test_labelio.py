@@ -125,3 +125,19 @@ def test_binary_load_rejects_malformed(P, tmp_path):
         with pytest.raises(P.CHLError) as e:
             P.Labeling.load(str(q))
         assert e.value.status in (P.CHL_ERR_FORMAT,), what
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(GRAPHS))
+def test_export_paths_agree(P, name):
+    """chl_labels_export of labels in HBM (fetched to host memory by the
+    call) equals a second export of the same, now host-resident, labels."""
+    g = GRAPHS[name](P)
+    order = P.Order.degree(g, seed=3)
+    L = P.build(g, order)
+    first = L.export()
+    L.label(0, 0)                   # fetches the labels to host memory
+    second = L.export()             # expanded on the host
+    for x, y in zip(first, second):
+        assert np.array_equal(x, y)
+    assert int(first[0][-1]) == len(first[1]) == L.total()
